@@ -1,0 +1,212 @@
+/*
+ * sph_gb300.h -- C ABI of the GB300-native Demo4 SPH step.
+ *
+ * One `sph_sim` is one simulation, living on one CUDA device and one CUDA
+ * stream.  The entry points mirror the reference's simulation interface
+ * `BaseSimulation` (NBodySimulation/base.h:8-38) as implemented by
+ * `Demo4::ParticleSimulation` (NBodySimulation/demo4.h:178-267,
+ * demo4.cpp:13-451); each declaration names the reference member it replaces.
+ * Differences a caller must know:
+ *
+ *  - Every function returns an `int` status (SPH_OK or an SPH_ERR_* code);
+ *    the reference returns nothing and asserts or overruns on overflow.
+ *  - Vectors are passed by value as `sph_vec2` instead of `const Vec2f &`.
+ *  - `Render` (base.h:25) has no counterpart: particle data is read with
+ *    `sph_read_particles` (host copy) or `sph_device_arrays` (device
+ *    pointers) instead of handing the AoS array to OpenGL.
+ *  - What the reference fixes at compile time (sph.h:15-72: box size, grid
+ *    cell size, capacities) is the `sph_domain` given to `sph_create`.
+ *  - Multithreading switches are accepted for interface compatibility; the
+ *    step always runs on the GPU.
+ *
+ * Results: one `sph_update` from a given labelled state equals the
+ * reference's single-worker `Update` on the same state (same particle
+ * numbering, same cell arrays, same neighbour lists) to within FP32 rounding
+ * of the summation order; the neighbour structure and cell assignment are
+ * bit-identical.  Between updates the library renumbers particles
+ * (cell-major); `sph_read_particles` returns data in AddParticle order,
+ * `sph_dump_state` in the internal numbering.
+ */
+#ifndef SPH_GB300_H
+#define SPH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define SPH_OK 0
+#define SPH_ERR_INVALID_ARGUMENT 1
+#define SPH_ERR_CAPACITY 2       /* a domain capacity would be exceeded */
+#define SPH_ERR_CUDA 3           /* a CUDA runtime call failed */
+#define SPH_ERR_DEVICE_OVERFLOW 4 /* a kernel flagged a capacity overflow */
+#define SPH_ERR_TIMEOUT 5        /* a bounded device-side wait ran out */
+#define SPH_ERR_NOT_SUPPORTED 6
+#define SPH_ERR_NO_DEVICE 7
+
+typedef struct sph_sim sph_sim;
+
+typedef struct sph_vec2 {
+	float x, y;
+} sph_vec2;
+
+/* The compile-time constants of sph.h:15-72, as runtime values. */
+typedef struct sph_domain {
+	float width;              /* kSPHBoundaryWidth; box centred on the origin */
+	float height;             /* kSPHBoundaryHeight */
+	float cell_size;          /* kSPHGridCellSize; grid = (int)(width/cell) x (int)(height/cell) */
+	uint32_t max_particles;   /* kSPHMaxParticleCount */
+	uint32_t max_cell_particles; /* kSPHMaxCellParticleCount (also the stats seed) */
+	uint32_t max_neighbors;   /* kSPHMaxParticleNeighborCount */
+	float particle_radius;    /* kSPHParticleCollisionRadius */
+	float collision_margin;   /* kSPHCollisionMargin */
+	float jitter_kernel_height; /* kSPHKernelHeight, as the volume/emitter jitter uses it */
+	float jitter_scale;       /* kSPHVolumeParticleDistributionScale */
+} sph_domain;
+
+/* SPHParameters (sph.h:77-86), same member order. */
+typedef struct sph_params {
+	float kernel_height;
+	float cell_size;
+	float particle_spacing;
+	float inv_kernel_height;
+	float rest_density;
+	float stiffness;
+	float near_stiffness;
+	float linear_viscosity;
+	float quadratic_viscosity;
+} sph_params;
+
+/* SPHStatistics (sph.h:125-141); times in milliseconds (device time). */
+typedef struct sph_stats {
+	uint64_t min_particle_neighbor_count;
+	uint64_t max_particle_neighbor_count;
+	uint64_t min_cell_particle_count;
+	uint64_t max_cell_particle_count;
+	float time_emitters;
+	float time_integration;
+	float time_viscosity_forces;
+	float time_predict;
+	float time_update_grid;
+	float time_neighbor_search;
+	float time_density_and_pressure;
+	float time_delta_positions;
+	float time_collisions;
+} sph_stats;
+
+/* The reference's constants (sph.h:18-72) and SPHParameters() (sph.h:88-98). */
+int sph_reference_domain(sph_domain *out);
+int sph_default_params(sph_params *out);
+const char *sph_status_string(int status);
+
+/* Demo4::ParticleSimulation() / ~ParticleSimulation() (demo4.cpp:14-35).
+ * `device` selects the CUDA device; all device memory for `domain` is
+ * allocated here. */
+int sph_create(const sph_domain *domain, int device, sph_sim **out);
+int sph_destroy(sph_sim *sim);
+
+/* BaseSimulation::ResetStats / ClearBodies / ClearParticles / ClearEmitters
+ * (base.h:10-13; demo4.cpp:78-140). */
+int sph_reset_stats(sph_sim *sim);
+int sph_clear_bodies(sph_sim *sim);
+int sph_clear_particles(sph_sim *sim);
+int sph_clear_emitters(sph_sim *sim);
+
+/* BaseSimulation::AddPlane / AddCircle / AddLineSegment / AddPolygon
+ * (base.h:15-18; demo4.cpp:82-123).  At most 100 bodies (kSPHMaxBodyCount),
+ * polygons of at most 8 vertices (kMaxScenarioPolygonCount). */
+int sph_add_plane(sph_sim *sim, sph_vec2 normal, float distance);
+int sph_add_circle(sph_sim *sim, sph_vec2 pos, float radius);
+int sph_add_line_segment(sph_sim *sim, sph_vec2 a, sph_vec2 b);
+int sph_add_polygon(sph_sim *sim, size_t vertex_count, const sph_vec2 *verts);
+
+/* BaseSimulation::AddParticle (base.h:20; demo4.cpp:142-153).  The returned
+ * index is stable for the particle's lifetime (until ClearParticles). */
+int sph_add_particle(sph_sim *sim, sph_vec2 position, sph_vec2 force, size_t *out_index);
+/* `count` AddParticle calls in one transfer; indices first_index.. follow. */
+int sph_add_particles(sph_sim *sim, size_t count, const sph_vec2 *positions, const sph_vec2 *forces,
+                      size_t *first_index);
+/* BaseSimulation::AddVolume (base.h:21; demo4.cpp:169-181).  Jitter draws on
+ * the C library's rand(), as the reference does. */
+int sph_add_volume(sph_sim *sim, sph_vec2 center, sph_vec2 force, int count_x, int count_y, float spacing);
+/* BaseSimulation::AddEmitter (base.h:22; demo4.cpp:155-167). */
+int sph_add_emitter(sph_sim *sim, sph_vec2 position, sph_vec2 direction, float radius, float speed, float rate,
+                    float duration);
+
+/* BaseSimulation::Update (base.h:24; demo4.cpp:286-451).  Asynchronous on
+ * the simulation's stream except where emitters fire; errors flagged by
+ * kernels are reported by the next call that synchronises (sph_get_stats,
+ * sph_read_particles, sph_dump_state, sph_synchronize). */
+int sph_update(sph_sim *sim, float delta_time);
+
+/* BaseSimulation::AddExternalForces / ClearExternalForce (base.h:27-28). */
+int sph_add_external_forces(sph_sim *sim, sph_vec2 force);
+int sph_clear_external_force(sph_sim *sim);
+
+/* BaseSimulation::GetParticleCount / SetGravity / GetParams / GetStats /
+ * SetParams (base.h:30-34). */
+int sph_get_particle_count(sph_sim *sim, size_t *out);
+int sph_set_gravity(sph_sim *sim, sph_vec2 gravity);
+int sph_get_params(sph_sim *sim, sph_params *out);
+int sph_get_stats(sph_sim *sim, sph_stats *out);
+int sph_set_params(sph_sim *sim, const sph_params *params);
+
+/* BaseSimulation::SetMultiThreading / IsMultiThreadingSupported /
+ * IsMultiThreading / GetWorkerThreadCount (base.h:35-38).  Kept for
+ * interface compatibility: the value is stored and reported back. */
+int sph_set_multithreading(sph_sim *sim, int value);
+int sph_is_multithreading_supported(sph_sim *sim, int *out);
+int sph_is_multithreading(sph_sim *sim, int *out);
+int sph_get_worker_thread_count(sph_sim *sim, size_t *out);
+
+/* Replaces the raw AoS pointer Render hands to OpenGL (demo4.cpp:520-531):
+ * copies `count` particles (AddParticle order) to host arrays; any pointer
+ * may be NULL.  dens = (density, nearDensity), press = (pressure,
+ * nearPressure), as in ParticleData (demo4.h:81-109). */
+int sph_read_particles(sph_sim *sim, size_t count, sph_vec2 *pos, sph_vec2 *prev, sph_vec2 *vel, sph_vec2 *acc,
+                       sph_vec2 *dens, sph_vec2 *press);
+
+/* Full state in the internal numbering, for snapshots and teacher forcing.
+ * Particle arrays hold `count` entries each (any pointer may be NULL).
+ * `cell` is the linear cell index y*gx+x of each particle's last grid
+ * insertion (ParticleIndex::cellIndex); `id` its AddParticle index.
+ * Cells: `cell_start`/`cell_count` (gx*gy entries) give each cell's array as
+ * a range of internal numbers for the first `canonical_count` particles;
+ * particles numbered >= canonical_count were added since the last update,
+ * sit at the end of their cell's array in numbering order and have no
+ * neighbour list.  Every particle below canonical_count has the neighbour
+ * list the reference's NeighborSearch (demo4.cpp:183-206) builds from these
+ * cell arrays. */
+typedef struct sph_state_view {
+	size_t count;
+	size_t canonical_count;
+	int grid_x, grid_y;
+	sph_vec2 *pos, *prev, *vel, *acc, *dens, *press;
+	int32_t *id;
+	int32_t *cell;
+	int32_t *cell_start, *cell_count;
+} sph_state_view;
+int sph_state_info(sph_sim *sim, size_t *count, size_t *canonical_count, int *grid_x, int *grid_y);
+int sph_dump_state(sph_sim *sim, const sph_state_view *out);
+/* Inverse of sph_dump_state (all particle pointers and the cell tables are
+ * required).  The cell tables must describe a consistent canonical state. */
+int sph_load_state(sph_sim *sim, const sph_state_view *in);
+
+/* The simulation's CUDA stream (cudaStream_t) and device arrays, for callers
+ * that time on the stream or consume results on the device.  Device arrays
+ * are float2 in the internal numbering and are valid until the next call
+ * that changes the simulation. */
+int sph_get_stream(sph_sim *sim, void **stream);
+int sph_device_arrays(sph_sim *sim, const void **pos, const void **vel, const void **dens, const void **press);
+int sph_synchronize(sph_sim *sim);
+/* Number of kernels this library launched for `sim` since creation. */
+int sph_kernel_launches(sph_sim *sim, uint64_t *out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPH_GB300_H */

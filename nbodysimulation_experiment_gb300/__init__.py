@@ -1,0 +1,25 @@
+"""GB300-native Demo4 SPH step (Clavet-style double-density relaxation).
+
+A drop-in for the data-oriented Demo4 solver of f1nalspace/nbodysimulation_experiment
+(NBodySimulation/demo4.cpp): the same scene, particle, body and parameter
+interface (``BaseSimulation``, NBodySimulation/base.h:8-38), with the step
+computed by hand-written CUDA kernels for sm_103a behind the C ABI of
+``include/sph_gb300.h``.  ``Simulation`` is the Python face of that ABI.
+"""
+from ._build import build, LIB_PATH
+from .simulation import (
+    Domain,
+    Params,
+    SphError,
+    Simulation,
+    Stats,
+    default_params,
+    load_library,
+    reference_domain,
+)
+from . import scenes
+
+__all__ = [
+    "Domain", "Params", "SphError", "Simulation", "Stats", "build", "default_params", "load_library",
+    "reference_domain", "scenes", "LIB_PATH",
+]

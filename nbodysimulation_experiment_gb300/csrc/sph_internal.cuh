@@ -1,0 +1,99 @@
+// Internal device-side declarations shared by the kernels and the host code
+// of the GB300 Demo4 SPH step.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace sphgb {
+
+constexpr int kWarp = 32;
+// Particles staged in shared memory per sweep task: the 3x3 cell block a
+// neighbour list covers.  At least kSPHMaxParticleNeighborCount (1000,
+// sph.h:69), so every scene the reference accepts fits.
+constexpr int kStageCap = 1024;
+// Particles staged per delta-sweep task: the new cells of the task's bounding
+// box grown by one (5x5 cells when particles left the cell in every
+// direction).
+constexpr int kDeltaStageCap = 2048;
+// In-range pairs buffered between the parallel geometry phase and the serial
+// chain of one particle; longer lists are drained in several rounds.
+constexpr int kChainCap = 256;
+// Working array of one cell during the grid update (kSPHMaxCellParticleCount
+// is 500, sph.h:68).
+constexpr int kCellCap = 512;
+// Cells of a delta-sweep staging region (bounding box of a task's new cells,
+// grown by one).  Larger regions fall back to per-particle staging.
+constexpr int kRegionCells = 64;
+constexpr int kMaxBodies = 100;  // kSPHMaxBodyCount, sph.h:71
+constexpr int kMaxPoly = 8;      // kMaxScenarioPolygonCount, sph.h:161
+// Appendix particles (added since the last update) are swept serially in runs
+// of this many consecutive numbers.
+constexpr int kAppendixRun = 32;
+
+// Error bits raised by kernels into SimTables::error.
+enum : uint32_t {
+	kErrStageOverflow = 1u,    // a 3x3 block exceeds the staging capacity
+	kErrCellOverflow = 2u,     // a cell exceeds kCellCap during the grid update
+	kErrTimeout = 4u,          // a bounded wait on another task ran out
+	kErrIndex = 8u,            // an index failed a bounds check (skipped)
+};
+
+enum BodyType : int { kBodyPlane = 1, kBodyCircle = 2, kBodySegment = 3, kBodyPolygon = 4 };
+
+// One collision body (demo4.h:59-120), flattened.
+struct Body {
+	int type;
+	int vertexCount;
+	float ax, ay;  // plane normal | circle centre | segment a
+	float bx, by;  // segment b
+	float r;       // plane distance | circle radius
+	float pad;
+	float verts[2 * kMaxPoly];
+};
+
+// Scalars of one step, prepared on the host in FP32 exactly as the
+// reference computes them.
+struct StepParams {
+	float h2;       // kernelHeight * kernelHeight   (sph.h:470)
+	float invH;     // params.invKernelHeight
+	float rho0, k, kNear, sigma, beta;
+	float dt, invDt, dt2;  // dt, 1/dt (demo4.cpp:287), dt*dt (sph.h:492)
+	float extX, extY;      // gravity + externalForce (demo4.cpp:306)
+	float halfW, halfH, cellSize;  // grid mapping (sph.h:450-463)
+	int gx, gy, ncell;
+	float radius;   // kSPHParticleCollisionRadius
+	float margin;   // kSPHCollisionMargin
+	int nbodies;
+};
+
+// Particle arrays of one buffer set, in the internal numbering.
+struct Particles {
+	float2 *pos, *prev, *vel, *acc, *dens, *press;
+	int *id;      // AddParticle index
+	int *cellOf;  // linear cell of the last grid insertion
+};
+
+// Grid and scheduling tables.  Canonical numbering: the particles of cell c
+// (after the last update) are numbers cellStart[c] .. +cellCount[c]-1, cells
+// in colour-major rank order; numbers >= n0 are the appendix.
+struct SimTables {
+	int *cellStart, *cellCount;        // canonical ranges, by cell id
+	int *rankOfCell, *cellOfRank;
+	int *appCount, *appStart, *appIdx, *appCursor;  // appendix members per cell
+	int *newCell;                      // cell after predict, per particle
+	int *enterCount, *leaveCount, *enterOffset, *enterCursor, *enterList;
+	int *moverList, *moverCount;       // moverCount[0]: movers; [1]: max cell move
+	int *bbox;                         // per cell: x0, y0, x1, y1 of new cells
+	int *newCount, *newStart;
+	int *newIdx;    // new number -> old number (the new cell arrays, concatenated)
+	int *newLabel;  // old number -> new number
+	uint32_t *done;                    // per sweep task
+	int *taskCounter;                  // [0] viscosity, [1] delta
+	uint32_t *stats;                   // minNb, maxNb, minCell, maxCell
+	uint32_t *error;
+	uint32_t *abort;
+	Body *bodies;
+};
+
+}  // namespace sphgb

@@ -1,0 +1,1126 @@
+// CUDA kernels of the GB300-native Demo4 SPH step (sm_103a).
+//
+// One Update (NBodySimulation/demo4.cpp:286-451) runs as:
+//   k_integrate     integrate forces (demo4.cpp:302-309) + per-step resets
+//   k_viscosity     ordered viscosity sweep over the stale neighbour lists
+//                   (demo4.cpp:223-237, sph.h:497-512)
+//   k_predict       prev = x; x += v dt; new cell (demo4.cpp:329-347, sph.h:450-463)
+//   k_scan          prefix sums of the grid update
+//   k_scatter       appendix and mover lists per cell
+//   k_grid_update   the reference's remove/insert grid update, event by event
+//                   (demo4.cpp:341-356, 37-76)
+//   k_density       density and pressure gather (demo4.cpp:208-221, sph.h:465-481)
+//   k_delta         ordered double-density relaxation sweep (demo4.cpp:239-255,
+//                   sph.h:483-495)
+//   k_collide       body collisions + velocity + renumbering (demo4.cpp:411-450)
+//
+// The two pairwise passes of the reference are serial Gauss-Seidel sweeps in
+// particle-number order: a particle's updates land in its neighbours
+// immediately.  They are reproduced exactly by running them as dataflow
+// "sweeps": a task is a run of consecutively numbered particles processed in
+// order by one warp, tasks are claimed in increasing order, and a task first
+// waits (bounded) until every earlier task whose footprint can overlap its own
+// has finished.  Two particles' footprints overlap only when their cells are
+// at most two apart, so with particles numbered cell by cell in a
+// 3x3-colour-major cell order most tasks are independent.  All waits are
+// bounded; a timeout raises kErrTimeout and an abort flag that releases every
+// other wait, so a kernel always terminates.
+//
+// Arithmetic: the library is compiled with --fmad=false and IEEE division and
+// square root, and every expression below follows the reference's operation
+// order, so per-pair results are bit-identical to the reference.
+#include "sph_internal.cuh"
+#include "sph_kernels.cuh"
+
+namespace sphgb {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s per wait
+constexpr uint32_t kWaitLimitIter = 1u << 24;
+
+__device__ __forceinline__ uint64_t global_ns() {
+	uint64_t t;
+	asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+	return t;
+}
+__device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p) {
+	uint32_t v;
+	asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+	return v;
+}
+__device__ __forceinline__ void st_release(uint32_t *p, uint32_t v) {
+	asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned lanemask_lt() {
+	unsigned m;
+	asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+	return m;
+}
+
+// Bounded wait until *flag != 0.  Returns false if the wait gave up.
+__device__ bool wait_done(const uint32_t *flag, uint32_t *abortFlag, uint32_t *err) {
+	if (ld_acquire(flag) != 0u) return true;
+	const uint64_t t0 = global_ns();
+	unsigned ns = 32;
+	for (uint32_t it = 0; it < kWaitLimitIter; ++it) {
+		if (ld_acquire(flag) != 0u) return true;
+		if (ld_acquire(abortFlag) != 0u) return false;
+		if (global_ns() - t0 > kWaitLimitNs) break;
+		__nanosleep(ns);
+		if (ns < 2048) ns <<= 1;
+	}
+	atomicOr(err, kErrTimeout);
+	atomicExch(abortFlag, 1u);
+	return false;
+}
+
+__device__ __forceinline__ int cell_of(float2 p, const StepParams &s) {
+	// SPHComputeCellPos + clamp (sph.h:450-463): IEEE divide, truncation.
+	int x = (int)((p.x + s.halfW) / s.cellSize);
+	int y = (int)((p.y + s.halfH) / s.cellSize);
+	x = min(max(x, 0), s.gx - 1);
+	y = min(max(y, 0), s.gy - 1);
+	return y * s.gx + x;
+}
+
+__device__ __forceinline__ int rect_dist(int ax0, int ay0, int ax1, int ay1, int bx0, int by0, int bx1, int by1) {
+	int dx = max(0, max(ax0 - bx1, bx0 - ax1));
+	int dy = max(0, max(ay0 - by1, by0 - ay1));
+	return max(dx, dy);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Integrate forces (demo4.cpp:302-309) and reset the per-step cell tables.
+__global__ void k_integrate(int n, Particles P, SimTables T, StepParams s) {
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < n) {
+		float2 a = P.acc[i];
+		float2 v = P.vel[i];
+		a.x = s.extX + a.x;  // acceleration += gravity + externalForce
+		a.y = s.extY + a.y;
+		v.x = a.x * s.dt + v.x;  // velocity += acceleration * dt
+		v.y = a.y * s.dt + v.y;
+		P.vel[i] = v;
+		P.acc[i] = make_float2(0.0f, 0.0f);
+	}
+	if (i < s.ncell) {
+		T.enterCount[i] = 0;
+		T.leaveCount[i] = 0;
+		T.enterCursor[i] = 0;
+		T.appCursor[i] = 0;
+		const int cx = i % s.gx, cy = i / s.gx;
+		T.bbox[4 * i + 0] = cx;
+		T.bbox[4 * i + 1] = cy;
+		T.bbox[4 * i + 2] = cx;
+		T.bbox[4 * i + 3] = cy;
+	}
+	if (i == 0) {
+		T.moverCount[0] = 0;
+		T.moverCount[1] = 0;
+	}
+}
+
+// ---------------------------------------------------------------------------
+// Viscosity sweep.  Task t = canonical cell cellOfRank[t]; its particles share
+// one stale neighbour list: the first (list-time) members of the 3x3 block of
+// cells around it, y-major then x, each cell in array order (demo4.cpp:
+// 188-201).  The whole block (positions and velocities) is staged in shared
+// memory, the task's particles are processed in number order, and the block's
+// velocities are written back.  Two tasks conflict iff their cells are at most
+// two apart; every task waits for the earlier conflicting ones.
+
+struct ViscWarp {
+	float2 pos[kStageCap];
+	float2 vel[kStageCap];
+	float4 cand[kChainCap];  // in-range candidates: slot, rx, ry, r2
+	float2 cn[kChainCap];    // unit vector of the pair
+	float comq[kChainCap];   // 1 - q
+	int cslot[kChainCap];
+};
+
+namespace {
+
+// Segment of a flat index among NSEG consecutive segments with start
+// offsets off[] (off[0] == 0); empty segments are skipped.
+template <int NSEG>
+__device__ __forceinline__ int seg_of(int e, const int (&off)[NSEG]) {
+	int q = 0;
+#pragma unroll
+	for (int s = 1; s < NSEG; ++s) q += (e >= off[s]) ? 1 : 0;
+	return q;
+}
+
+// The serial part of the viscosity pass for m buffered pairs, in list order
+// (sph.h:497-512, demo4.cpp:231-234): v_i carries from pair to pair.  Each
+// slot occurs once per list, so the next pairs' velocities may be loaded
+// before this pair's store.
+__device__ __forceinline__ void visc_chain(ViscWarp &S, int m, float2 &vi, const StepParams &s) {
+	int q = 0;
+	for (; q + 4 <= m; q += 4) {
+		int j[4];
+		float2 n[4], vj[4];
+		float o[4];
+#pragma unroll
+		for (int u = 0; u < 4; ++u) {
+			j[u] = S.cslot[q + u];
+			n[u] = S.cn[q + u];
+			o[u] = S.comq[q + u];
+		}
+#pragma unroll
+		for (int u = 0; u < 4; ++u) vj[u] = S.vel[j[u]];
+#pragma unroll
+		for (int u = 0; u < 4; ++u) {
+			const float uu = (vi.x - vj[u].x) * n[u].x + (vi.y - vj[u].y) * n[u].y;
+			if (uu > 0.0f) {
+				const float f = o[u] * (s.sigma * uu + s.beta * (uu * uu));
+				const float ix = (f * n[u].x * 0.5f) * s.dt;
+				const float iy = (f * n[u].y * 0.5f) * s.dt;
+				vi.x = vi.x - ix;
+				vi.y = vi.y - iy;
+				S.vel[j[u]] = make_float2(ix + vj[u].x, iy + vj[u].y);
+			}
+		}
+	}
+	for (; q < m; ++q) {
+		const int j = S.cslot[q];
+		const float2 n = S.cn[q];
+		const float2 vj = S.vel[j];
+		const float uu = (vi.x - vj.x) * n.x + (vi.y - vj.y) * n.y;
+		if (uu > 0.0f) {
+			const float f = S.comq[q] * (s.sigma * uu + s.beta * (uu * uu));
+			const float ix = (f * n.x * 0.5f) * s.dt;
+			const float iy = (f * n.y * 0.5f) * s.dt;
+			vi.x = vi.x - ix;
+			vi.y = vi.y - iy;
+			S.vel[j] = make_float2(ix + vj.x, iy + vj.y);
+		}
+	}
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kViscWarps * kWarp) k_viscosity(Particles P, SimTables T, StepParams s) {
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	ViscWarp &S = reinterpret_cast<ViscWarp *>(smem_raw)[threadIdx.x / kWarp];
+	const int lane = threadIdx.x & (kWarp - 1);
+	const int gx = s.gx, gy = s.gy;
+	for (;;) {
+		int t = 0;
+		if (lane == 0) t = atomicAdd(&T.taskCounter[0], 1);
+		t = __shfl_sync(kFull, t, 0);
+		if (t >= s.ncell) break;
+		const int c = T.cellOfRank[t];
+		const int cnt = T.cellCount[c];
+		if (cnt > 0) {
+			const int cx = c % gx, cy = c / gx;
+			// Wait for earlier tasks within Chebyshev distance 2.
+			if (lane < 25) {
+				const int x = cx + lane % 5 - 2, y = cy + lane / 5 - 2;
+				if (lane != 12 && x >= 0 && x < gx && y >= 0 && y < gy) {
+					const int c2 = y * gx + x;
+					const int r2 = T.rankOfCell[c2];
+					if (r2 < t && T.cellCount[c2] > 0) wait_done(&T.done[r2], T.abort, T.error);
+				}
+			}
+			__syncwarp();
+			// Segments of the 3x3 block in list order.
+			int segStart[9], segOff[9];
+			int L = 0, own = 0;
+#pragma unroll
+			for (int q = 0; q < 9; ++q) {
+				const int x = cx + q % 3 - 1, y = cy + q / 3 - 1;
+				int st = 0, nn = 0;
+				if (x >= 0 && x < gx && y >= 0 && y < gy) {
+					const int c2 = y * gx + x;
+					st = T.cellStart[c2];
+					nn = T.cellCount[c2];
+				}
+				segStart[q] = st;
+				segOff[q] = L;
+				if (q == 4) own = L;
+				L += nn;
+			}
+			if (L > kStageCap) {
+				if (lane == 0) atomicOr(T.error, kErrStageOverflow);
+			} else {
+				for (int base = 0; base < L; base += 4 * kWarp) {
+					float2 xp[4], vp[4];
+#pragma unroll
+					for (int u = 0; u < 4; ++u) {
+						const int e = base + u * kWarp + lane;
+						if (e < L) {
+							const int q = seg_of<9>(e, segOff);
+							const int src = segStart[q] + (e - segOff[q]);
+							xp[u] = __ldcg(&P.pos[src]);
+							vp[u] = __ldcg(&P.vel[src]);
+						}
+					}
+#pragma unroll
+					for (int u = 0; u < 4; ++u) {
+						const int e = base + u * kWarp + lane;
+						if (e < L) {
+							S.pos[e] = xp[u];
+							S.vel[e] = vp[u];
+						}
+					}
+				}
+				__syncwarp();
+				for (int k = 0; k < cnt; ++k) {
+					const int slot = own + k;
+					const float2 xi = S.pos[slot];
+					float2 vi = S.vel[slot];  // meaningful on lane 0 only
+					int m = 0;
+					for (int base = 0; base < L; base += kWarp) {
+						// Cheap test first; the IEEE sqrt and divide run only on
+						// the compacted in-range pairs.
+						const int e = base + lane;
+						bool in = false;
+						float rx = 0.f, ry = 0.f, r2 = 0.f;
+						if (e < L) {
+							const float2 xj = S.pos[e];
+							rx = xj.x - xi.x;
+							ry = xj.y - xi.y;
+							r2 = rx * rx + ry * ry;
+							in = r2 < s.h2;
+						}
+						const unsigned mask = __ballot_sync(kFull, in);
+						if (in) S.cand[m + __popc(mask & lanemask_lt())] = make_float4(__int_as_float(e), rx, ry, r2);
+						m += __popc(mask);
+						if (m > kChainCap - kWarp || base + kWarp >= L) {
+							__syncwarp();
+							for (int q = lane; q < m; q += kWarp) {
+								const float4 cd = S.cand[q];
+								const float r = sqrtf(cd.w);
+								const float qq = r * s.invH;
+								float len = r;  // Vec2Length(Rij) == rij
+								if (len == 0.0f) len = 1.0f;
+								const float inv = 1.0f / len;
+								S.cslot[q] = __float_as_int(cd.x);
+								S.cn[q] = make_float2(cd.y * inv, cd.z * inv);
+								S.comq[q] = 1.0f - qq;
+							}
+							__syncwarp();
+							if (lane == 0) visc_chain(S, m, vi, s);
+							m = 0;
+							__syncwarp();
+						}
+					}
+					if (lane == 0) S.vel[slot] = vi;
+					__syncwarp();
+				}
+				for (int base = 0; base < L; base += kWarp) {
+					const int e = base + lane;
+					if (e < L) {
+						const int q = seg_of<9>(e, segOff);
+						__stcg(&P.vel[segStart[q] + (e - segOff[q])], S.vel[e]);
+					}
+				}
+			}
+			__syncwarp();
+			__threadfence();
+		}
+		__syncwarp();
+		if (lane == 0) st_release(&T.done[t], 1u);
+	}
+}
+
+// ---------------------------------------------------------------------------
+// Predict (demo4.cpp:329-337) and the new cell (demo4.cpp:347).  Movers
+// extend the bounding box of new cells of their old cell, count as leaving
+// their old cell and entering their new cell.
+__global__ void k_predict(int n, Particles P, SimTables T, StepParams s) {
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	const float2 x = P.pos[i];
+	const float2 v = P.vel[i];
+	P.prev[i] = x;
+	const float2 xn = make_float2(v.x * s.dt + x.x, v.y * s.dt + x.y);
+	P.pos[i] = xn;
+	const int nc = cell_of(xn, s);
+	T.newCell[i] = nc;
+	const int oc = P.cellOf[i];
+	if (nc != oc) {
+		atomicAdd(&T.enterCount[nc], 1);
+		atomicAdd(&T.leaveCount[oc], 1);
+		const int nx = nc % s.gx, ny = nc / s.gx;
+		const int ox = oc % s.gx, oy = oc / s.gx;
+		atomicMin(&T.bbox[4 * oc + 0], nx);
+		atomicMin(&T.bbox[4 * oc + 1], ny);
+		atomicMax(&T.bbox[4 * oc + 2], nx);
+		atomicMax(&T.bbox[4 * oc + 3], ny);
+		atomicMax(&T.moverCount[1], max(abs(nx - ox), abs(ny - oy)));
+		atomicAdd(&T.moverCount[0], 1);
+	}
+}
+
+// ---------------------------------------------------------------------------
+// Exclusive scans over cells (single block).  Each thread owns a contiguous
+// run of cells (or ranks), sums it, the block scans the run totals, and each
+// thread writes its run's prefixes.
+__device__ void block_exscan_runs(int ncell, const int *in, const int *order, int *out) {
+	__shared__ int sums[kScanThreads];
+	const int tid = threadIdx.x;
+	const int per = (ncell + kScanThreads - 1) / kScanThreads;
+	const int b = tid * per, e = min(ncell, b + per);
+	int acc = 0;
+	for (int r = b; r < e; ++r) acc += in[order ? order[r] : r];
+	sums[tid] = acc;
+	__syncthreads();
+	for (int off = 1; off < kScanThreads; off <<= 1) {
+		int v = tid >= off ? sums[tid - off] : 0;
+		__syncthreads();
+		sums[tid] += v;
+		__syncthreads();
+	}
+	int run = tid > 0 ? sums[tid - 1] : 0;
+	for (int r = b; r < e; ++r) {
+		const int c = order ? order[r] : r;
+		out[c] = run;
+		run += in[c];
+	}
+	__syncthreads();
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan(SimTables T, StepParams s, uint32_t nbSeed) {
+	const int ncell = s.ncell;
+	for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+		T.newCount[c] = T.cellCount[c] + T.appCount[c] - T.leaveCount[c] + T.enterCount[c];
+	}
+	__syncthreads();
+	block_exscan_runs(ncell, T.appCount, nullptr, T.appStart);
+	block_exscan_runs(ncell, T.enterCount, nullptr, T.enterOffset);
+	block_exscan_runs(ncell, T.newCount, T.cellOfRank, T.newStart);
+	if (threadIdx.x == 0) {
+		// Neighbour-count statistics restart every search (demo4.cpp:369-370).
+		T.stats[0] = nbSeed;
+		T.stats[1] = 0;
+	}
+}
+
+// Appendix members and movers into per-cell lists (order fixed later).
+__global__ void k_scatter(int n, int n0, Particles P, SimTables T) {
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	const int oc = P.cellOf[i];
+	if (i >= n0) {
+		const int slot = T.appStart[oc] + atomicAdd(&T.appCursor[oc], 1);
+		T.appIdx[slot] = i;
+	}
+	const int nc = T.newCell[i];
+	if (nc != oc) {
+		const int slot = T.enterOffset[nc] + atomicAdd(&T.enterCursor[nc], 1);
+		T.enterList[slot] = i;
+	}
+}
+
+// ---------------------------------------------------------------------------
+// Grid update, exactly as the reference's serial loop (demo4.cpp:344-352):
+// particles in number order that changed cell are removed from the old cell
+// by swap-with-last (demo4.cpp:56-76) and appended to the new one
+// (demo4.cpp:37-54).  A cell's final array depends only on the order of its
+// own events, so each warp replays one cell's events in number order.
+
+struct GridWarp {
+	int arr[kCellCap];
+	int leave[kCellCap];
+	int enter[kCellCap];
+};
+
+__device__ void insertion_sort(int *a, int n) {
+	for (int i = 1; i < n; ++i) {
+		const int v = a[i];
+		int j = i - 1;
+		while (j >= 0 && a[j] > v) {
+			a[j + 1] = a[j];
+			--j;
+		}
+		a[j + 1] = v;
+	}
+}
+
+__global__ void __launch_bounds__(kGridWarps * kWarp) k_grid_update(int n, Particles P, Particles Q, SimTables T,
+                                                                      StepParams s) {
+	__shared__ GridWarp W[kGridWarps];
+	GridWarp &S = W[threadIdx.x / kWarp];
+	const int lane = threadIdx.x & (kWarp - 1);
+	const int warpsTotal = gridDim.x * kGridWarps;
+	for (int c = blockIdx.x * kGridWarps + threadIdx.x / kWarp; c < s.ncell; c += warpsTotal) {
+		const int cs = T.cellStart[c], cc = T.cellCount[c];
+		const int as = T.appStart[c], ac = T.appCount[c];
+		const int eo = T.enterOffset[c], ec = T.enterCount[c];
+		const int init = cc + ac;
+		const int outStart = T.newStart[c], outCount = T.newCount[c];
+		if (init == 0 && ec == 0) continue;
+		if (init + ec > kCellCap || outCount > kCellCap) {
+			// Over capacity: keep memory consistent (members in some order)
+			// and report; the result of this update is not meaningful.
+			if (lane == 0) {
+				atomicOr(T.error, kErrCellOverflow);
+				int w = 0;
+				for (int j = 0; j < cc && w < outCount; ++j)
+					if (T.newCell[cs + j] == c) T.newIdx[outStart + w++] = cs + j;
+				for (int j = 0; j < ac && w < outCount; ++j)
+					if (T.newCell[T.appIdx[as + j]] == c) T.newIdx[outStart + w++] = T.appIdx[as + j];
+				for (int j = 0; j < ec && w < outCount; ++j) T.newIdx[outStart + w++] = T.enterList[eo + j];
+				for (; w < outCount; ++w) T.newIdx[outStart + w] = 0;
+				for (int j = 0; j < outCount; ++j) {
+					const int p = T.newIdx[outStart + j];
+					T.newLabel[p] = outStart + j;
+					Q.pos[outStart + j] = P.pos[p];
+				}
+			}
+			__syncwarp();
+			continue;
+		}
+		for (int j = lane; j < cc; j += kWarp) S.arr[j] = cs + j;
+		for (int j = lane; j < ac; j += kWarp) S.arr[cc + j] = T.appIdx[as + j];
+		for (int j = lane; j < ec; j += kWarp) S.enter[j] = T.enterList[eo + j];
+		__syncwarp();
+		if (lane == 0) {
+			// Appendix members joined in number order; entering particles
+			// are applied in number order.
+			insertion_sort(S.arr + cc, ac);
+			insertion_sort(S.enter, ec);
+		}
+		__syncwarp();
+		// Leaving particles, in number order (the array is sorted here).
+		int nl = 0;
+		for (int base = 0; base < init; base += kWarp) {
+			const int j = base + lane;
+			bool lv = false;
+			int p = 0;
+			if (j < init) {
+				p = S.arr[j];
+				lv = T.newCell[p] != c;
+			}
+			const unsigned mask = __ballot_sync(kFull, lv);
+			if (lv) S.leave[nl + __popc(mask & lanemask_lt())] = p;
+			nl += __popc(mask);
+		}
+		__syncwarp();
+		if (lane == 0) {
+			int cnt = init;
+			int lo = 0x7fffffff, hi = 0;
+			int a = 0, b = 0;
+			while (a < nl || b < ec) {
+				if (b >= ec || (a < nl && S.leave[a] < S.enter[b])) {
+					const int p = S.leave[a++];
+					int at = 0;
+					while (at < cnt && S.arr[at] != p) ++at;
+					const int last = cnt - 1;
+					if (at < cnt && at != last) {
+						S.arr[at] = S.arr[last];
+						S.arr[last] = p;
+					}
+					--cnt;
+				} else {
+					S.arr[cnt++] = S.enter[b++];
+				}
+				lo = min(lo, cnt);
+				hi = max(hi, cnt);
+			}
+			if (nl + ec > 0) {
+				atomicMin(&T.stats[2], (uint32_t)lo);
+				atomicMax(&T.stats[3], (uint32_t)hi);
+			}
+			if (cnt != outCount) atomicOr(T.error, kErrIndex);
+		}
+		__syncwarp();
+		// The new cell arrays are the next canonical numbering: the particle
+		// at position j of cell c becomes number newStart[c] + j.  Positions
+		// are gathered into that order for the density and delta passes.
+		for (int j = lane; j < outCount; j += kWarp) {
+			int p = S.arr[j];
+			if (p < 0 || p >= n) {
+				atomicOr(T.error, kErrIndex);
+				p = 0;
+			}
+			T.newIdx[outStart + j] = p;
+			T.newLabel[p] = outStart + j;
+			Q.pos[outStart + j] = P.pos[p];
+		}
+		__syncwarp();
+	}
+}
+
+// ---------------------------------------------------------------------------
+// Density and pressure (demo4.cpp:208-221): a pure gather.  One warp per new
+// cell stages the 3x3 block of the new cell arrays (the particle's neighbour
+// list, demo4.cpp:183-206), then each lane sums its particle's list in order.
+
+struct DensWarp {
+	float2 pos[kStageCap];
+};
+
+__global__ void __launch_bounds__(kDensWarps * kWarp) k_density(int n, Particles Q, SimTables T, StepParams s) {
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	DensWarp &S = reinterpret_cast<DensWarp *>(smem_raw)[threadIdx.x / kWarp];
+	const int lane = threadIdx.x & (kWarp - 1);
+	const int warpsTotal = gridDim.x * kDensWarps;
+	for (int c = blockIdx.x * kDensWarps + threadIdx.x / kWarp; c < s.ncell; c += warpsTotal) {
+		const int cnt = T.newCount[c];
+		if (cnt == 0) continue;
+		const int cx = c % s.gx, cy = c / s.gx;
+		int segStart[9], segOff[9];
+		int L = 0, own = 0;
+#pragma unroll
+		for (int q = 0; q < 9; ++q) {
+			const int x = cx + q % 3 - 1, y = cy + q / 3 - 1;
+			int st = 0, nn = 0;
+			if (x >= 0 && x < s.gx && y >= 0 && y < s.gy) {
+				const int c2 = y * s.gx + x;
+				st = T.newStart[c2];
+				nn = T.newCount[c2];
+			}
+			segStart[q] = st;
+			segOff[q] = L;
+			if (q == 4) own = L;
+			L += nn;
+		}
+		if (lane == 0) {
+			atomicMin(&T.stats[0], (uint32_t)L);
+			atomicMax(&T.stats[1], (uint32_t)L);
+		}
+		if (L > kStageCap) {
+			if (lane == 0) atomicOr(T.error, kErrStageOverflow);
+			continue;
+		}
+		for (int base = 0; base < L; base += 4 * kWarp) {
+			float2 xp[4];
+#pragma unroll
+			for (int u = 0; u < 4; ++u) {
+				const int e = base + u * kWarp + lane;
+				if (e < L) {
+					const int q = seg_of<9>(e, segOff);
+					xp[u] = Q.pos[segStart[q] + (e - segOff[q])];
+				}
+			}
+#pragma unroll
+			for (int u = 0; u < 4; ++u) {
+				const int e = base + u * kWarp + lane;
+				if (e < L) S.pos[e] = xp[u];
+			}
+		}
+		__syncwarp();
+		const int st = T.newStart[c];
+		for (int g = 0; g < cnt; g += kWarp) {
+			const int j = g + lane;
+			if (j < cnt) {
+				const float2 xi = S.pos[own + j];
+				float d0 = 0.0f, d1 = 0.0f;
+				for (int e = 0; e < L; ++e) {
+					const float2 xj = S.pos[e];
+					const float rx = xj.x - xi.x, ry = xj.y - xi.y;
+					const float r2 = rx * rx + ry * ry;
+					if (r2 < s.h2) {
+						const float r = sqrtf(r2);
+						const float term = 1.0f - r * s.invH;
+						d0 = d0 + term * term;
+						d1 = d1 + term * term * term;
+					}
+				}
+				Q.dens[st + j] = make_float2(d0, d1);
+				Q.press[st + j] = make_float2(s.k * (d0 - s.rho0), s.kNear * d1);
+			}
+		}
+		__syncwarp();
+	}
+}
+
+// ---------------------------------------------------------------------------
+// Delta sweep (double-density relaxation, demo4.cpp:239-255).  Tasks in
+// number order: canonical cells in rank order, then the appendix in runs of
+// kAppendixRun consecutive numbers.  A particle's list is the 3x3 block of
+// NEW cells around its new cell.  A task stages the new cells of its
+// bounding box grown by one, processes its particles in order, and writes
+// back only cells inside its particles' 3x3 blocks.  Earlier tasks whose
+// bounding boxes come within two cells are waited for.
+
+struct DeltaWarp {
+	float2 pos[kDeltaStageCap];
+	float4 cand[kChainCap];  // in-range candidates: slot, x_j.x, x_j.y, r2
+	float2 half[kChainCap];  // delta * 0.5 of the buffered pairs, list order
+	int segOff[kRegionCells + 1];
+	int segStart[kRegionCells];
+	int owned[kRegionCells];
+};
+
+namespace {
+
+struct Region {
+	int x0, y0, x1, y1, w, ncells, L;
+};
+
+// Stage the new cells of [x0,x1]x[y0,y1] (row-major) from the positions in
+// new-number order, where each cell is a contiguous range.  Returns false if
+// the region does not fit.
+__device__ bool stage_region(DeltaWarp &S, Region &R, const Particles &Q, const SimTables &T, const StepParams &s,
+                             int lane) {
+	R.w = R.x1 - R.x0 + 1;
+	R.ncells = R.w * (R.y1 - R.y0 + 1);
+	if (R.ncells > kRegionCells) return false;
+	int carry = 0;
+	for (int base = 0; base < R.ncells; base += kWarp) {
+		const int q = base + lane;
+		int nn = 0, st = 0;
+		if (q < R.ncells) {
+			const int c2 = (R.y0 + q / R.w) * s.gx + (R.x0 + q % R.w);
+			nn = T.newCount[c2];
+			st = T.newStart[c2];
+		}
+		int incl = nn;
+#pragma unroll
+		for (int o = 1; o < kWarp; o <<= 1) {
+			const int v = __shfl_up_sync(kFull, incl, o);
+			if (lane >= o) incl += v;
+		}
+		if (q < R.ncells) {
+			S.segOff[q] = carry + incl - nn;
+			S.segStart[q] = st;
+			S.owned[q] = 0;
+		}
+		carry += __shfl_sync(kFull, incl, kWarp - 1);
+	}
+	R.L = carry;
+	if (lane == 0) S.segOff[R.ncells] = carry;
+	__syncwarp();
+	if (carry > kDeltaStageCap) return false;
+	for (int base = 0; base < R.L; base += 4 * kWarp) {
+		float2 xp[4];
+#pragma unroll
+		for (int u = 0; u < 4; ++u) {
+			const int e = base + u * kWarp + lane;
+			if (e < R.L) {
+				int lo = 0, hi = R.ncells;
+				while (hi - lo > 1) {
+					const int mid = (lo + hi) >> 1;
+					if (S.segOff[mid] <= e) lo = mid; else hi = mid;
+				}
+				xp[u] = __ldcg(&Q.pos[S.segStart[lo] + (e - S.segOff[lo])]);
+			}
+		}
+#pragma unroll
+		for (int u = 0; u < 4; ++u) {
+			const int e = base + u * kWarp + lane;
+			if (e < R.L) S.pos[e] = xp[u];
+		}
+	}
+	__syncwarp();
+	return true;
+}
+
+__device__ void write_back_owned(DeltaWarp &S, const Region &R, const Particles &Q, int lane) {
+	for (int q = 0; q < R.ncells; ++q) {
+		if (!S.owned[q]) continue;
+		const int off = S.segOff[q], nn = S.segOff[q + 1] - off, st = S.segStart[q];
+		for (int j = lane; j < nn; j += kWarp) __stcg(&Q.pos[st + j], S.pos[off + j]);
+	}
+}
+
+// Relax one particle k (old number) whose 3x3 block lies inside the staged
+// region (demo4.cpp:240-254, sph.h:483-495).
+__device__ void relax_particle(DeltaWarp &S, const Region &R, int k, const Particles &Q, const SimTables &T,
+                               const StepParams &s, int lane) {
+	const int nc = T.newCell[k];
+	const int jk = T.newLabel[k];
+	const int x = nc % s.gx, y = nc / s.gx;
+	int off[9], lo[9];
+	int L = 0;
+#pragma unroll
+	for (int q = 0; q < 9; ++q) {
+		const int xx = x + q % 3 - 1, yy = y + q / 3 - 1;
+		int o = 0, nn = 0;
+		if (xx >= 0 && xx < s.gx && yy >= 0 && yy < s.gy) {
+			const int rq = (yy - R.y0) * R.w + (xx - R.x0);
+			o = S.segOff[rq];
+			nn = S.segOff[rq + 1] - o;
+			if (lane == q) S.owned[rq] = 1;
+		}
+		off[q] = o;
+		lo[q] = L;
+		L += nn;
+	}
+	const int ownSeg = (y - R.y0) * R.w + (x - R.x0);
+	const int inCell = jk - S.segStart[ownSeg];
+	if (inCell < 0 || inCell >= S.segOff[ownSeg + 1] - S.segOff[ownSeg]) {
+		if (lane == 0) atomicOr(T.error, kErrIndex);
+		__syncwarp();
+		return;
+	}
+	const int own = S.segOff[ownSeg] + inCell;
+	const float2 xk = S.pos[own];
+	const float2 pk = Q.press[jk];
+	float2 dx = make_float2(0.0f, 0.0f);  // lane 0
+	int m = 0;
+	for (int base = 0; base < L; base += kWarp) {
+		const int e = base + lane;
+		bool in = false;
+		int slot = 0;
+		float2 xj = make_float2(0.f, 0.f);
+		float r2 = 0.f;
+		if (e < L) {
+			const int q = seg_of<9>(e, lo);
+			slot = off[q] + (e - lo[q]);
+			xj = S.pos[slot];
+			const float rx = xj.x - xk.x, ry = xj.y - xk.y;
+			r2 = rx * rx + ry * ry;
+			in = r2 < s.h2;
+		}
+		const unsigned mask = __ballot_sync(kFull, in);
+		if (in) S.cand[m + __popc(mask & lanemask_lt())] = make_float4(__int_as_float(slot), xj.x, xj.y, r2);
+		m += __popc(mask);
+		if (m > kChainCap - kWarp || base + kWarp >= L) {
+			__syncwarp();
+			for (int q = lane; q < m; q += kWarp) {
+				const float4 cd = S.cand[q];
+				const float rx = cd.y - xk.x, ry = cd.z - xk.y;
+				const float rij = sqrtf(cd.w);
+				float len = rij;
+				if (len == 0.0f) len = 1.0f;
+				const float inv = 1.0f / len;
+				const float nx = rx * inv, ny = ry * inv;
+				const float term = 1.0f - rij * s.invH;
+				const float d = s.dt2 * (pk.x * term + pk.y * (term * term));
+				const float2 half = make_float2(d * nx * 0.5f, d * ny * 0.5f);
+				S.pos[__float_as_int(cd.x)] = make_float2(half.x + cd.y, half.y + cd.z);
+				S.half[q] = half;
+			}
+			__syncwarp();
+			if (lane == 0) {
+				for (int q = 0; q < m; ++q) {
+					const float2 h = S.half[q];
+					dx.x = dx.x - h.x;
+					dx.y = dx.y - h.y;
+				}
+			}
+			m = 0;
+			__syncwarp();
+		}
+	}
+	if (lane == 0) {
+		const float2 xo = S.pos[own];
+		S.pos[own] = make_float2(dx.x + xo.x, dx.y + xo.y);
+	}
+	__syncwarp();
+}
+
+// Process particles [p0, p1) (old numbers) in order: one staged region if
+// it fits, otherwise one 3x3 region per particle.
+__device__ void relax_group(DeltaWarp &S, int p0, int p1, int bx0, int by0, int bx1, int by1, const Particles &Q,
+                            const SimTables &T, const StepParams &s, int lane) {
+	Region R;
+	R.x0 = max(bx0 - 1, 0);
+	R.y0 = max(by0 - 1, 0);
+	R.x1 = min(bx1 + 1, s.gx - 1);
+	R.y1 = min(by1 + 1, s.gy - 1);
+	if (stage_region(S, R, Q, T, s, lane)) {
+		for (int k = p0; k < p1; ++k) relax_particle(S, R, k, Q, T, s, lane);
+		write_back_owned(S, R, Q, lane);
+		return;
+	}
+	__syncwarp();
+	for (int k = p0; k < p1; ++k) {
+		const int nc = T.newCell[k];
+		const int x = nc % s.gx, y = nc / s.gx;
+		R.x0 = max(x - 1, 0);
+		R.y0 = max(y - 1, 0);
+		R.x1 = min(x + 1, s.gx - 1);
+		R.y1 = min(y + 1, s.gy - 1);
+		if (!stage_region(S, R, Q, T, s, lane)) {
+			if (lane == 0) atomicOr(T.error, kErrStageOverflow);
+			__syncwarp();
+			continue;
+		}
+		relax_particle(S, R, k, Q, T, s, lane);
+		write_back_owned(S, R, Q, lane);
+		__syncwarp();
+	}
+}
+
+// Wait for canonical tasks (old cells) near [bx0,bx1]x[by0,by1] whose
+// new-cell bounding boxes come within two cells of it and whose rank is
+// below `limitRank`.
+__device__ void wait_canonical(int bx0, int by0, int bx1, int by1, int moveMax, int limitRank, int selfCell,
+                               const SimTables &T, const StepParams &s, int lane) {
+	const int rad = 2 + moveMax;
+	const int x0 = max(bx0 - rad, 0), x1 = min(bx1 + rad, s.gx - 1);
+	const int y0 = max(by0 - rad, 0), y1 = min(by1 + rad, s.gy - 1);
+	const int w = x1 - x0 + 1;
+	const int total = w * (y1 - y0 + 1);
+	for (int q = lane; q < total; q += kWarp) {
+		const int c2 = (y0 + q / w) * s.gx + (x0 + q % w);
+		if (c2 == selfCell) continue;
+		const int r2 = T.rankOfCell[c2];
+		if (r2 >= limitRank || T.cellCount[c2] == 0) continue;
+		const int4 b = *reinterpret_cast<const int4 *>(&T.bbox[4 * c2]);
+		if (rect_dist(b.x, b.y, b.z, b.w, bx0, by0, bx1, by1) <= 2) wait_done(&T.done[r2], T.abort, T.error);
+	}
+	__syncwarp();
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kDeltaWarps * kWarp) k_delta(int n, int n0, Particles Q, SimTables T, StepParams s) {
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	DeltaWarp &S = reinterpret_cast<DeltaWarp *>(smem_raw)[threadIdx.x / kWarp];
+	const int lane = threadIdx.x & (kWarp - 1);
+	const int runs = (n - n0 + kAppendixRun - 1) / kAppendixRun;
+	const int ntask = s.ncell + runs;
+	const int moveMax = T.moverCount[1];
+	for (;;) {
+		int t = 0;
+		if (lane == 0) t = atomicAdd(&T.taskCounter[1], 1);
+		t = __shfl_sync(kFull, t, 0);
+		if (t >= ntask) break;
+		if (t < s.ncell) {
+			const int c = T.cellOfRank[t];
+			const int p0 = T.cellStart[c], cnt = T.cellCount[c];
+			if (cnt > 0) {
+				const int4 b = *reinterpret_cast<const int4 *>(&T.bbox[4 * c]);
+				wait_canonical(b.x, b.y, b.z, b.w, moveMax, t, c, T, s, lane);
+				relax_group(S, p0, p0 + cnt, b.x, b.y, b.z, b.w, Q, T, s, lane);
+				__syncwarp();
+				__threadfence();
+			}
+		} else {
+			const int run = t - s.ncell;
+			const int p0 = n0 + run * kAppendixRun;
+			const int p1 = min(n, p0 + kAppendixRun);
+			int bx0 = s.gx, by0 = s.gy, bx1 = -1, by1 = -1;
+			for (int k = p0 + lane; k < p1; k += kWarp) {
+				const int nc = T.newCell[k];
+				bx0 = min(bx0, nc % s.gx);
+				bx1 = max(bx1, nc % s.gx);
+				by0 = min(by0, nc / s.gx);
+				by1 = max(by1, nc / s.gx);
+			}
+			for (int o = 16; o > 0; o >>= 1) {
+				bx0 = min(bx0, __shfl_xor_sync(kFull, bx0, o));
+				by0 = min(by0, __shfl_xor_sync(kFull, by0, o));
+				bx1 = max(bx1, __shfl_xor_sync(kFull, bx1, o));
+				by1 = max(by1, __shfl_xor_sync(kFull, by1, o));
+			}
+			// All canonical tasks precede the appendix; the appendix itself
+			// is swept run after run.
+			wait_canonical(bx0, by0, bx1, by1, moveMax, s.ncell, -1, T, s, lane);
+			if (lane == 0 && run > 0) wait_done(&T.done[t - 1], T.abort, T.error);
+			__syncwarp();
+			relax_group(S, p0, p1, bx0, by0, bx1, by1, Q, T, s, lane);
+			__syncwarp();
+			__threadfence();
+		}
+		__syncwarp();
+		if (lane == 0) st_release(&T.done[t], 1u);
+	}
+}
+
+// ---------------------------------------------------------------------------
+// Collisions (demo4.cpp:411-444, sph.h:514-681), velocity (demo4.cpp:446-450)
+// and the renumbering into canonical order: the particle at position j of
+// new cell c gets number newStart[c] + j.
+
+namespace {
+
+__device__ __forceinline__ float2 v2(float x, float y) { return make_float2(x, y); }
+
+__device__ __forceinline__ float2 normalize2(float2 v) {
+	float len = sqrtf(v.x * v.x + v.y * v.y);
+	if (len == 0.0f) len = 1.0f;
+	const float inv = 1.0f / len;
+	return v2(v.x * inv, v.y * inv);
+}
+
+__device__ void solve_plane(float2 &p, const Body &b, const StepParams &s) {
+	const float2 pp = v2(b.ax * b.r, b.ay * b.r);
+	const float2 d = v2(p.x - pp.x, p.y - pp.y);
+	const float proj = d.x * b.ax + d.y * b.ay;
+	if (proj <= s.radius) {
+		const float pen = s.radius - proj;
+		p = v2(b.ax * pen + p.x, b.ay * pen + p.y);
+	}
+}
+
+__device__ void solve_circle(float2 &p, const Body &b, const StepParams &s) {
+	const float both = b.r + s.radius;
+	const float2 d = v2(p.x - b.ax, p.y - b.ay);
+	const float d2 = d.x * d.x + d.y * d.y;
+	if (d2 <= both * both) {
+		if (fabsf(d2) > 0.0f) {
+			const float dist = sqrtf(d2);
+			const float inv = 1.0f / dist;
+			const float2 nrm = v2(d.x * inv, d.y * inv);
+			const float pen = both - dist;
+			p = v2(nrm.x * pen + p.x, nrm.y * pen + p.y);
+		}
+	}
+}
+
+__device__ void solve_segment(float2 &p, const Body &b, const StepParams &s) {
+	const float both = s.margin + s.radius;
+	const float2 a = v2(b.ax, b.ay), bb = v2(b.bx, b.by);
+	const float2 e = v2(bb.x - a.x, bb.y - a.y);
+	const float u = e.x * (bb.x - p.x) + e.y * (bb.y - p.y);
+	const float v = e.x * (p.x - a.x) + e.y * (p.y - a.y);
+	float2 closest, nrm;
+	if (v <= 0.0f) {
+		closest = a;
+		const float2 d = v2(p.x - closest.x, p.y - closest.y);
+		if (d.x * d.x + d.y * d.y > both * both) return;
+		nrm = normalize2(v2(p.x - closest.x, p.y - closest.y));
+	} else if (u <= 0.0f) {
+		closest = bb;
+		const float2 d = v2(p.x - closest.x, p.y - closest.y);
+		if (d.x * d.x + d.y * d.y > both * both) return;
+		nrm = normalize2(v2(p.x - closest.x, p.y - closest.y));
+	} else {
+		const float den = e.x * e.x + e.y * e.y;
+		const float inv = 1.0f / den;
+		closest = v2((a.x * u + bb.x * v) * inv, (a.y * u + bb.y * v) * inv);
+		const float2 d = v2(p.x - closest.x, p.y - closest.y);
+		if (d.x * d.x + d.y * d.y > both * both) return;
+		nrm = v2(-e.y, e.x);
+		if (nrm.x * (p.x - a.x) + nrm.y * (p.y - a.y) < 0.0f) nrm = v2(-nrm.x, -nrm.y);
+		nrm = normalize2(nrm);
+	}
+	const float2 dp = v2(p.x - closest.x, p.y - closest.y);
+	const float dist = nrm.x * dp.x + nrm.y * dp.y;
+	const float pen = both - dist;
+	p = v2(nrm.x * pen + p.x, nrm.y * pen + p.y);
+}
+
+// FindMTVCirclePolygon + SPHSolvePolygonCollision (sph.h:600-681), keeping
+// the reference's Vec2DistanceSquared, which squares the product of the
+// coordinate differences (vecmath.h:292-296).
+__device__ void solve_polygon(float2 &p, const Body &b, const StepParams &s) {
+	const float radius = s.margin + s.radius;
+	const int n = b.vertexCount;
+	if (n <= 0 || n > kMaxPoly) return;
+	int edge = 0;
+	float2 normal = v2(0.f, 0.f);
+	float separation = -3.40282347e+38f;
+	for (int k = 0; k < n; ++k) {
+		const int k2 = (k + 1) % n;
+		const float2 a = v2(b.verts[2 * k], b.verts[2 * k + 1]);
+		const float2 c = v2(b.verts[2 * k2], b.verts[2 * k2 + 1]);
+		const float2 ab = v2(c.x - a.x, c.y - a.y);
+		const float2 nn = normalize2(v2(1.0f * ab.y, -1.0f * ab.x));
+		const float sep = nn.x * (p.x - a.x) + nn.y * (p.y - a.y);
+		if (sep > radius) return;
+		if (sep > separation) {
+			normal = nn;
+			separation = sep;
+			edge = k;
+		}
+	}
+	const int e2 = (edge + 1) % n;
+	const float2 v1 = v2(b.verts[2 * edge], b.verts[2 * edge + 1]);
+	const float2 v2p = v2(b.verts[2 * e2], b.verts[2 * e2 + 1]);
+	float2 mtv;
+	if (separation < 1.1920929e-07f) {
+		const float pen = radius - separation;
+		mtv = v2(normal.x * pen, normal.y * pen);
+	} else {
+		const float u1 = (p.x - v1.x) * (v2p.x - v1.x) + (p.y - v1.y) * (v2p.y - v1.y);
+		const float u2 = (p.x - v2p.x) * (v1.x - v2p.x) + (p.y - v2p.y) * (v1.y - v2p.y);
+		if (u1 <= 0.0f) {
+			const float f = (v1.x - p.x) * (v1.y - p.y);
+			if (f * f > radius * radius) return;
+			const float2 d = v2(p.x - v1.x, p.y - v1.y);
+			const float2 nn = normalize2(d);
+			const float pen = radius - (nn.x * d.x + nn.y * d.y);
+			mtv = v2(nn.x * pen, nn.y * pen);
+		} else if (u2 <= 0.0f) {
+			const float f = (v2p.x - p.x) * (v2p.y - p.y);
+			if (f * f > radius * radius) return;
+			const float2 d = v2(p.x - v2p.x, p.y - v2p.y);
+			const float2 nn = normalize2(d);
+			const float pen = radius - (nn.x * d.x + nn.y * d.y);
+			mtv = v2(nn.x * pen, nn.y * pen);
+		} else {
+			const float2 mid = v2((1.0f - 0.5f) * v1.x + 0.5f * v2p.x, (1.0f - 0.5f) * v1.y + 0.5f * v2p.y);
+			const float sd = (p.x - mid.x) * normal.x + (p.y - mid.y) * normal.y;
+			if (sd > radius) return;
+			const float pen = radius - sd;
+			mtv = v2(normal.x * pen, normal.y * pen);
+		}
+	}
+	p = v2(mtv.x + p.x, mtv.y + p.y);
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kCollideThreads) k_collide(int n, Particles P, Particles Q, SimTables T, StepParams s) {
+	__shared__ Body bodies[kMaxBodies];
+	for (int b = threadIdx.x; b < s.nbodies; b += blockDim.x) bodies[b] = T.bodies[b];
+	__syncthreads();
+	// j: new number.  Positions, densities and pressures are already in new
+	// order; the rest is gathered from the old number.
+	const int j = blockIdx.x * blockDim.x + threadIdx.x;
+	if (j < s.ncell) T.appCount[j] = 0;
+	if (j >= n) return;
+	float2 x = Q.pos[j];
+	for (int b = 0; b < s.nbodies; ++b) {
+		const Body &bd = bodies[b];
+		switch (bd.type) {
+			case kBodyPlane: solve_plane(x, bd, s); break;
+			case kBodyCircle: solve_circle(x, bd, s); break;
+			case kBodySegment: solve_segment(x, bd, s); break;
+			case kBodyPolygon: solve_polygon(x, bd, s); break;
+			default: break;
+		}
+	}
+	int o = T.newIdx[j];
+	if (o < 0 || o >= n) {
+		atomicOr(T.error, kErrIndex);
+		o = 0;
+	}
+	const float2 pv = P.prev[o];
+	Q.pos[j] = x;
+	Q.prev[j] = pv;
+	Q.vel[j] = make_float2((x.x - pv.x) * s.invDt, (x.y - pv.y) * s.invDt);
+	Q.acc[j] = make_float2(0.0f, 0.0f);
+	Q.id[j] = P.id[o];
+	Q.cellOf[j] = T.newCell[o];
+}
+
+// ---------------------------------------------------------------------------
+// AddParticle (demo4.cpp:142-153) for a batch of numbers [first, first+count):
+// the new particles join the appendix of their cell.
+__global__ void k_add(int first, int count, const float2 *pos, const float2 *force, Particles P, SimTables T,
+                      StepParams s) {
+	const int j = blockIdx.x * blockDim.x + threadIdx.x;
+	if (j >= count) return;
+	const int i = first + j;
+	const float2 x = pos[j];
+	P.pos[i] = x;
+	P.prev[i] = x;
+	P.vel[i] = make_float2(0.f, 0.f);
+	P.acc[i] = force[j];
+	P.dens[i] = make_float2(0.f, 0.f);
+	P.press[i] = make_float2(0.f, 0.f);
+	P.id[i] = i;
+	const int c = cell_of(x, s);
+	P.cellOf[i] = c;
+	const int before = atomicAdd(&T.appCount[c], 1);
+	const uint32_t now = (uint32_t)(T.cellCount[c] + before + 1);
+	atomicMin(&T.stats[2], now);
+	atomicMax(&T.stats[3], now);
+}
+
+// Scatter internal numbering -> AddParticle order for host reads.
+__global__ void k_gather_by_id(int n, const int *id, const float2 *src, float2 *dst) {
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	const int k = id[i];
+	if (k >= 0 && k < n) dst[k] = src[i];
+}
+
+size_t visc_smem_bytes() { return sizeof(ViscWarp) * kViscWarps; }
+size_t delta_smem_bytes() { return sizeof(DeltaWarp) * kDeltaWarps; }
+size_t dens_smem_bytes() { return sizeof(DensWarp) * kDensWarps; }
+
+}  // namespace sphgb

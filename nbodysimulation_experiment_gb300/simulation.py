@@ -1,0 +1,389 @@
+"""Python face of the GB300 Demo4 SPH step, over the C ABI of
+``include/sph_gb300.h``.
+
+``Simulation`` mirrors the reference's ``BaseSimulation`` interface
+(NBodySimulation/base.h:8-38) method by method, in snake_case, with the same
+argument meaning.  The only compute path is the CUDA library
+``libsph_gb300.so``; if it cannot be loaded or no CUDA device is present the
+constructor raises -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Dict, Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import _build
+
+_c = ctypes
+
+SPH_OK = 0
+SPH_ERR_INVALID_ARGUMENT = 1
+SPH_ERR_CAPACITY = 2
+SPH_ERR_CUDA = 3
+SPH_ERR_DEVICE_OVERFLOW = 4
+SPH_ERR_TIMEOUT = 5
+SPH_ERR_NOT_SUPPORTED = 6
+SPH_ERR_NO_DEVICE = 7
+
+
+class Vec2(ctypes.Structure):
+    _fields_ = [("x", _c.c_float), ("y", _c.c_float)]
+
+
+class Domain(ctypes.Structure):
+    """``sph_domain``: the reference's compile-time constants (sph.h:15-72)."""
+
+    _fields_ = [
+        ("width", _c.c_float), ("height", _c.c_float), ("cell_size", _c.c_float),
+        ("max_particles", _c.c_uint32), ("max_cell_particles", _c.c_uint32), ("max_neighbors", _c.c_uint32),
+        ("particle_radius", _c.c_float), ("collision_margin", _c.c_float),
+        ("jitter_kernel_height", _c.c_float), ("jitter_scale", _c.c_float),
+    ]
+
+    def grid(self) -> Tuple[int, int]:
+        w, h, cs = np.float32(self.width), np.float32(self.height), np.float32(self.cell_size)
+        return int(w / cs), int(h / cs)
+
+
+class Params(ctypes.Structure):
+    """``sph_params`` = SPHParameters (sph.h:77-86), same member order."""
+
+    _fields_ = [(name, _c.c_float) for name in (
+        "kernel_height", "cell_size", "particle_spacing", "inv_kernel_height", "rest_density",
+        "stiffness", "near_stiffness", "linear_viscosity", "quadratic_viscosity")]
+
+    def as_array(self) -> np.ndarray:
+        return np.array([getattr(self, f) for f, _ in self._fields_], np.float32)
+
+    @classmethod
+    def from_array(cls, a) -> "Params":
+        p = cls()
+        for (f, _), v in zip(cls._fields_, np.asarray(a, np.float32)):
+            setattr(p, f, float(v))
+        return p
+
+
+class Stats(ctypes.Structure):
+    """``sph_stats`` = SPHStatistics (sph.h:125-141)."""
+
+    _fields_ = [
+        ("min_particle_neighbor_count", _c.c_uint64), ("max_particle_neighbor_count", _c.c_uint64),
+        ("min_cell_particle_count", _c.c_uint64), ("max_cell_particle_count", _c.c_uint64),
+    ] + [(name, _c.c_float) for name in (
+        "time_emitters", "time_integration", "time_viscosity_forces", "time_predict", "time_update_grid",
+        "time_neighbor_search", "time_density_and_pressure", "time_delta_positions", "time_collisions")]
+
+
+class StateView(ctypes.Structure):
+    _fields_ = [
+        ("count", _c.c_size_t), ("canonical_count", _c.c_size_t),
+        ("grid_x", _c.c_int), ("grid_y", _c.c_int),
+        ("pos", _c.c_void_p), ("prev", _c.c_void_p), ("vel", _c.c_void_p), ("acc", _c.c_void_p),
+        ("dens", _c.c_void_p), ("press", _c.c_void_p),
+        ("id", _c.c_void_p), ("cell", _c.c_void_p), ("cell_start", _c.c_void_p), ("cell_count", _c.c_void_p),
+    ]
+
+
+class SphError(RuntimeError):
+    def __init__(self, status: int, what: str):
+        self.status = status
+        super().__init__("%s failed: %s (status %d)" % (what, _status_string(status), status))
+
+
+_LIB = None
+
+
+def _status_string(status: int) -> str:
+    if _LIB is None:
+        return "status"
+    return _LIB.sph_status_string(status).decode()
+
+
+def library_path() -> str:
+    return _build.LIB_PATH
+
+
+def load_library(build_if_missing: bool = True):
+    """Load ``libsph_gb300.so`` (building it first if allowed)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.LIB_PATH
+    if not os.path.exists(path) or not _build.up_to_date():
+        if not build_if_missing:
+            raise FileNotFoundError(path)
+        _build.build()
+    lib = ctypes.CDLL(path)
+    P = _c.POINTER
+    vp = _c.c_void_p
+    sig = {
+        "sph_reference_domain": [P(Domain)],
+        "sph_default_params": [P(Params)],
+        "sph_create": [P(Domain), _c.c_int, P(vp)],
+        "sph_destroy": [vp],
+        "sph_reset_stats": [vp],
+        "sph_clear_bodies": [vp],
+        "sph_clear_particles": [vp],
+        "sph_clear_emitters": [vp],
+        "sph_add_plane": [vp, Vec2, _c.c_float],
+        "sph_add_circle": [vp, Vec2, _c.c_float],
+        "sph_add_line_segment": [vp, Vec2, Vec2],
+        "sph_add_polygon": [vp, _c.c_size_t, vp],
+        "sph_add_particle": [vp, Vec2, Vec2, P(_c.c_size_t)],
+        "sph_add_particles": [vp, _c.c_size_t, vp, vp, P(_c.c_size_t)],
+        "sph_add_volume": [vp, Vec2, Vec2, _c.c_int, _c.c_int, _c.c_float],
+        "sph_add_emitter": [vp, Vec2, Vec2, _c.c_float, _c.c_float, _c.c_float, _c.c_float],
+        "sph_update": [vp, _c.c_float],
+        "sph_add_external_forces": [vp, Vec2],
+        "sph_clear_external_force": [vp],
+        "sph_get_particle_count": [vp, P(_c.c_size_t)],
+        "sph_set_gravity": [vp, Vec2],
+        "sph_get_params": [vp, P(Params)],
+        "sph_get_stats": [vp, P(Stats)],
+        "sph_set_params": [vp, P(Params)],
+        "sph_set_multithreading": [vp, _c.c_int],
+        "sph_is_multithreading_supported": [vp, P(_c.c_int)],
+        "sph_is_multithreading": [vp, P(_c.c_int)],
+        "sph_get_worker_thread_count": [vp, P(_c.c_size_t)],
+        "sph_read_particles": [vp, _c.c_size_t, vp, vp, vp, vp, vp, vp],
+        "sph_state_info": [vp, P(_c.c_size_t), P(_c.c_size_t), P(_c.c_int), P(_c.c_int)],
+        "sph_dump_state": [vp, P(StateView)],
+        "sph_load_state": [vp, P(StateView)],
+        "sph_get_stream": [vp, P(vp)],
+        "sph_device_arrays": [vp, P(vp), P(vp), P(vp), P(vp)],
+        "sph_synchronize": [vp],
+        "sph_kernel_launches": [vp, P(_c.c_uint64)],
+    }
+    for name, args in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = _c.c_int
+    lib.sph_status_string.argtypes = [_c.c_int]
+    lib.sph_status_string.restype = _c.c_char_p
+    _LIB = lib
+    return lib
+
+
+#: Exported C symbols, in the order include/sph_gb300.h declares them.
+C_SYMBOLS = (
+    "sph_reference_domain", "sph_default_params", "sph_status_string", "sph_create", "sph_destroy",
+    "sph_reset_stats", "sph_clear_bodies", "sph_clear_particles", "sph_clear_emitters", "sph_add_plane",
+    "sph_add_circle", "sph_add_line_segment", "sph_add_polygon", "sph_add_particle", "sph_add_particles",
+    "sph_add_volume", "sph_add_emitter", "sph_update", "sph_add_external_forces", "sph_clear_external_force",
+    "sph_get_particle_count", "sph_set_gravity", "sph_get_params", "sph_get_stats", "sph_set_params",
+    "sph_set_multithreading", "sph_is_multithreading_supported", "sph_is_multithreading",
+    "sph_get_worker_thread_count", "sph_read_particles", "sph_state_info", "sph_dump_state", "sph_load_state",
+    "sph_get_stream", "sph_device_arrays", "sph_synchronize", "sph_kernel_launches",
+)
+
+
+def _check(status: int, what: str) -> None:
+    if status != SPH_OK:
+        raise SphError(status, what)
+
+
+def reference_domain() -> Domain:
+    d = Domain()
+    _check(load_library().sph_reference_domain(_c.byref(d)), "sph_reference_domain")
+    return d
+
+
+def default_params() -> Params:
+    p = Params()
+    _check(load_library().sph_default_params(_c.byref(p)), "sph_default_params")
+    return p
+
+
+def _v(x, y) -> Vec2:
+    return Vec2(float(x), float(y))
+
+
+def _f2(a: np.ndarray) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float32).reshape(-1, 2)
+
+
+class Simulation:
+    """GB300 Demo4 particle simulation (``BaseSimulation``, base.h:8-38)."""
+
+    def __init__(self, domain: Optional[Domain] = None, device: int = 0):
+        self._lib = load_library()
+        self.domain = domain if domain is not None else reference_domain()
+        h = _c.c_void_p()
+        _check(self._lib.sph_create(_c.byref(self.domain), int(device), _c.byref(h)), "sph_create")
+        self._h = h
+        self.grid = self.domain.grid()
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.sph_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _call(self, name: str, *args) -> None:
+        _check(getattr(self._lib, name)(self._h, *args), name)
+
+    # --- BaseSimulation ------------------------------------------------------
+    def reset_stats(self):
+        self._call("sph_reset_stats")
+
+    def clear_bodies(self):
+        self._call("sph_clear_bodies")
+
+    def clear_particles(self):
+        self._call("sph_clear_particles")
+
+    def clear_emitters(self):
+        self._call("sph_clear_emitters")
+
+    def add_plane(self, normal, distance):
+        self._call("sph_add_plane", _v(*normal), float(distance))
+
+    def add_circle(self, pos, radius):
+        self._call("sph_add_circle", _v(*pos), float(radius))
+
+    def add_line_segment(self, a, b):
+        self._call("sph_add_line_segment", _v(*a), _v(*b))
+
+    def add_polygon(self, verts):
+        v = _f2(verts)
+        self._call("sph_add_polygon", len(v), v.ctypes.data_as(_c.c_void_p))
+
+    def add_particle(self, position, force=(0.0, 0.0)) -> int:
+        out = _c.c_size_t()
+        self._call("sph_add_particle", _v(*position), _v(*force), _c.byref(out))
+        return out.value
+
+    def add_particles(self, positions, forces=None) -> int:
+        p = _f2(positions)
+        f = _f2(forces) if forces is not None else None
+        first = _c.c_size_t()
+        self._call("sph_add_particles", len(p), p.ctypes.data_as(_c.c_void_p),
+                   f.ctypes.data_as(_c.c_void_p) if f is not None else None, _c.byref(first))
+        return first.value
+
+    def add_volume(self, center, force, count_x, count_y, spacing):
+        self._call("sph_add_volume", _v(*center), _v(*force), int(count_x), int(count_y), float(spacing))
+
+    def add_emitter(self, position, direction, radius, speed, rate, duration):
+        self._call("sph_add_emitter", _v(*position), _v(*direction), float(radius), float(speed), float(rate),
+                   float(duration))
+
+    def update(self, delta_time: float):
+        self._call("sph_update", float(np.float32(delta_time)))
+
+    def add_external_forces(self, force):
+        self._call("sph_add_external_forces", _v(*force))
+
+    def clear_external_force(self):
+        self._call("sph_clear_external_force")
+
+    def get_particle_count(self) -> int:
+        out = _c.c_size_t()
+        self._call("sph_get_particle_count", _c.byref(out))
+        return out.value
+
+    def set_gravity(self, gravity):
+        self._call("sph_set_gravity", _v(*gravity))
+
+    def get_params(self) -> Params:
+        p = Params()
+        self._call("sph_get_params", _c.byref(p))
+        return p
+
+    def set_params(self, params: Params):
+        self._call("sph_set_params", _c.byref(params))
+
+    def get_stats(self) -> Stats:
+        s = Stats()
+        self._call("sph_get_stats", _c.byref(s))
+        return s
+
+    def set_multithreading(self, value: bool):
+        self._call("sph_set_multithreading", 1 if value else 0)
+
+    def is_multithreading_supported(self) -> bool:
+        out = _c.c_int()
+        self._call("sph_is_multithreading_supported", _c.byref(out))
+        return bool(out.value)
+
+    def is_multithreading(self) -> bool:
+        out = _c.c_int()
+        self._call("sph_is_multithreading", _c.byref(out))
+        return bool(out.value)
+
+    def get_worker_thread_count(self) -> int:
+        out = _c.c_size_t()
+        self._call("sph_get_worker_thread_count", _c.byref(out))
+        return out.value
+
+    # --- data access ------------------------------------------------------------
+    def read_particles(self, fields: Sequence[str] = ("pos", "prev", "vel", "acc", "dens", "press")
+                       ) -> Dict[str, np.ndarray]:
+        """Particle arrays in AddParticle order, as (n, 2) float32 arrays."""
+        n = self.get_particle_count()
+        out = {f: np.zeros((n, 2), np.float32) for f in fields}
+        ptr = lambda f: out[f].ctypes.data_as(_c.c_void_p) if f in out else None
+        self._call("sph_read_particles", n, ptr("pos"), ptr("prev"), ptr("vel"), ptr("acc"), ptr("dens"),
+                   ptr("press"))
+        return out
+
+    def state_info(self) -> Tuple[int, int, int, int]:
+        n, n0 = _c.c_size_t(), _c.c_size_t()
+        gx, gy = _c.c_int(), _c.c_int()
+        self._call("sph_state_info", _c.byref(n), _c.byref(n0), _c.byref(gx), _c.byref(gy))
+        return n.value, n0.value, gx.value, gy.value
+
+    def dump_state(self) -> Dict[str, np.ndarray]:
+        """Full state in the internal numbering (see sph_dump_state)."""
+        n, n0, gx, gy = self.state_info()
+        st = {k: np.zeros((n, 2), np.float32) for k in ("pos", "prev", "vel", "acc", "dens", "press")}
+        st["id"] = np.zeros(n, np.int32)
+        st["cell"] = np.zeros(n, np.int32)
+        st["cell_start"] = np.zeros(gx * gy, np.int32)
+        st["cell_count"] = np.zeros(gx * gy, np.int32)
+        v = StateView(count=n, canonical_count=n0, grid_x=gx, grid_y=gy)
+        for k in ("pos", "prev", "vel", "acc", "dens", "press", "id", "cell", "cell_start", "cell_count"):
+            setattr(v, k, st[k].ctypes.data)
+        self._call("sph_dump_state", _c.byref(v))
+        st["canonical_count"] = n0
+        st["grid"] = (gx, gy)
+        return st
+
+    def load_state(self, st: Dict[str, np.ndarray]) -> None:
+        n = len(st["pos"])
+        gx, gy = self.grid
+        arrs = {k: np.ascontiguousarray(st[k], np.float32).reshape(-1, 2)
+                for k in ("pos", "prev", "vel", "acc", "dens", "press")}
+        for k in ("id", "cell", "cell_start", "cell_count"):
+            arrs[k] = np.ascontiguousarray(st[k], np.int32)
+        v = StateView(count=n, canonical_count=int(st["canonical_count"]), grid_x=gx, grid_y=gy)
+        for k, a in arrs.items():
+            setattr(v, k, a.ctypes.data)
+        self._call("sph_load_state", _c.byref(v))
+
+    def stream(self) -> int:
+        out = _c.c_void_p()
+        self._call("sph_get_stream", _c.byref(out))
+        return out.value or 0
+
+    def synchronize(self):
+        self._call("sph_synchronize")
+
+    def kernel_launches(self) -> int:
+        out = _c.c_uint64()
+        self._call("sph_kernel_launches", _c.byref(out))
+        return out.value
