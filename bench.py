@@ -1,0 +1,324 @@
+"""Benchmark of the GB300 Demo4 SPH step (one JSON line on rank 0).
+
+Workload (one "step" = one ``Update`` of the whole scene): ``obstacles_65536``
+-- a 256x256 jittered block (65,536 particles, spacing h/6) in a 51.2 x 28.8
+box with four walls, eight seeded circles (radii 2h..6h) and four seeded line
+segments, gravity (0, -10), the reference's sph.h constants, FP32.
+
+* ``value``: particle-steps/s with the scene resident in HBM; each timed step
+  is bracketed by CUDA events on the simulation's stream, and L2 is flushed
+  (a 256 MiB write) between steps, outside the events.
+* ``e2e``: the same metric through the C ABI with host buffers: every step
+  loads the full state from pinned host memory (``sph_load_state``), updates
+  and reads the full state back (``sph_dump_state``).
+* ``roofline``: the dominant kernel (the ordered delta sweep) against the
+  measured HBM copy bandwidth; achieved = algorithmic bytes (24 B per
+  particle: read position and pressure, write position) / its event-timed
+  duration.
+* ``cpu_baseline``: the CPU restatement of the reference step (oracle/),
+  multithreaded like the reference's ThreadPool on all host cores, on a
+  bounded sample of the same workload.
+
+``--impl reference`` times that CPU implementation alone (rank 0 only).
+Multi-GPU runs are independent replicas (the step does not shard).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s (1 GB300) plain vs batched vs learned at stated density error"
+UNIT = "particle-steps/s"
+DELTA_BYTES_PER_PARTICLE = 24  # read pos 8 + pressure 8, write pos 8
+WORKLOAD = ("obstacles_65536: 65,536-particle jittered block (spacing h/6) in a 51.2 x 28.8 box, "
+            "4 walls + 8 circles + 4 segments, plain Demo4 step (viscosity on, springs off), FP32")
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic(n_particles: int):
+    """DRAM bytes per launch of the delta sweep from the committed ncu
+    summary (captured on a smaller case, scaled by particle count)."""
+    path = os.path.join(ROOT, "profiles", "k_delta_traffic.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["dram_bytes_per_particle"]) * n_particles
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(scene, state_gpu, steps: int, workers: int):
+    """Time the CPU restatement (multithreaded like the reference) on a
+    bounded sample: `steps` updates from the GPU's mid-run state."""
+    from oracle.oracle import OracleSim
+    from oracle import state as ostate
+    orc = OracleSim(scene.oracle_domain(OracleSim), fp64=False, workers=workers)
+    scene.apply(orc)
+    orc.set_state(ostate.to_reference_state(state_gpu))
+    orc.update(float(scene_dt()))  # warm the pool and caches
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        orc.update(float(scene_dt()))
+    dt = time.perf_counter() - t0
+    orc.close()
+    return scene.n * steps / dt, dt
+
+
+def scene_dt():
+    from nbodysimulation_experiment_gb300 import scenes
+    return scenes.DT
+
+
+def run_reference_arm(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from nbodysimulation_experiment_gb300 import scenes
+    from oracle.oracle import OracleSim, build as build_oracle
+    build_oracle(reference=True)
+    scene = scenes.obstacles_65536()
+    workers = OracleSim.hardware_threads()
+    orc = OracleSim(scene.oracle_domain(OracleSim), fp64=False, workers=workers)
+    scene.apply(orc)
+    orc.update(float(scenes.DT))  # first update (AddParticle order)
+    per = max(1, args.cpu_steps // max(1, args.steps))
+    for _ in range(args.warmup):
+        orc.update(float(scenes.DT))
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        for _ in range(per):
+            orc.update(float(scenes.DT))
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = scene.n * per * args.steps / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / (per * args.steps),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)", "config": {"workload": WORKLOAD, "particles": scene.n},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": workers, "kind": "port",
+                         "sample": "%d updates of the %d-particle scene per step, %d steps, after %d warm-up "
+                                   "updates" % (per, scene.n, args.steps, args.warmup + 1)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-steps", type=int, default=60, help="CPU-baseline sample size in updates")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    if args.impl == "reference":
+        return run_reference_arm(args)
+
+    import torch
+    import torch.distributed as dist
+    import nbodysimulation_experiment_gb300 as pkg
+    from nbodysimulation_experiment_gb300 import scenes
+
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    pkg.build()
+
+    scene = scenes.obstacles_65536()
+    sim = pkg.Simulation(scene.domain(), device=local)
+    scene.apply(sim)
+    dt = float(scenes.DT)
+    stream = torch.cuda.ExternalStream(sim.stream())
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    for _ in range(args.warmup):
+        sim.update(dt)
+    sim.synchronize()
+
+    # --- device-resident timed region -------------------------------------
+    launches0 = sim.kernel_launches()
+    sampler = ClockSampler(local)
+    sampler.start()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    step_ms, delta_ms = [], []
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        sim.update(dt)
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        delta_ms.append(sim.get_stats().time_delta_positions)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clocks = sampler.stop()
+    launches = sim.kernel_launches() - launches0 - 0  # get_stats launches nothing
+    total_s = sum(step_ms) / 1e3
+    if world > 1:
+        t = torch.tensor([total_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+    value = scene.n * args.steps * world / total_s
+
+    # density deviation from the rest density at the end of the run
+    rd = sim.read_particles(("dens",))
+    rho0 = float(scene.params[4])
+    dens_err = float(np.mean(np.abs(rd["dens"][:, 0] - rho0)) / rho0)
+
+    # --- end to end through the C ABI with host buffers --------------------
+    st = sim.dump_state()
+    pinned = {}
+    for k in ("pos", "prev", "vel", "acc", "dens", "press", "id", "cell", "cell_start", "cell_count"):
+        a = st[k]
+        t = torch.empty(a.shape, dtype=torch.float32 if a.dtype == np.float32 else torch.int32, pin_memory=True)
+        arr = t.numpy()
+        arr[...] = a
+        pinned[k] = arr
+    pinned["canonical_count"] = st["canonical_count"]
+    pinned["grid"] = st["grid"]
+    e2e_steps = max(10, args.steps // 4)
+    h2d = sum(pinned[k].nbytes for k in ("pos", "prev", "vel", "acc", "dens", "press", "id", "cell",
+                                        "cell_start", "cell_count"))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sim.load_state(pinned)
+        sim.update(dt)
+        out = sim.dump_state()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = scene.n * e2e_steps * world / e2e_s
+
+    hbm, peak_kind = measured_peaks()
+    mean_delta_s = statistics.mean(delta_ms) / 1e3
+    achieved = DELTA_BYTES_PER_PARTICLE * scene.n / mean_delta_s / 1e9
+    traffic = profile_traffic(scene.n)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        from oracle.oracle import OracleSim, build as build_oracle
+        build_oracle(reference=False)
+        workers = OracleSim.hardware_threads()
+        cval, csec = cpu_baseline(scene, st, args.cpu_steps, workers)
+        cpu = {"value": cval, "unit": UNIT, "cores": workers, "kind": "port",
+               "sample": "%d updates of the %d-particle scene from the GPU's state after %d updates "
+                         "(%.1f s)" % (args.cpu_steps, scene.n, args.warmup, csec)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "particles": scene.n, "l2": "flushed between steps (256 MiB write)",
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "density_error": dens_err},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(h2d)},
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "kernel": "k_delta", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": traffic,
+                         "algorithmic_bytes": DELTA_BYTES_PER_PARTICLE * scene.n,
+                         "kernel_ms": 1e3 * mean_delta_s},
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    sim.close()
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -89,6 +89,7 @@ struct sph_sim {
 	float emitterMs = 0.0f;
 	uint64_t launches = 0;
 	int stickyError = SPH_OK;
+	unsigned long long *prof = nullptr;
 
 	uint32_t maxNbSeed() const { return dom.max_neighbors; }
 };
@@ -140,6 +141,8 @@ StepParams step_params(const sph_sim *s, float dt) {
 
 SimTables tables(sph_sim *s) {
 	SimTables t = s->T;
+	t.prof = s->prof;
+	t.profStride = s->prof ? (int)s->doneDCap : 0;
 	t.cellStart = s->cellStartA;
 	t.cellCount = s->cellCountA;
 	t.newStart = s->cellStartB;
@@ -515,7 +518,7 @@ int sph_destroy(sph_sim *s) {
 	                T.appCount,    T.appStart,    T.appIdx,      T.appCursor,   T.newCell,     T.enterCount,
 	                T.leaveCount,  T.enterOffset, T.enterCursor, T.enterList,   T.moverCount,  T.bbox,
 	                T.newIdx,      T.newLabel, T.taskCounter, T.stats,      T.error,       T.abort,
-	                T.bodies,      s->doneV,      s->doneD,      s->stagePos,   s->stageForce};
+	                T.bodies,      s->doneV,      s->doneD,      s->stagePos,   s->stageForce, s->prof};
 	for (void *p : ptrs)
 		if (p) cudaFree(p);
 	if (s->hostPos) cudaFreeHost(s->hostPos);
@@ -915,6 +918,30 @@ int sph_synchronize(sph_sim *s) {
 	int rc = flush_adds(s);
 	if (rc) return rc;
 	return check_device_errors(s);
+}
+
+// Diagnostics (not part of the reference interface): per-task timestamps of
+// the two ordered sweeps of the next updates.
+extern "C" int sph_profile_tasks(sph_sim *s, int enable) {
+	if (!s) return SPH_ERR_INVALID_ARGUMENT;
+	if (enable && !s->prof) {
+		SPH_CUDA(cudaMalloc(&s->prof, sizeof(unsigned long long) * 8 * s->doneDCap));
+		SPH_CUDA(cudaMemset(s->prof, 0, sizeof(unsigned long long) * 8 * s->doneDCap));
+	} else if (!enable && s->prof) {
+		cudaFree(s->prof);
+		s->prof = nullptr;
+	}
+	return SPH_OK;
+}
+
+extern "C" int sph_profile_read(sph_sim *s, unsigned long long *out, size_t capacity, size_t *stride) {
+	if (!s || !stride) return SPH_ERR_INVALID_ARGUMENT;
+	*stride = s->doneDCap;
+	if (!s->prof || !out) return SPH_OK;
+	const size_t total = std::min(capacity, (size_t)8 * s->doneDCap);
+	SPH_CUDA(cudaStreamSynchronize(s->stream));
+	SPH_CUDA(cudaMemcpy(out, s->prof, total * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+	return SPH_OK;
 }
 
 int sph_kernel_launches(sph_sim *s, uint64_t *out) {

@@ -19,6 +19,8 @@ constexpr int kDeltaStageCap = 2048;
 // In-range pairs buffered between the parallel geometry phase and the serial
 // chain of one particle; longer lists are drained in several rounds.
 constexpr int kChainCap = 256;
+// Per-particle inputs of the delta sweep prefetched per chunk of a task.
+constexpr int kPrefetch = 128;
 // Working array of one cell during the grid update (kSPHMaxCellParticleCount
 // is 500, sph.h:68).
 constexpr int kCellCap = 512;
@@ -94,6 +96,10 @@ struct SimTables {
 	uint32_t *error;
 	uint32_t *abort;
 	Body *bodies;
+	// Diagnostics: when non-null, sweep tasks record %globaltimer stamps
+	// (claimed, dependencies met, staged, done) at prof[(sweep * profStride + task) * 4].
+	unsigned long long *prof;
+	int profStride;
 };
 
 }  // namespace sphgb

@@ -69,11 +69,16 @@ __device__ bool wait_done(const uint32_t *flag, uint32_t *abortFlag, uint32_t *e
 		if (ld_acquire(abortFlag) != 0u) return false;
 		if (global_ns() - t0 > kWaitLimitNs) break;
 		__nanosleep(ns);
-		if (ns < 2048) ns <<= 1;
+		if (ns < 256) ns <<= 1;
 	}
 	atomicOr(err, kErrTimeout);
 	atomicExch(abortFlag, 1u);
 	return false;
+}
+
+__device__ __forceinline__ void stamp(const SimTables &T, int sweep, int task, int slot, int lane) {
+	if (T.prof != nullptr && lane == 0 && task < T.profStride)
+		T.prof[((size_t)sweep * T.profStride + task) * 4 + slot] = global_ns();
 }
 
 __device__ __forceinline__ int cell_of(float2 p, const StepParams &s) {
@@ -144,21 +149,39 @@ struct ViscWarp {
 
 namespace {
 
-// Segment of a flat index among NSEG consecutive segments with start
-// offsets off[] (off[0] == 0); empty segments are skipped.
+// Source index of flat position e of NSEG consecutive segments (segment s
+// starts at flat offset off[s] and at source index start[s]); selects only,
+// so the arrays stay in registers.
 template <int NSEG>
-__device__ __forceinline__ int seg_of(int e, const int (&off)[NSEG]) {
-	int q = 0;
+__device__ __forceinline__ int seg_src(int e, const int (&off)[NSEG], const int (&start)[NSEG]) {
+	int src = start[0] + e;
 #pragma unroll
-	for (int s = 1; s < NSEG; ++s) q += (e >= off[s]) ? 1 : 0;
-	return q;
+	for (int q = 1; q < NSEG; ++q) src = (e >= off[q]) ? start[q] + (e - off[q]) : src;
+	return src;
 }
 
 // The serial part of the viscosity pass for m buffered pairs, in list order
 // (sph.h:497-512, demo4.cpp:231-234): v_i carries from pair to pair.  Each
 // slot occurs once per list, so the next pairs' velocities may be loaded
-// before this pair's store.
+// before this pair's store.  The impulse (f n * 0.5) * dt is computed as
+// (f n) * (0.5 dt): 0.5 dt is exact and halving is exact, so both round the
+// same real product once (unless |f n| < 2^-125).
+__device__ __forceinline__ void visc_pair(ViscWarp &S, int j, float2 n, float o, float2 vj, float2 &vi,
+                                          const StepParams &s, float hdt) {
+	// Computed unconditionally and selected: only approaching pairs (u > 0)
+	// exchange an impulse.
+	const float uu = (vi.x - vj.x) * n.x + (vi.y - vj.y) * n.y;
+	const float f = o * (s.sigma * uu + s.beta * (uu * uu));
+	const float ix = (f * n.x) * hdt;
+	const float iy = (f * n.y) * hdt;
+	const bool ap = uu > 0.0f;
+	vi.x = ap ? vi.x - ix : vi.x;
+	vi.y = ap ? vi.y - iy : vi.y;
+	S.vel[j] = ap ? make_float2(ix + vj.x, iy + vj.y) : vj;
+}
+
 __device__ __forceinline__ void visc_chain(ViscWarp &S, int m, float2 &vi, const StepParams &s) {
+	const float hdt = 0.5f * s.dt;
 	int q = 0;
 	for (; q + 4 <= m; q += 4) {
 		int j[4];
@@ -173,37 +196,17 @@ __device__ __forceinline__ void visc_chain(ViscWarp &S, int m, float2 &vi, const
 #pragma unroll
 		for (int u = 0; u < 4; ++u) vj[u] = S.vel[j[u]];
 #pragma unroll
-		for (int u = 0; u < 4; ++u) {
-			const float uu = (vi.x - vj[u].x) * n[u].x + (vi.y - vj[u].y) * n[u].y;
-			if (uu > 0.0f) {
-				const float f = o[u] * (s.sigma * uu + s.beta * (uu * uu));
-				const float ix = (f * n[u].x * 0.5f) * s.dt;
-				const float iy = (f * n[u].y * 0.5f) * s.dt;
-				vi.x = vi.x - ix;
-				vi.y = vi.y - iy;
-				S.vel[j[u]] = make_float2(ix + vj[u].x, iy + vj[u].y);
-			}
-		}
+		for (int u = 0; u < 4; ++u) visc_pair(S, j[u], n[u], o[u], vj[u], vi, s, hdt);
 	}
 	for (; q < m; ++q) {
 		const int j = S.cslot[q];
-		const float2 n = S.cn[q];
-		const float2 vj = S.vel[j];
-		const float uu = (vi.x - vj.x) * n.x + (vi.y - vj.y) * n.y;
-		if (uu > 0.0f) {
-			const float f = S.comq[q] * (s.sigma * uu + s.beta * (uu * uu));
-			const float ix = (f * n.x * 0.5f) * s.dt;
-			const float iy = (f * n.y * 0.5f) * s.dt;
-			vi.x = vi.x - ix;
-			vi.y = vi.y - iy;
-			S.vel[j] = make_float2(ix + vj.x, iy + vj.y);
-		}
+		visc_pair(S, j, S.cn[q], S.comq[q], S.vel[j], vi, s, hdt);
 	}
 }
 
 }  // namespace
 
-__global__ void __launch_bounds__(kViscWarps * kWarp) k_viscosity(Particles P, SimTables T, StepParams s) {
+__global__ void __launch_bounds__(kViscWarps * kWarp, 2) k_viscosity(Particles P, SimTables T, StepParams s) {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	ViscWarp &S = reinterpret_cast<ViscWarp *>(smem_raw)[threadIdx.x / kWarp];
 	const int lane = threadIdx.x & (kWarp - 1);
@@ -213,6 +216,7 @@ __global__ void __launch_bounds__(kViscWarps * kWarp) k_viscosity(Particles P, S
 		if (lane == 0) t = atomicAdd(&T.taskCounter[0], 1);
 		t = __shfl_sync(kFull, t, 0);
 		if (t >= s.ncell) break;
+		stamp(T, 0, t, 0, lane);
 		const int c = T.cellOfRank[t];
 		const int cnt = T.cellCount[c];
 		if (cnt > 0) {
@@ -227,6 +231,7 @@ __global__ void __launch_bounds__(kViscWarps * kWarp) k_viscosity(Particles P, S
 				}
 			}
 			__syncwarp();
+			stamp(T, 0, t, 1, lane);
 			// Segments of the 3x3 block in list order.
 			int segStart[9], segOff[9];
 			int L = 0, own = 0;
@@ -253,8 +258,7 @@ __global__ void __launch_bounds__(kViscWarps * kWarp) k_viscosity(Particles P, S
 					for (int u = 0; u < 4; ++u) {
 						const int e = base + u * kWarp + lane;
 						if (e < L) {
-							const int q = seg_of<9>(e, segOff);
-							const int src = segStart[q] + (e - segOff[q]);
+							const int src = seg_src<9>(e, segOff, segStart);
 							xp[u] = __ldcg(&P.pos[src]);
 							vp[u] = __ldcg(&P.vel[src]);
 						}
@@ -269,6 +273,7 @@ __global__ void __launch_bounds__(kViscWarps * kWarp) k_viscosity(Particles P, S
 					}
 				}
 				__syncwarp();
+				stamp(T, 0, t, 2, lane);
 				for (int k = 0; k < cnt; ++k) {
 					const int slot = own + k;
 					const float2 xi = S.pos[slot];
@@ -315,8 +320,7 @@ __global__ void __launch_bounds__(kViscWarps * kWarp) k_viscosity(Particles P, S
 				for (int base = 0; base < L; base += kWarp) {
 					const int e = base + lane;
 					if (e < L) {
-						const int q = seg_of<9>(e, segOff);
-						__stcg(&P.vel[segStart[q] + (e - segOff[q])], S.vel[e]);
+						__stcg(&P.vel[seg_src<9>(e, segOff, segStart)], S.vel[e]);
 					}
 				}
 			}
@@ -324,6 +328,7 @@ __global__ void __launch_bounds__(kViscWarps * kWarp) k_viscosity(Particles P, S
 			__threadfence();
 		}
 		__syncwarp();
+		stamp(T, 0, t, 3, lane);
 		if (lane == 0) st_release(&T.done[t], 1u);
 	}
 }
@@ -595,8 +600,7 @@ __global__ void __launch_bounds__(kDensWarps * kWarp) k_density(int n, Particles
 			for (int u = 0; u < 4; ++u) {
 				const int e = base + u * kWarp + lane;
 				if (e < L) {
-					const int q = seg_of<9>(e, segOff);
-					xp[u] = Q.pos[segStart[q] + (e - segOff[q])];
+					xp[u] = Q.pos[seg_src<9>(e, segOff, segStart)];
 				}
 			}
 #pragma unroll
@@ -644,6 +648,9 @@ struct DeltaWarp {
 	float2 pos[kDeltaStageCap];
 	float4 cand[kChainCap];  // in-range candidates: slot, x_j.x, x_j.y, r2
 	float2 half[kChainCap];  // delta * 0.5 of the buffered pairs, list order
+	int pnc[kPrefetch];      // prefetched per particle: new cell,
+	int pjk[kPrefetch];      // new number,
+	float2 ppk[kPrefetch];   // pressure and near pressure
 	int segOff[kRegionCells + 1];
 	int segStart[kRegionCells];
 	int owned[kRegionCells];
@@ -658,7 +665,7 @@ struct Region {
 // Stage the new cells of [x0,x1]x[y0,y1] (row-major) from the positions in
 // new-number order, where each cell is a contiguous range.  Returns false if
 // the region does not fit.
-__device__ bool stage_region(DeltaWarp &S, Region &R, const Particles &Q, const SimTables &T, const StepParams &s,
+__device__ __forceinline__ bool stage_region(DeltaWarp &S, Region &R, const Particles &Q, const SimTables &T, const StepParams &s,
                              int lane) {
 	R.w = R.x1 - R.x0 + 1;
 	R.ncells = R.w * (R.y1 - R.y0 + 1);
@@ -713,7 +720,7 @@ __device__ bool stage_region(DeltaWarp &S, Region &R, const Particles &Q, const 
 	return true;
 }
 
-__device__ void write_back_owned(DeltaWarp &S, const Region &R, const Particles &Q, int lane) {
+__device__ __forceinline__ void write_back_owned(DeltaWarp &S, const Region &R, const Particles &Q, int lane) {
 	for (int q = 0; q < R.ncells; ++q) {
 		if (!S.owned[q]) continue;
 		const int off = S.segOff[q], nn = S.segOff[q + 1] - off, st = S.segStart[q];
@@ -721,29 +728,32 @@ __device__ void write_back_owned(DeltaWarp &S, const Region &R, const Particles 
 	}
 }
 
-// Relax one particle k (old number) whose 3x3 block lies inside the staged
-// region (demo4.cpp:240-254, sph.h:483-495).
-__device__ void relax_particle(DeltaWarp &S, const Region &R, int k, const Particles &Q, const SimTables &T,
+// Relax one particle (new cell nc, new number jk, pressures pk) whose 3x3
+// block lies inside the staged region (demo4.cpp:240-254, sph.h:483-495).
+// In the row-major staged region the three cells of one block row are
+// consecutive, so the particle's list (y-major, then x, then cell order) is
+// three contiguous ranges of staged slots.
+__device__ __forceinline__ void relax_particle(DeltaWarp &S, const Region &R, int nc, int jk, float2 pk, const SimTables &T,
                                const StepParams &s, int lane) {
-	const int nc = T.newCell[k];
-	const int jk = T.newLabel[k];
 	const int x = nc % s.gx, y = nc / s.gx;
-	int off[9], lo[9];
-	int L = 0;
+	const int xa = max(x - 1, 0), xb = min(x + 1, s.gx - 1);
+	int off0 = 0, off1 = 0, off2 = 0, len0 = 0, len1 = 0, len2 = 0;
 #pragma unroll
-	for (int q = 0; q < 9; ++q) {
-		const int xx = x + q % 3 - 1, yy = y + q / 3 - 1;
-		int o = 0, nn = 0;
-		if (xx >= 0 && xx < s.gx && yy >= 0 && yy < s.gy) {
-			const int rq = (yy - R.y0) * R.w + (xx - R.x0);
-			o = S.segOff[rq];
-			nn = S.segOff[rq + 1] - o;
-			if (lane == q) S.owned[rq] = 1;
+	for (int r = 0; r < 3; ++r) {
+		const int yy = y + r - 1;
+		int o = 0, len = 0;
+		if (yy >= 0 && yy < s.gy) {
+			const int rq0 = (yy - R.y0) * R.w + (xa - R.x0);
+			const int rq1 = rq0 + (xb - xa);
+			o = S.segOff[rq0];
+			len = S.segOff[rq1 + 1] - o;
+			if (lane <= xb - xa) S.owned[rq0 + lane] = 1;
 		}
-		off[q] = o;
-		lo[q] = L;
-		L += nn;
+		if (r == 0) { off0 = o; len0 = len; }
+		if (r == 1) { off1 = o; len1 = len; }
+		if (r == 2) { off2 = o; len2 = len; }
 	}
+	const int L = len0 + len1 + len2;
 	const int ownSeg = (y - R.y0) * R.w + (x - R.x0);
 	const int inCell = jk - S.segStart[ownSeg];
 	if (inCell < 0 || inCell >= S.segOff[ownSeg + 1] - S.segOff[ownSeg]) {
@@ -753,27 +763,37 @@ __device__ void relax_particle(DeltaWarp &S, const Region &R, int k, const Parti
 	}
 	const int own = S.segOff[ownSeg] + inCell;
 	const float2 xk = S.pos[own];
-	const float2 pk = Q.press[jk];
+	const int l01 = len0 + len1;
 	float2 dx = make_float2(0.0f, 0.0f);  // lane 0
 	int m = 0;
-	for (int base = 0; base < L; base += kWarp) {
-		const int e = base + lane;
-		bool in = false;
-		int slot = 0;
-		float2 xj = make_float2(0.f, 0.f);
-		float r2 = 0.f;
-		if (e < L) {
-			const int q = seg_of<9>(e, lo);
-			slot = off[q] + (e - lo[q]);
-			xj = S.pos[slot];
-			const float rx = xj.x - xk.x, ry = xj.y - xk.y;
-			r2 = rx * rx + ry * ry;
-			in = r2 < s.h2;
+	for (int base = 0; base < L; base += 2 * kWarp) {
+		bool in[2];
+		int slot[2];
+		float2 xj[2];
+		float r2[2];
+#pragma unroll
+		for (int u = 0; u < 2; ++u) {
+			const int e = base + u * kWarp + lane;
+			in[u] = false;
+			slot[u] = 0;
+			xj[u] = make_float2(0.f, 0.f);
+			r2[u] = 0.f;
+			if (e < L) {
+				slot[u] = e < len0 ? off0 + e : (e < l01 ? off1 + (e - len0) : off2 + (e - l01));
+				xj[u] = S.pos[slot[u]];
+				const float rx = xj[u].x - xk.x, ry = xj[u].y - xk.y;
+				r2[u] = rx * rx + ry * ry;
+				in[u] = r2[u] < s.h2;
+			}
 		}
-		const unsigned mask = __ballot_sync(kFull, in);
-		if (in) S.cand[m + __popc(mask & lanemask_lt())] = make_float4(__int_as_float(slot), xj.x, xj.y, r2);
-		m += __popc(mask);
-		if (m > kChainCap - kWarp || base + kWarp >= L) {
+		const unsigned m0 = __ballot_sync(kFull, in[0]);
+		const unsigned m1 = __ballot_sync(kFull, in[1]);
+		const unsigned lt = lanemask_lt();
+		if (in[0]) S.cand[m + __popc(m0 & lt)] = make_float4(__int_as_float(slot[0]), xj[0].x, xj[0].y, r2[0]);
+		if (in[1])
+			S.cand[m + __popc(m0) + __popc(m1 & lt)] = make_float4(__int_as_float(slot[1]), xj[1].x, xj[1].y, r2[1]);
+		m += __popc(m0) + __popc(m1);
+		if (m > kChainCap - 2 * kWarp || base + 2 * kWarp >= L) {
 			__syncwarp();
 			for (int q = lane; q < m; q += kWarp) {
 				const float4 cd = S.cand[q];
@@ -791,7 +811,19 @@ __device__ void relax_particle(DeltaWarp &S, const Region &R, int k, const Parti
 			}
 			__syncwarp();
 			if (lane == 0) {
-				for (int q = 0; q < m; ++q) {
+				// dx -= delta * 0.5 in list order (demo4.cpp:251).
+				int q = 0;
+				for (; q + 8 <= m; q += 8) {
+					float2 h[8];
+#pragma unroll
+					for (int u = 0; u < 8; ++u) h[u] = S.half[q + u];
+#pragma unroll
+					for (int u = 0; u < 8; ++u) {
+						dx.x = dx.x - h[u].x;
+						dx.y = dx.y - h[u].y;
+					}
+				}
+				for (; q < m; ++q) {
 					const float2 h = S.half[q];
 					dx.x = dx.x - h.x;
 					dx.y = dx.y - h.y;
@@ -809,42 +841,57 @@ __device__ void relax_particle(DeltaWarp &S, const Region &R, int k, const Parti
 }
 
 // Process particles [p0, p1) (old numbers) in order: one staged region if
-// it fits, otherwise one 3x3 region per particle.
-__device__ void relax_group(DeltaWarp &S, int p0, int p1, int bx0, int by0, int bx1, int by1, const Particles &Q,
+// it fits, otherwise one 3x3 region per particle.  Per-particle inputs (new
+// cell, new number, pressure) are prefetched in chunks, off the serial path.
+__device__ __forceinline__ void relax_group(DeltaWarp &S, int p0, int p1, int bx0, int by0, int bx1, int by1, const Particles &Q,
                             const SimTables &T, const StepParams &s, int lane) {
 	Region R;
 	R.x0 = max(bx0 - 1, 0);
 	R.y0 = max(by0 - 1, 0);
 	R.x1 = min(bx1 + 1, s.gx - 1);
 	R.y1 = min(by1 + 1, s.gy - 1);
-	if (stage_region(S, R, Q, T, s, lane)) {
-		for (int k = p0; k < p1; ++k) relax_particle(S, R, k, Q, T, s, lane);
-		write_back_owned(S, R, Q, lane);
-		return;
-	}
+	const bool staged = stage_region(S, R, Q, T, s, lane);
 	__syncwarp();
-	for (int k = p0; k < p1; ++k) {
-		const int nc = T.newCell[k];
-		const int x = nc % s.gx, y = nc / s.gx;
-		R.x0 = max(x - 1, 0);
-		R.y0 = max(y - 1, 0);
-		R.x1 = min(x + 1, s.gx - 1);
-		R.y1 = min(y + 1, s.gy - 1);
-		if (!stage_region(S, R, Q, T, s, lane)) {
-			if (lane == 0) atomicOr(T.error, kErrStageOverflow);
-			__syncwarp();
-			continue;
+	for (int c0 = p0; c0 < p1; c0 += kPrefetch) {
+		const int c1 = min(p1, c0 + kPrefetch);
+		for (int k = c0 + lane; k < c1; k += kWarp) {
+			const int jk = T.newLabel[k];
+			S.pnc[k - c0] = T.newCell[k];
+			S.pjk[k - c0] = jk;
+			S.ppk[k - c0] = Q.press[jk];
 		}
-		relax_particle(S, R, k, Q, T, s, lane);
-		write_back_owned(S, R, Q, lane);
+		__syncwarp();
+		for (int k = c0; k < c1; ++k) {
+			const int nc = S.pnc[k - c0], jk = S.pjk[k - c0];
+			const float2 pk = S.ppk[k - c0];
+			if (staged) {
+				relax_particle(S, R, nc, jk, pk, T, s, lane);
+				continue;
+			}
+			Region R1;
+			const int x = nc % s.gx, y = nc / s.gx;
+			R1.x0 = max(x - 1, 0);
+			R1.y0 = max(y - 1, 0);
+			R1.x1 = min(x + 1, s.gx - 1);
+			R1.y1 = min(y + 1, s.gy - 1);
+			if (!stage_region(S, R1, Q, T, s, lane)) {
+				if (lane == 0) atomicOr(T.error, kErrStageOverflow);
+				__syncwarp();
+				continue;
+			}
+			relax_particle(S, R1, nc, jk, pk, T, s, lane);
+			write_back_owned(S, R1, Q, lane);
+			__syncwarp();
+		}
 		__syncwarp();
 	}
+	if (staged) write_back_owned(S, R, Q, lane);
 }
 
 // Wait for canonical tasks (old cells) near [bx0,bx1]x[by0,by1] whose
 // new-cell bounding boxes come within two cells of it and whose rank is
 // below `limitRank`.
-__device__ void wait_canonical(int bx0, int by0, int bx1, int by1, int moveMax, int limitRank, int selfCell,
+__device__ __forceinline__ void wait_canonical(int bx0, int by0, int bx1, int by1, int moveMax, int limitRank, int selfCell,
                                const SimTables &T, const StepParams &s, int lane) {
 	const int rad = 2 + moveMax;
 	const int x0 = max(bx0 - rad, 0), x1 = min(bx1 + rad, s.gx - 1);
@@ -864,7 +911,7 @@ __device__ void wait_canonical(int bx0, int by0, int bx1, int by1, int moveMax, 
 
 }  // namespace
 
-__global__ void __launch_bounds__(kDeltaWarps * kWarp) k_delta(int n, int n0, Particles Q, SimTables T, StepParams s) {
+__global__ void __launch_bounds__(kDeltaWarps * kWarp, 2) k_delta(int n, int n0, Particles Q, SimTables T, StepParams s) {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	DeltaWarp &S = reinterpret_cast<DeltaWarp *>(smem_raw)[threadIdx.x / kWarp];
 	const int lane = threadIdx.x & (kWarp - 1);
@@ -876,12 +923,14 @@ __global__ void __launch_bounds__(kDeltaWarps * kWarp) k_delta(int n, int n0, Pa
 		if (lane == 0) t = atomicAdd(&T.taskCounter[1], 1);
 		t = __shfl_sync(kFull, t, 0);
 		if (t >= ntask) break;
+		stamp(T, 1, t, 0, lane);
 		if (t < s.ncell) {
 			const int c = T.cellOfRank[t];
 			const int p0 = T.cellStart[c], cnt = T.cellCount[c];
 			if (cnt > 0) {
 				const int4 b = *reinterpret_cast<const int4 *>(&T.bbox[4 * c]);
 				wait_canonical(b.x, b.y, b.z, b.w, moveMax, t, c, T, s, lane);
+				stamp(T, 1, t, 1, lane);
 				relax_group(S, p0, p0 + cnt, b.x, b.y, b.z, b.w, Q, T, s, lane);
 				__syncwarp();
 				__threadfence();
@@ -914,6 +963,7 @@ __global__ void __launch_bounds__(kDeltaWarps * kWarp) k_delta(int n, int n0, Pa
 			__threadfence();
 		}
 		__syncwarp();
+		stamp(T, 1, t, 3, lane);
 		if (lane == 0) st_release(&T.done[t], 1u);
 	}
 }
