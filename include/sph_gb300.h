@@ -205,6 +205,26 @@ int sph_synchronize(sph_sim *sim);
 /* Number of kernels this library launched for `sim` since creation. */
 int sph_kernel_launches(sph_sim *sim, uint64_t *out);
 
+/* No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * (code running inside another component's memory budget or allocator, or a
+ * real-time loop that must not allocate): density and pressure
+ * (SPHComputeDensity/SPHComputePressure semantics, what one update computes
+ * for freshly added particles) of `count` particles whose positions are on
+ * the current device at `pos`, written to `dens` (density, near density) and
+ * `press` (pressure, near pressure), enqueued on `stream` (a cudaStream_t;
+ * NULL = legacy default stream).  It allocates nothing: its working memory is
+ * one fixed device array inside the library, sized for at most
+ * SPH_NOALLOC_MAX_PARTICLES particles and SPH_NOALLOC_MAX_CELLS grid cells
+ * (about 5 MiB, held by every GPU that loads the library until the process
+ * exits); larger inputs return SPH_ERR_CAPACITY.  The first call on a device
+ * looks up that array's device address; make it before any stream capture.
+ * All calls share the array: calls whose work overlaps on the GPU (other
+ * streams, other threads) race and must be serialised by the caller. */
+#define SPH_NOALLOC_MAX_PARTICLES 262144
+#define SPH_NOALLOC_MAX_CELLS 262144
+int sph_density_pressure_noalloc(const sph_domain *domain, const sph_params *params, const sph_vec2 *pos,
+                                 size_t count, sph_vec2 *dens, sph_vec2 *press, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
