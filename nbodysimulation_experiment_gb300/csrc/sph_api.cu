@@ -300,7 +300,7 @@ int run_step(sph_sim *s, float dt) {
 	if (n0 > 0) {
 		SPH_CUDA(cudaMemsetAsync(s->doneV, 0, sizeof(uint32_t) * s->ncell, st));
 		SPH_CUDA(cudaMemsetAsync(T.taskCounter, 0, sizeof(int), st));
-		k_viscosity<<<s->viscBlocks, kViscWarps * kWarp, visc_smem_bytes(), st>>>(A.view(), [&] {
+		k_viscosity<<<s->viscBlocks, kViscTaskWarps * kWarp, visc_smem_bytes(), st>>>(A.view(), [&] {
 			SimTables v = T;
 			v.done = s->doneV;
 			return v;
@@ -331,7 +331,7 @@ int run_step(sph_sim *s, float dt) {
 	{
 		SimTables d = T;
 		d.done = s->doneD;
-		k_delta<<<s->deltaBlocks, kDeltaWarps * kWarp, delta_smem_bytes(), st>>>(n, n0, B.view(), d, sp);
+		k_delta<<<s->deltaBlocks, kDeltaTaskWarps * kWarp, delta_smem_bytes(), st>>>(n, n0, B.view(), d, sp);
 		SPH_LAUNCHED(s);
 	}
 	SPH_CUDA(cudaEventRecord(s->ev[kEvDelta], st));
@@ -480,12 +480,12 @@ int sph_create(const sph_domain *domain, int device, sph_sim **out) {
 	        cudaSuccess)
 		return fail(SPH_ERR_CUDA);
 	int occ = 0;
-	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_viscosity, kViscWarps * kWarp, visc_smem_bytes()) !=
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_viscosity, kViscTaskWarps * kWarp, visc_smem_bytes()) !=
 	        cudaSuccess ||
 	    occ < 1)
 		return fail(SPH_ERR_CUDA);
 	s->viscBlocks = occ * s->numSMs;
-	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_delta, kDeltaWarps * kWarp, delta_smem_bytes()) !=
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_delta, kDeltaTaskWarps * kWarp, delta_smem_bytes()) !=
 	        cudaSuccess ||
 	    occ < 1)
 		return fail(SPH_ERR_CUDA);

@@ -15,10 +15,12 @@ constexpr int kStageCap = 1024;
 // Particles staged per delta-sweep task: the new cells of the task's bounding
 // box grown by one (5x5 cells when particles left the cell in every
 // direction).
-constexpr int kDeltaStageCap = 2048;
+constexpr int kDeltaStageCap = 4096;
 // In-range pairs buffered between the parallel geometry phase and the serial
 // chain of one particle; longer lists are drained in several rounds.
 constexpr int kChainCap = 256;
+// In-range pairs buffered per particle by a delta-sweep block.
+constexpr int kDeltaChainCap = 512;
 // Per-particle inputs of the delta sweep prefetched per chunk of a task.
 constexpr int kPrefetch = 128;
 // Working array of one cell during the grid update (kSPHMaxCellParticleCount
@@ -26,7 +28,7 @@ constexpr int kPrefetch = 128;
 constexpr int kCellCap = 512;
 // Cells of a delta-sweep staging region (bounding box of a task's new cells,
 // grown by one).  Larger regions fall back to per-particle staging.
-constexpr int kRegionCells = 64;
+constexpr int kRegionCells = 100;
 constexpr int kMaxBodies = 100;  // kSPHMaxBodyCount, sph.h:71
 constexpr int kMaxPoly = 8;      // kMaxScenarioPolygonCount, sph.h:161
 // Appendix particles (added since the last update) are swept serially in runs

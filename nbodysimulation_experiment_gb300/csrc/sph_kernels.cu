@@ -59,26 +59,31 @@ __device__ __forceinline__ unsigned lanemask_lt() {
 	return m;
 }
 
-// Bounded wait until *flag != 0.  Returns false if the wait gave up.
-__device__ bool wait_done(const uint32_t *flag, uint32_t *abortFlag, uint32_t *err) {
-	if (ld_acquire(flag) != 0u) return true;
-	const uint64_t t0 = global_ns();
-	unsigned ns = 32;
-	for (uint32_t it = 0; it < kWaitLimitIter; ++it) {
-		if (ld_acquire(flag) != 0u) return true;
-		if (ld_acquire(abortFlag) != 0u) return false;
-		if (global_ns() - t0 > kWaitLimitNs) break;
-		__nanosleep(ns);
-		if (ns < 256) ns <<= 1;
-	}
-	atomicOr(err, kErrTimeout);
-	atomicExch(abortFlag, 1u);
-	return false;
-}
-
 __device__ __forceinline__ void stamp(const SimTables &T, int sweep, int task, int slot, int lane) {
 	if (T.prof != nullptr && lane == 0 && task < T.profStride)
 		T.prof[((size_t)sweep * T.profStride + task) * 4 + slot] = global_ns();
+}
+
+// Converged bounded wait of a whole warp: each lane names one done flag (or
+// none) and the warp polls until every named flag is set.  All lanes run the
+// same loop, so a wait never leaves a warp diverged.  Gives up after 2 s or
+// 2^24 polls, raising kErrTimeout and the abort flag that ends every wait.
+__device__ __forceinline__ void warp_wait(const uint32_t *flag, uint32_t *abortFlag, uint32_t *err) {
+	if (!__any_sync(kFull, flag != nullptr && ld_acquire(flag) == 0u)) return;
+	const uint64_t t0 = global_ns();
+	unsigned ns = 32;
+	for (uint32_t it = 0; it < kWaitLimitIter; ++it) {
+		const bool pending = flag != nullptr && ld_acquire(flag) == 0u;
+		if (!__any_sync(kFull, pending)) return;
+		if (__any_sync(kFull, ld_acquire(abortFlag) != 0u)) return;
+		if (__any_sync(kFull, global_ns() - t0 > kWaitLimitNs)) break;
+		__nanosleep(ns);
+		if (ns < 256) ns <<= 1;
+	}
+	if ((threadIdx.x & 31) == 0) {
+		atomicOr(err, kErrTimeout);
+		atomicExch(abortFlag, 1u);
+	}
 }
 
 __device__ __forceinline__ int cell_of(float2 p, const StepParams &s) {
@@ -138,16 +143,25 @@ __global__ void k_integrate(int n, Particles P, SimTables T, StepParams s) {
 // velocities are written back.  Two tasks conflict iff their cells are at most
 // two apart; every task waits for the earlier conflicting ones.
 
-struct ViscWarp {
+// One task per block: warp 0 runs the ordered velocity chain of particle k
+// while warps 1..3 compute the compacted pair geometry of particle k+1
+// (positions do not change during this pass, so the geometry of every
+// particle of the task is known in advance).
+struct ViscSmem {
 	float2 pos[kStageCap];
 	float2 vel[kStageCap];
-	float4 cand[kChainCap];  // in-range candidates: slot, rx, ry, r2
-	float2 cn[kChainCap];    // unit vector of the pair
-	float comq[kChainCap];   // 1 - q
-	int cslot[kChainCap];
+	int cslot[2][kStageCap];   // in-range pairs of a particle, list order
+	float2 cn[2][kStageCap];   // unit vector of the pair
+	float comq[2][kStageCap];  // 1 - q
+	int m[2];
+	int warpCnt[2][kViscTaskWarps];
+	int task;
 };
 
 namespace {
+
+constexpr int kVT = kViscTaskWarps * kWarp;  // threads per viscosity task
+constexpr int kVP = kVT - kWarp;             // producer threads (warps 1..)
 
 // Source index of flat position e of NSEG consecutive segments (segment s
 // starts at flat offset off[s] and at source index start[s]); selects only,
@@ -160,13 +174,62 @@ __device__ __forceinline__ int seg_src(int e, const int (&off)[NSEG], const int 
 	return src;
 }
 
-// The serial part of the viscosity pass for m buffered pairs, in list order
+__device__ __forceinline__ void producers_sync() {
+	asm volatile("bar.sync 1, %0;" ::"r"(kVP) : "memory");
+}
+
+// Geometry of the particle at staged slot `slot` over the L staged entries
+// (its whole list): in-range pairs in list order with their unit vectors
+// and 1 - q (sph.h:497-505).  Run by the producer warps only.
+__device__ __forceinline__ void visc_geometry(ViscSmem &S, int buf, int slot, int L, const StepParams &s, int p) {
+	const int lane = p & (kWarp - 1), w = p / kWarp;
+	const float2 xi = S.pos[slot];
+	int m = 0, parity = 0;
+	for (int base = 0; base < L; base += kVP) {
+		const int e = base + p;
+		bool in = false;
+		float rx = 0.f, ry = 0.f, r2 = 0.f;
+		if (e < L) {
+			const float2 xj = S.pos[e];
+			rx = xj.x - xi.x;
+			ry = xj.y - xi.y;
+			r2 = rx * rx + ry * ry;
+			in = r2 < s.h2;
+		}
+		const unsigned mask = __ballot_sync(kFull, in);
+		if (lane == 0) S.warpCnt[parity][w] = __popc(mask);
+		producers_sync();
+		int before = m, total = 0;
+#pragma unroll
+		for (int q = 0; q < kViscTaskWarps - 1; ++q) {
+			const int c = S.warpCnt[parity][q];
+			before += (q < w) ? c : 0;
+			total += c;
+		}
+		if (in) {
+			const int at = before + __popc(mask & lanemask_lt());
+			const float r = sqrtf(r2);
+			const float qq = r * s.invH;
+			float len = r;  // Vec2Length(Rij) == rij
+			if (len == 0.0f) len = 1.0f;
+			const float inv = 1.0f / len;
+			S.cslot[buf][at] = e;
+			S.cn[buf][at] = make_float2(rx * inv, ry * inv);
+			S.comq[buf][at] = 1.0f - qq;
+		}
+		m += total;
+		parity ^= 1;
+	}
+	if (p == 0) S.m[buf] = m;
+}
+
+// The serial part of the viscosity pass for one particle, in list order
 // (sph.h:497-512, demo4.cpp:231-234): v_i carries from pair to pair.  Each
 // slot occurs once per list, so the next pairs' velocities may be loaded
 // before this pair's store.  The impulse (f n * 0.5) * dt is computed as
 // (f n) * (0.5 dt): 0.5 dt is exact and halving is exact, so both round the
 // same real product once (unless |f n| < 2^-125).
-__device__ __forceinline__ void visc_pair(ViscWarp &S, int j, float2 n, float o, float2 vj, float2 &vi,
+__device__ __forceinline__ void visc_pair(ViscSmem &S, int j, float2 n, float o, float2 vj, float2 &vi,
                                           const StepParams &s, float hdt) {
 	// Computed unconditionally and selected: only approaching pairs (u > 0)
 	// exchange an impulse.
@@ -180,8 +243,10 @@ __device__ __forceinline__ void visc_pair(ViscWarp &S, int j, float2 n, float o,
 	S.vel[j] = ap ? make_float2(ix + vj.x, iy + vj.y) : vj;
 }
 
-__device__ __forceinline__ void visc_chain(ViscWarp &S, int m, float2 &vi, const StepParams &s) {
+__device__ __forceinline__ void visc_chain(ViscSmem &S, int buf, int slot, const StepParams &s) {
 	const float hdt = 0.5f * s.dt;
+	const int m = S.m[buf];
+	float2 vi = S.vel[slot];
 	int q = 0;
 	for (; q + 4 <= m; q += 4) {
 		int j[4];
@@ -189,9 +254,9 @@ __device__ __forceinline__ void visc_chain(ViscWarp &S, int m, float2 &vi, const
 		float o[4];
 #pragma unroll
 		for (int u = 0; u < 4; ++u) {
-			j[u] = S.cslot[q + u];
-			n[u] = S.cn[q + u];
-			o[u] = S.comq[q + u];
+			j[u] = S.cslot[buf][q + u];
+			n[u] = S.cn[buf][q + u];
+			o[u] = S.comq[buf][q + u];
 		}
 #pragma unroll
 		for (int u = 0; u < 4; ++u) vj[u] = S.vel[j[u]];
@@ -199,39 +264,43 @@ __device__ __forceinline__ void visc_chain(ViscWarp &S, int m, float2 &vi, const
 		for (int u = 0; u < 4; ++u) visc_pair(S, j[u], n[u], o[u], vj[u], vi, s, hdt);
 	}
 	for (; q < m; ++q) {
-		const int j = S.cslot[q];
-		visc_pair(S, j, S.cn[q], S.comq[q], S.vel[j], vi, s, hdt);
+		const int j = S.cslot[buf][q];
+		visc_pair(S, j, S.cn[buf][q], S.comq[buf][q], S.vel[j], vi, s, hdt);
 	}
+	S.vel[slot] = vi;
 }
 
 }  // namespace
 
-__global__ void __launch_bounds__(kViscWarps * kWarp, 2) k_viscosity(Particles P, SimTables T, StepParams s) {
+__global__ void __launch_bounds__(kViscTaskWarps * kWarp, 4) k_viscosity(Particles P, SimTables T, StepParams s) {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
-	ViscWarp &S = reinterpret_cast<ViscWarp *>(smem_raw)[threadIdx.x / kWarp];
-	const int lane = threadIdx.x & (kWarp - 1);
+	ViscSmem &S = *reinterpret_cast<ViscSmem *>(smem_raw);
+	const int tid = threadIdx.x, warp = tid / kWarp;
 	const int gx = s.gx, gy = s.gy;
 	for (;;) {
-		int t = 0;
-		if (lane == 0) t = atomicAdd(&T.taskCounter[0], 1);
-		t = __shfl_sync(kFull, t, 0);
+		if (tid == 0) S.task = atomicAdd(&T.taskCounter[0], 1);
+		__syncthreads();
+		const int t = S.task;
+		__syncthreads();
 		if (t >= s.ncell) break;
-		stamp(T, 0, t, 0, lane);
+		stamp(T, 0, t, 0, tid);
 		const int c = T.cellOfRank[t];
 		const int cnt = T.cellCount[c];
 		if (cnt > 0) {
 			const int cx = c % gx, cy = c / gx;
-			// Wait for earlier tasks within Chebyshev distance 2.
-			if (lane < 25) {
-				const int x = cx + lane % 5 - 2, y = cy + lane / 5 - 2;
-				if (lane != 12 && x >= 0 && x < gx && y >= 0 && y < gy) {
+			// Wait for earlier tasks within Chebyshev distance 2 (warp 0).
+			if (warp == 0) {
+				const uint32_t *flag = nullptr;
+				const int x = cx + tid % 5 - 2, y = cy + tid / 5 - 2;
+				if (tid < 25 && tid != 12 && x >= 0 && x < gx && y >= 0 && y < gy) {
 					const int c2 = y * gx + x;
 					const int r2 = T.rankOfCell[c2];
-					if (r2 < t && T.cellCount[c2] > 0) wait_done(&T.done[r2], T.abort, T.error);
+					if (r2 < t && T.cellCount[c2] > 0) flag = &T.done[r2];
 				}
+				warp_wait(flag, T.abort, T.error);
 			}
-			__syncwarp();
-			stamp(T, 0, t, 1, lane);
+			__syncthreads();
+			stamp(T, 0, t, 1, tid);
 			// Segments of the 3x3 block in list order.
 			int segStart[9], segOff[9];
 			int L = 0, own = 0;
@@ -250,13 +319,13 @@ __global__ void __launch_bounds__(kViscWarps * kWarp, 2) k_viscosity(Particles P
 				L += nn;
 			}
 			if (L > kStageCap) {
-				if (lane == 0) atomicOr(T.error, kErrStageOverflow);
+				if (tid == 0) atomicOr(T.error, kErrStageOverflow);
 			} else {
-				for (int base = 0; base < L; base += 4 * kWarp) {
+				for (int base = 0; base < L; base += 4 * kVT) {
 					float2 xp[4], vp[4];
 #pragma unroll
 					for (int u = 0; u < 4; ++u) {
-						const int e = base + u * kWarp + lane;
+						const int e = base + u * kVT + tid;
 						if (e < L) {
 							const int src = seg_src<9>(e, segOff, segStart);
 							xp[u] = __ldcg(&P.pos[src]);
@@ -265,71 +334,33 @@ __global__ void __launch_bounds__(kViscWarps * kWarp, 2) k_viscosity(Particles P
 					}
 #pragma unroll
 					for (int u = 0; u < 4; ++u) {
-						const int e = base + u * kWarp + lane;
+						const int e = base + u * kVT + tid;
 						if (e < L) {
 							S.pos[e] = xp[u];
 							S.vel[e] = vp[u];
 						}
 					}
 				}
-				__syncwarp();
-				stamp(T, 0, t, 2, lane);
+				__syncthreads();
+				stamp(T, 0, t, 2, tid);
+				if (warp > 0) visc_geometry(S, 0, own, L, s, tid - kWarp);
+				__syncthreads();
 				for (int k = 0; k < cnt; ++k) {
-					const int slot = own + k;
-					const float2 xi = S.pos[slot];
-					float2 vi = S.vel[slot];  // meaningful on lane 0 only
-					int m = 0;
-					for (int base = 0; base < L; base += kWarp) {
-						// Cheap test first; the IEEE sqrt and divide run only on
-						// the compacted in-range pairs.
-						const int e = base + lane;
-						bool in = false;
-						float rx = 0.f, ry = 0.f, r2 = 0.f;
-						if (e < L) {
-							const float2 xj = S.pos[e];
-							rx = xj.x - xi.x;
-							ry = xj.y - xi.y;
-							r2 = rx * rx + ry * ry;
-							in = r2 < s.h2;
-						}
-						const unsigned mask = __ballot_sync(kFull, in);
-						if (in) S.cand[m + __popc(mask & lanemask_lt())] = make_float4(__int_as_float(e), rx, ry, r2);
-						m += __popc(mask);
-						if (m > kChainCap - kWarp || base + kWarp >= L) {
-							__syncwarp();
-							for (int q = lane; q < m; q += kWarp) {
-								const float4 cd = S.cand[q];
-								const float r = sqrtf(cd.w);
-								const float qq = r * s.invH;
-								float len = r;  // Vec2Length(Rij) == rij
-								if (len == 0.0f) len = 1.0f;
-								const float inv = 1.0f / len;
-								S.cslot[q] = __float_as_int(cd.x);
-								S.cn[q] = make_float2(cd.y * inv, cd.z * inv);
-								S.comq[q] = 1.0f - qq;
-							}
-							__syncwarp();
-							if (lane == 0) visc_chain(S, m, vi, s);
-							m = 0;
-							__syncwarp();
-						}
+					if (warp == 0) {
+						if (tid == 0) visc_chain(S, k & 1, own + k, s);
+					} else if (k + 1 < cnt) {
+						visc_geometry(S, (k + 1) & 1, own + k + 1, L, s, tid - kWarp);
 					}
-					if (lane == 0) S.vel[slot] = vi;
-					__syncwarp();
+					__syncthreads();
 				}
-				for (int base = 0; base < L; base += kWarp) {
-					const int e = base + lane;
-					if (e < L) {
-						__stcg(&P.vel[seg_src<9>(e, segOff, segStart)], S.vel[e]);
-					}
-				}
+				for (int e = tid; e < L; e += kVT) __stcg(&P.vel[seg_src<9>(e, segOff, segStart)], S.vel[e]);
 			}
-			__syncwarp();
+			__syncthreads();
 			__threadfence();
 		}
-		__syncwarp();
-		stamp(T, 0, t, 3, lane);
-		if (lane == 0) st_release(&T.done[t], 1u);
+		__syncthreads();
+		stamp(T, 0, t, 3, tid);
+		if (tid == 0) st_release(&T.done[t], 1u);
 	}
 }
 
@@ -644,63 +675,74 @@ __global__ void __launch_bounds__(kDensWarps * kWarp) k_density(int n, Particles
 // back only cells inside its particles' 3x3 blocks.  Earlier tasks whose
 // bounding boxes come within two cells are waited for.
 
-struct DeltaWarp {
+// One task per block of kDeltaTaskWarps warps: the whole block stages the
+// task's region, and for each particle scans the list, compacts the in-range
+// pairs and evaluates them in parallel; one thread then adds the halves to
+// dx in list order.
+struct DeltaSmem {
 	float2 pos[kDeltaStageCap];
-	float4 cand[kChainCap];  // in-range candidates: slot, x_j.x, x_j.y, r2
-	float2 half[kChainCap];  // delta * 0.5 of the buffered pairs, list order
-	int pnc[kPrefetch];      // prefetched per particle: new cell,
-	int pjk[kPrefetch];      // new number,
-	float2 ppk[kPrefetch];   // pressure and near pressure
+	float4 cand[kDeltaChainCap];  // in-range candidates: slot, x_j.x, x_j.y, r2
+	float2 half[kDeltaChainCap];  // delta * 0.5 of the buffered pairs, list order
+	int pnc[kPrefetch];           // prefetched per particle: new cell,
+	int pjk[kPrefetch];           // new number,
+	float2 ppk[kPrefetch];        // pressure and near pressure
 	int segOff[kRegionCells + 1];
 	int segStart[kRegionCells];
 	int owned[kRegionCells];
+	int warpCnt[2][kDeltaTaskWarps];
+	int task;
 };
 
 namespace {
+
+constexpr int kDT = kDeltaTaskWarps * kWarp;  // threads per delta task
 
 struct Region {
 	int x0, y0, x1, y1, w, ncells, L;
 };
 
 // Stage the new cells of [x0,x1]x[y0,y1] (row-major) from the positions in
-// new-number order, where each cell is a contiguous range.  Returns false if
-// the region does not fit.
-__device__ __forceinline__ bool stage_region(DeltaWarp &S, Region &R, const Particles &Q, const SimTables &T, const StepParams &s,
-                             int lane) {
+// new-number order, where each cell is a contiguous range.  Collective over
+// the block; returns false (uniformly) if the region does not fit.
+__device__ __forceinline__ bool stage_region(DeltaSmem &S, Region &R, const Particles &Q, const SimTables &T,
+                                             const StepParams &s, int tid) {
 	R.w = R.x1 - R.x0 + 1;
 	R.ncells = R.w * (R.y1 - R.y0 + 1);
 	if (R.ncells > kRegionCells) return false;
-	int carry = 0;
-	for (int base = 0; base < R.ncells; base += kWarp) {
-		const int q = base + lane;
-		int nn = 0, st = 0;
-		if (q < R.ncells) {
-			const int c2 = (R.y0 + q / R.w) * s.gx + (R.x0 + q % R.w);
-			nn = T.newCount[c2];
-			st = T.newStart[c2];
-		}
-		int incl = nn;
+	if (tid < kWarp) {
+		const int lane = tid;
+		int carry = 0;
+		for (int base = 0; base < R.ncells; base += kWarp) {
+			const int q = base + lane;
+			int nn = 0, st = 0;
+			if (q < R.ncells) {
+				const int c2 = (R.y0 + q / R.w) * s.gx + (R.x0 + q % R.w);
+				nn = T.newCount[c2];
+				st = T.newStart[c2];
+			}
+			int incl = nn;
 #pragma unroll
-		for (int o = 1; o < kWarp; o <<= 1) {
-			const int v = __shfl_up_sync(kFull, incl, o);
-			if (lane >= o) incl += v;
+			for (int o = 1; o < kWarp; o <<= 1) {
+				const int v = __shfl_up_sync(kFull, incl, o);
+				if (lane >= o) incl += v;
+			}
+			if (q < R.ncells) {
+				S.segOff[q] = carry + incl - nn;
+				S.segStart[q] = st;
+				S.owned[q] = 0;
+			}
+			carry += __shfl_sync(kFull, incl, kWarp - 1);
 		}
-		if (q < R.ncells) {
-			S.segOff[q] = carry + incl - nn;
-			S.segStart[q] = st;
-			S.owned[q] = 0;
-		}
-		carry += __shfl_sync(kFull, incl, kWarp - 1);
+		if (lane == 0) S.segOff[R.ncells] = carry;
 	}
-	R.L = carry;
-	if (lane == 0) S.segOff[R.ncells] = carry;
-	__syncwarp();
-	if (carry > kDeltaStageCap) return false;
-	for (int base = 0; base < R.L; base += 4 * kWarp) {
+	__syncthreads();
+	R.L = S.segOff[R.ncells];
+	if (R.L > kDeltaStageCap) return false;
+	for (int base = 0; base < R.L; base += 4 * kDT) {
 		float2 xp[4];
 #pragma unroll
 		for (int u = 0; u < 4; ++u) {
-			const int e = base + u * kWarp + lane;
+			const int e = base + u * kDT + tid;
 			if (e < R.L) {
 				int lo = 0, hi = R.ncells;
 				while (hi - lo > 1) {
@@ -712,19 +754,19 @@ __device__ __forceinline__ bool stage_region(DeltaWarp &S, Region &R, const Part
 		}
 #pragma unroll
 		for (int u = 0; u < 4; ++u) {
-			const int e = base + u * kWarp + lane;
+			const int e = base + u * kDT + tid;
 			if (e < R.L) S.pos[e] = xp[u];
 		}
 	}
-	__syncwarp();
+	__syncthreads();
 	return true;
 }
 
-__device__ __forceinline__ void write_back_owned(DeltaWarp &S, const Region &R, const Particles &Q, int lane) {
+__device__ __forceinline__ void write_back_owned(DeltaSmem &S, const Region &R, const Particles &Q, int tid) {
 	for (int q = 0; q < R.ncells; ++q) {
 		if (!S.owned[q]) continue;
 		const int off = S.segOff[q], nn = S.segOff[q + 1] - off, st = S.segStart[q];
-		for (int j = lane; j < nn; j += kWarp) __stcg(&Q.pos[st + j], S.pos[off + j]);
+		for (int j = tid; j < nn; j += kDT) __stcg(&Q.pos[st + j], S.pos[off + j]);
 	}
 }
 
@@ -732,9 +774,10 @@ __device__ __forceinline__ void write_back_owned(DeltaWarp &S, const Region &R, 
 // block lies inside the staged region (demo4.cpp:240-254, sph.h:483-495).
 // In the row-major staged region the three cells of one block row are
 // consecutive, so the particle's list (y-major, then x, then cell order) is
-// three contiguous ranges of staged slots.
-__device__ __forceinline__ void relax_particle(DeltaWarp &S, const Region &R, int nc, int jk, float2 pk, const SimTables &T,
-                               const StepParams &s, int lane) {
+// three contiguous ranges of staged slots.  Collective over the block.
+__device__ __forceinline__ void relax_particle(DeltaSmem &S, const Region &R, int nc, int jk, float2 pk,
+                                               const SimTables &T, const StepParams &s, int tid) {
+	const int lane = tid & (kWarp - 1), warp = tid / kWarp;
 	const int x = nc % s.gx, y = nc / s.gx;
 	const int xa = max(x - 1, 0), xb = min(x + 1, s.gx - 1);
 	int off0 = 0, off1 = 0, off2 = 0, len0 = 0, len1 = 0, len2 = 0;
@@ -747,7 +790,7 @@ __device__ __forceinline__ void relax_particle(DeltaWarp &S, const Region &R, in
 			const int rq1 = rq0 + (xb - xa);
 			o = S.segOff[rq0];
 			len = S.segOff[rq1 + 1] - o;
-			if (lane <= xb - xa) S.owned[rq0 + lane] = 1;
+			if (tid <= xb - xa) S.owned[rq0 + tid] = 1;
 		}
 		if (r == 0) { off0 = o; len0 = len; }
 		if (r == 1) { off1 = o; len1 = len; }
@@ -757,23 +800,23 @@ __device__ __forceinline__ void relax_particle(DeltaWarp &S, const Region &R, in
 	const int ownSeg = (y - R.y0) * R.w + (x - R.x0);
 	const int inCell = jk - S.segStart[ownSeg];
 	if (inCell < 0 || inCell >= S.segOff[ownSeg + 1] - S.segOff[ownSeg]) {
-		if (lane == 0) atomicOr(T.error, kErrIndex);
-		__syncwarp();
+		if (tid == 0) atomicOr(T.error, kErrIndex);
+		__syncthreads();
 		return;
 	}
 	const int own = S.segOff[ownSeg] + inCell;
 	const float2 xk = S.pos[own];
 	const int l01 = len0 + len1;
-	float2 dx = make_float2(0.0f, 0.0f);  // lane 0
-	int m = 0;
-	for (int base = 0; base < L; base += 2 * kWarp) {
+	float2 dx = make_float2(0.0f, 0.0f);  // thread 0
+	int m = 0, parity = 0;
+	for (int base = 0; base < L; base += 2 * kDT) {
 		bool in[2];
 		int slot[2];
 		float2 xj[2];
 		float r2[2];
 #pragma unroll
 		for (int u = 0; u < 2; ++u) {
-			const int e = base + u * kWarp + lane;
+			const int e = base + warp * 2 * kWarp + u * kWarp + lane;
 			in[u] = false;
 			slot[u] = 0;
 			xj[u] = make_float2(0.f, 0.f);
@@ -788,14 +831,25 @@ __device__ __forceinline__ void relax_particle(DeltaWarp &S, const Region &R, in
 		}
 		const unsigned m0 = __ballot_sync(kFull, in[0]);
 		const unsigned m1 = __ballot_sync(kFull, in[1]);
+		if (lane == 0) S.warpCnt[parity][warp] = __popc(m0) + __popc(m1);
+		__syncthreads();
+		int before = m, total = 0;
+#pragma unroll
+		for (int w = 0; w < kDeltaTaskWarps; ++w) {
+			const int c = S.warpCnt[parity][w];
+			before += (w < warp) ? c : 0;
+			total += c;
+		}
 		const unsigned lt = lanemask_lt();
-		if (in[0]) S.cand[m + __popc(m0 & lt)] = make_float4(__int_as_float(slot[0]), xj[0].x, xj[0].y, r2[0]);
+		if (in[0]) S.cand[before + __popc(m0 & lt)] = make_float4(__int_as_float(slot[0]), xj[0].x, xj[0].y, r2[0]);
 		if (in[1])
-			S.cand[m + __popc(m0) + __popc(m1 & lt)] = make_float4(__int_as_float(slot[1]), xj[1].x, xj[1].y, r2[1]);
-		m += __popc(m0) + __popc(m1);
-		if (m > kChainCap - 2 * kWarp || base + 2 * kWarp >= L) {
-			__syncwarp();
-			for (int q = lane; q < m; q += kWarp) {
+			S.cand[before + __popc(m0) + __popc(m1 & lt)] =
+			    make_float4(__int_as_float(slot[1]), xj[1].x, xj[1].y, r2[1]);
+		m += total;
+		parity ^= 1;
+		if (m > kDeltaChainCap - 2 * kDT || base + 2 * kDT >= L) {
+			__syncthreads();
+			for (int q = tid; q < m; q += kDT) {
 				const float4 cd = S.cand[q];
 				const float rx = cd.y - xk.x, ry = cd.z - xk.y;
 				const float rij = sqrtf(cd.w);
@@ -809,8 +863,8 @@ __device__ __forceinline__ void relax_particle(DeltaWarp &S, const Region &R, in
 				S.pos[__float_as_int(cd.x)] = make_float2(half.x + cd.y, half.y + cd.z);
 				S.half[q] = half;
 			}
-			__syncwarp();
-			if (lane == 0) {
+			__syncthreads();
+			if (tid == 0) {
 				// dx -= delta * 0.5 in list order (demo4.cpp:251).
 				int q = 0;
 				for (; q + 8 <= m; q += 8) {
@@ -830,42 +884,42 @@ __device__ __forceinline__ void relax_particle(DeltaWarp &S, const Region &R, in
 				}
 			}
 			m = 0;
-			__syncwarp();
 		}
 	}
-	if (lane == 0) {
+	if (tid == 0) {
 		const float2 xo = S.pos[own];
 		S.pos[own] = make_float2(dx.x + xo.x, dx.y + xo.y);
 	}
-	__syncwarp();
+	__syncthreads();
 }
 
 // Process particles [p0, p1) (old numbers) in order: one staged region if
 // it fits, otherwise one 3x3 region per particle.  Per-particle inputs (new
 // cell, new number, pressure) are prefetched in chunks, off the serial path.
-__device__ __forceinline__ void relax_group(DeltaWarp &S, int p0, int p1, int bx0, int by0, int bx1, int by1, const Particles &Q,
-                            const SimTables &T, const StepParams &s, int lane) {
+__device__ __forceinline__ void relax_group(DeltaSmem &S, int p0, int p1, int bx0, int by0, int bx1, int by1,
+                                            const Particles &Q, const SimTables &T, const StepParams &s, int tid,
+                                            int task) {
 	Region R;
 	R.x0 = max(bx0 - 1, 0);
 	R.y0 = max(by0 - 1, 0);
 	R.x1 = min(bx1 + 1, s.gx - 1);
 	R.y1 = min(by1 + 1, s.gy - 1);
-	const bool staged = stage_region(S, R, Q, T, s, lane);
-	__syncwarp();
+	const bool staged = stage_region(S, R, Q, T, s, tid);
+	stamp(T, 1, task, 2, staged ? tid : 1);
 	for (int c0 = p0; c0 < p1; c0 += kPrefetch) {
 		const int c1 = min(p1, c0 + kPrefetch);
-		for (int k = c0 + lane; k < c1; k += kWarp) {
+		for (int k = c0 + tid; k < c1; k += kDT) {
 			const int jk = T.newLabel[k];
 			S.pnc[k - c0] = T.newCell[k];
 			S.pjk[k - c0] = jk;
 			S.ppk[k - c0] = Q.press[jk];
 		}
-		__syncwarp();
+		__syncthreads();
 		for (int k = c0; k < c1; ++k) {
 			const int nc = S.pnc[k - c0], jk = S.pjk[k - c0];
 			const float2 pk = S.ppk[k - c0];
 			if (staged) {
-				relax_particle(S, R, nc, jk, pk, T, s, lane);
+				relax_particle(S, R, nc, jk, pk, T, s, tid);
 				continue;
 			}
 			Region R1;
@@ -874,65 +928,72 @@ __device__ __forceinline__ void relax_group(DeltaWarp &S, int p0, int p1, int bx
 			R1.y0 = max(y - 1, 0);
 			R1.x1 = min(x + 1, s.gx - 1);
 			R1.y1 = min(y + 1, s.gy - 1);
-			if (!stage_region(S, R1, Q, T, s, lane)) {
-				if (lane == 0) atomicOr(T.error, kErrStageOverflow);
-				__syncwarp();
+			if (!stage_region(S, R1, Q, T, s, tid)) {
+				if (tid == 0) atomicOr(T.error, kErrStageOverflow);
+				__syncthreads();
 				continue;
 			}
-			relax_particle(S, R1, nc, jk, pk, T, s, lane);
-			write_back_owned(S, R1, Q, lane);
-			__syncwarp();
+			relax_particle(S, R1, nc, jk, pk, T, s, tid);
+			write_back_owned(S, R1, Q, tid);
+			__syncthreads();
 		}
-		__syncwarp();
+		__syncthreads();
 	}
-	if (staged) write_back_owned(S, R, Q, lane);
+	if (staged) write_back_owned(S, R, Q, tid);
 }
 
 // Wait for canonical tasks (old cells) near [bx0,bx1]x[by0,by1] whose
 // new-cell bounding boxes come within two cells of it and whose rank is
-// below `limitRank`.
-__device__ __forceinline__ void wait_canonical(int bx0, int by0, int bx1, int by1, int moveMax, int limitRank, int selfCell,
-                               const SimTables &T, const StepParams &s, int lane) {
+// below `limitRank`.  Collective over the block.
+__device__ __forceinline__ void wait_canonical(int bx0, int by0, int bx1, int by1, int moveMax, int limitRank,
+                                               int selfCell, const SimTables &T, const StepParams &s, int tid) {
 	const int rad = 2 + moveMax;
 	const int x0 = max(bx0 - rad, 0), x1 = min(bx1 + rad, s.gx - 1);
 	const int y0 = max(by0 - rad, 0), y1 = min(by1 + rad, s.gy - 1);
 	const int w = x1 - x0 + 1;
 	const int total = w * (y1 - y0 + 1);
-	for (int q = lane; q < total; q += kWarp) {
-		const int c2 = (y0 + q / w) * s.gx + (x0 + q % w);
-		if (c2 == selfCell) continue;
-		const int r2 = T.rankOfCell[c2];
-		if (r2 >= limitRank || T.cellCount[c2] == 0) continue;
-		const int4 b = *reinterpret_cast<const int4 *>(&T.bbox[4 * c2]);
-		if (rect_dist(b.x, b.y, b.z, b.w, bx0, by0, bx1, by1) <= 2) wait_done(&T.done[r2], T.abort, T.error);
+	for (int q0 = 0; q0 < total; q0 += kDT) {
+		const int q = q0 + tid;
+		const uint32_t *flag = nullptr;
+		if (q < total) {
+			const int c2 = (y0 + q / w) * s.gx + (x0 + q % w);
+			const int r2 = T.rankOfCell[c2];
+			if (c2 != selfCell && r2 < limitRank && T.cellCount[c2] > 0) {
+				const int4 b = *reinterpret_cast<const int4 *>(&T.bbox[4 * c2]);
+				if (rect_dist(b.x, b.y, b.z, b.w, bx0, by0, bx1, by1) <= 2) flag = &T.done[r2];
+			}
+		}
+		warp_wait(flag, T.abort, T.error);
 	}
-	__syncwarp();
+	__syncthreads();
 }
 
 }  // namespace
 
-__global__ void __launch_bounds__(kDeltaWarps * kWarp, 2) k_delta(int n, int n0, Particles Q, SimTables T, StepParams s) {
+__global__ void __launch_bounds__(kDeltaTaskWarps * kWarp, 4) k_delta(int n, int n0, Particles Q, SimTables T,
+                                                                       StepParams s) {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
-	DeltaWarp &S = reinterpret_cast<DeltaWarp *>(smem_raw)[threadIdx.x / kWarp];
-	const int lane = threadIdx.x & (kWarp - 1);
+	DeltaSmem &S = *reinterpret_cast<DeltaSmem *>(smem_raw);
+	const int tid = threadIdx.x;
 	const int runs = (n - n0 + kAppendixRun - 1) / kAppendixRun;
 	const int ntask = s.ncell + runs;
 	const int moveMax = T.moverCount[1];
 	for (;;) {
-		int t = 0;
-		if (lane == 0) t = atomicAdd(&T.taskCounter[1], 1);
-		t = __shfl_sync(kFull, t, 0);
+		if (tid == 0) S.task = atomicAdd(&T.taskCounter[1], 1);
+		__syncthreads();
+		const int t = S.task;
+		__syncthreads();
 		if (t >= ntask) break;
-		stamp(T, 1, t, 0, lane);
+		stamp(T, 1, t, 0, tid);
 		if (t < s.ncell) {
 			const int c = T.cellOfRank[t];
 			const int p0 = T.cellStart[c], cnt = T.cellCount[c];
 			if (cnt > 0) {
 				const int4 b = *reinterpret_cast<const int4 *>(&T.bbox[4 * c]);
-				wait_canonical(b.x, b.y, b.z, b.w, moveMax, t, c, T, s, lane);
-				stamp(T, 1, t, 1, lane);
-				relax_group(S, p0, p0 + cnt, b.x, b.y, b.z, b.w, Q, T, s, lane);
-				__syncwarp();
+				wait_canonical(b.x, b.y, b.z, b.w, moveMax, t, c, T, s, tid);
+				stamp(T, 1, t, 1, tid);
+				relax_group(S, p0, p0 + cnt, b.x, b.y, b.z, b.w, Q, T, s, tid, t);
+				__syncthreads();
 				__threadfence();
 			}
 		} else {
@@ -940,31 +1001,47 @@ __global__ void __launch_bounds__(kDeltaWarps * kWarp, 2) k_delta(int n, int n0,
 			const int p0 = n0 + run * kAppendixRun;
 			const int p1 = min(n, p0 + kAppendixRun);
 			int bx0 = s.gx, by0 = s.gy, bx1 = -1, by1 = -1;
-			for (int k = p0 + lane; k < p1; k += kWarp) {
+			for (int k = p0 + tid; k < p1; k += kDT) {
 				const int nc = T.newCell[k];
 				bx0 = min(bx0, nc % s.gx);
 				bx1 = max(bx1, nc % s.gx);
 				by0 = min(by0, nc / s.gx);
 				by1 = max(by1, nc / s.gx);
 			}
-			for (int o = 16; o > 0; o >>= 1) {
-				bx0 = min(bx0, __shfl_xor_sync(kFull, bx0, o));
-				by0 = min(by0, __shfl_xor_sync(kFull, by0, o));
-				bx1 = max(bx1, __shfl_xor_sync(kFull, bx1, o));
-				by1 = max(by1, __shfl_xor_sync(kFull, by1, o));
+			// Block-wide min/max of the run's new cells (kAppendixRun <= 32:
+			// only warp 0 holds values).
+			if (tid < kWarp) {
+				for (int o = 16; o > 0; o >>= 1) {
+					bx0 = min(bx0, __shfl_xor_sync(kFull, bx0, o));
+					by0 = min(by0, __shfl_xor_sync(kFull, by0, o));
+					bx1 = max(bx1, __shfl_xor_sync(kFull, bx1, o));
+					by1 = max(by1, __shfl_xor_sync(kFull, by1, o));
+				}
+				if (tid == 0) {
+					S.warpCnt[0][0] = bx0;
+					S.warpCnt[0][1] = by0;
+					S.warpCnt[1][0] = bx1;
+					S.warpCnt[1][1] = by1;
+				}
 			}
+			__syncthreads();
+			bx0 = S.warpCnt[0][0];
+			by0 = S.warpCnt[0][1];
+			bx1 = S.warpCnt[1][0];
+			by1 = S.warpCnt[1][1];
+			__syncthreads();
 			// All canonical tasks precede the appendix; the appendix itself
 			// is swept run after run.
-			wait_canonical(bx0, by0, bx1, by1, moveMax, s.ncell, -1, T, s, lane);
-			if (lane == 0 && run > 0) wait_done(&T.done[t - 1], T.abort, T.error);
-			__syncwarp();
-			relax_group(S, p0, p1, bx0, by0, bx1, by1, Q, T, s, lane);
-			__syncwarp();
+			wait_canonical(bx0, by0, bx1, by1, moveMax, s.ncell, -1, T, s, tid);
+			if (tid < kWarp) warp_wait(tid == 0 && run > 0 ? &T.done[t - 1] : nullptr, T.abort, T.error);
+			__syncthreads();
+			relax_group(S, p0, p1, bx0, by0, bx1, by1, Q, T, s, tid, t);
+			__syncthreads();
 			__threadfence();
 		}
-		__syncwarp();
-		stamp(T, 1, t, 3, lane);
-		if (lane == 0) st_release(&T.done[t], 1u);
+		__syncthreads();
+		stamp(T, 1, t, 3, tid);
+		if (tid == 0) st_release(&T.done[t], 1u);
 	}
 }
 
@@ -1169,8 +1246,8 @@ __global__ void k_gather_by_id(int n, const int *id, const float2 *src, float2 *
 	if (k >= 0 && k < n) dst[k] = src[i];
 }
 
-size_t visc_smem_bytes() { return sizeof(ViscWarp) * kViscWarps; }
-size_t delta_smem_bytes() { return sizeof(DeltaWarp) * kDeltaWarps; }
+size_t visc_smem_bytes() { return sizeof(ViscSmem); }
+size_t delta_smem_bytes() { return sizeof(DeltaSmem); }
 size_t dens_smem_bytes() { return sizeof(DensWarp) * kDensWarps; }
 
 }  // namespace sphgb

@@ -5,16 +5,16 @@
 
 namespace sphgb {
 
-constexpr int kViscWarps = 4;      // warps (independent sweep workers) per block
-constexpr int kDeltaWarps = 4;
+constexpr int kViscTaskWarps = 4;   // warps cooperating on one viscosity task (one task per block)
+constexpr int kDeltaTaskWarps = 4;  // warps cooperating on one delta task (one task per block)
 constexpr int kDensWarps = 8;
 constexpr int kGridWarps = 4;
 constexpr int kScanThreads = 1024;
 constexpr int kElemThreads = 256;  // elementwise kernels
 constexpr int kCollideThreads = 256;
 
-struct ViscWarp;
-struct DeltaWarp;
+struct ViscSmem;
+struct DeltaSmem;
 struct DensWarp;
 
 size_t visc_smem_bytes();
