@@ -101,6 +101,9 @@ typedef struct sph_stats {
 int sph_reference_domain(sph_domain *out);
 int sph_default_params(sph_params *out);
 const char *sph_status_string(int status);
+/* No counterpart in the reference: the CUDA error name, failing call and
+ * message behind the last SPH_ERR_CUDA returned on this thread ("" if none). */
+const char *sph_last_error(void);
 
 /* Demo4::ParticleSimulation() / ~ParticleSimulation() (demo4.cpp:14-35).
  * `device` selects the CUDA device; all device memory for `domain` is
@@ -204,6 +207,54 @@ int sph_device_arrays(sph_sim *sim, const void **pos, const void **vel, const vo
 int sph_synchronize(sph_sim *sim);
 /* Number of kernels this library launched for `sim` since creation. */
 int sph_kernel_launches(sph_sim *sim, uint64_t *out);
+/* No counterpart in the reference.  Updates that repeat the previous one's
+ * shape (same scenes, bodies, parameters and dt; no particles added since)
+ * are replayed from a CUDA graph captured per step; enable = 0 launches every
+ * kernel one by one instead.  Results are identical either way.  Default 1. */
+int sph_use_graphs(sph_sim *sim, int enable);
+
+/* ---- Batched scenes (no single reference counterpart) ---------------------
+ * Many independent Demo4 scenes advanced together: one sph_update(sim, dt)
+ * advances every scene by dt with one launch per stage over all of them.
+ * Each scene's update equals what a single-scene simulation holding the same
+ * state computes (ParticleSimulation::Update, demo4.cpp:286-427), bit for
+ * bit; scenes never interact.  A batch is fixed at creation: its scenes,
+ * bodies and particles (the scene descriptions below, in the reference's
+ * AddParticle/AddPlane/AddCircle/AddLineSegment/AddPolygon terms) are given
+ * to sph_batch_create, and the single-scene mutators (Add*, Clear*,
+ * SetGravity, SetParams, external forces, sph_load_state) return
+ * SPH_ERR_NOT_SUPPORTED on a batch. */
+#define SPH_BODY_PLANE 1   /* a = normal, value = distance (demo4.cpp:121-125) */
+#define SPH_BODY_CIRCLE 2  /* a = centre, value = radius (demo4.cpp:127-131) */
+#define SPH_BODY_SEGMENT 3 /* a, b = end points (demo4.cpp:133-137) */
+#define SPH_BODY_POLYGON 4 /* verts[0..vertex_count) (demo4.cpp:139-140) */
+typedef struct sph_body_desc {
+	int type;
+	size_t vertex_count;
+	sph_vec2 a, b;
+	float value;
+	sph_vec2 verts[8];
+} sph_body_desc;
+typedef struct sph_scene_desc {
+	sph_domain domain;          /* max_particles is ignored: the capacity is particle_count */
+	sph_params params;
+	sph_vec2 gravity;
+	size_t particle_count;
+	const sph_vec2 *positions;  /* AddParticle order */
+	const sph_vec2 *forces;     /* NULL = zero */
+	size_t body_count;
+	const sph_body_desc *bodies;
+} sph_scene_desc;
+int sph_batch_create(const sph_scene_desc *scenes, size_t scene_count, int device, sph_sim **out);
+int sph_batch_scene_count(sph_sim *sim, size_t *out);
+/* Per-scene reads; `scene` indexes the creation order.  Arrays are in the
+ * scene's AddParticle order; any output pointer may be NULL. */
+int sph_batch_read_particles(sph_sim *sim, size_t scene, size_t count, sph_vec2 *pos, sph_vec2 *vel, sph_vec2 *dens,
+                             sph_vec2 *press);
+int sph_batch_get_stats(sph_sim *sim, size_t scene, sph_stats *out);
+int sph_batch_state_info(sph_sim *sim, size_t scene, size_t *count, size_t *canonical_count, int *grid_x,
+                         int *grid_y);
+int sph_batch_dump_state(sph_sim *sim, size_t scene, const sph_state_view *out);
 
 /* No counterpart in the reference.  For callers that cannot call cudaMalloc
  * (code running inside another component's memory budget or allocator, or a

@@ -1,8 +1,9 @@
 // Host side of the GB300 Demo4 SPH step: the simulation object behind the C
 // ABI of include/sph_gb300.h, mirroring Demo4::ParticleSimulation
-// (NBodySimulation/demo4.h:178-267).  All device memory is allocated once in
-// sph_create for the domain's capacities; an update is a fixed sequence of
-// kernel launches on the simulation's stream.
+// (NBodySimulation/demo4.h:178-267).  A simulation holds one scene
+// (sph_create: the reference's interface) or many independent scenes
+// (sph_batch_create) in one arena; all device memory is allocated at
+// creation, and an update is one launch per stage over every scene.
 //
 // Host arithmetic that feeds the step (volume and emitter particle
 // placement, step scalars) follows the reference's FP32 operation order; the
@@ -12,9 +13,11 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <new>
+#include <utility>
 #include <vector>
 
 #include "../../include/sph_gb300.h"
@@ -50,29 +53,39 @@ struct BufferSet {
 
 enum Stage { kEvBegin, kEvIntegrate, kEvVisc, kEvPredict, kEvGrid, kEvDensity, kEvDelta, kEvCollide, kEvCount };
 
+// One scene: the state Demo4::ParticleSimulation keeps on the host.
+struct Scene {
+	sph_domain dom{};
+	int gx = 0, gy = 0, ncell = 0;
+	sph_params params{};
+	sph_vec2 gravity{0.0f, 0.0f};
+	sph_vec2 external{0.0f, 0.0f};
+	std::vector<Body> bodies;
+	std::vector<Emitter> emitters;
+	size_t n = 0;     // particles (device-resident + pending)
+	size_t n0 = 0;    // canonical particles (numbered by the last update)
+	size_t nDev = 0;  // particles already on the device
+	size_t cap = 0;   // particle capacity
+	int cellBase = 0, pBase = 0, bodyBase = 0;  // offsets into the shared arrays
+	std::vector<float2> pendPos, pendForce;
+};
+
 }  // namespace
 
 struct sph_sim {
 	int device = 0;
 	cudaStream_t stream = nullptr;
-	sph_domain dom{};
-	int gx = 0, gy = 0, ncell = 0;
 	int numSMs = 0;
 	int viscBlocks = 0, deltaBlocks = 0, densBlocks = 0, gridBlocks = 0;
-
-	sph_params params{};
-	sph_vec2 gravity{0.0f, 0.0f};
-	sph_vec2 external{0.0f, 0.0f};
+	bool batch = false;
 	int multithreading = 0;
 
-	std::vector<Body> bodies;
+	std::vector<Scene> scenes;
+	int ncellTotal = 0;
+	size_t bodyCap = 0;
+	bool sceneTableDirty = true;
 	bool bodiesDirty = true;
-	std::vector<Emitter> emitters;
-
-	size_t n = 0;   // particles (device-resident + pending)
-	size_t n0 = 0;  // canonical count
-	size_t nDev = 0;  // particles already on the device
-	std::vector<float2> pendPos, pendForce;
+	float tableDt = 0.0f;
 
 	BufferSet buf[2];
 	int cur = 0;
@@ -80,28 +93,57 @@ struct sph_sim {
 	SimTables T{};
 	uint32_t *doneV = nullptr, *doneD = nullptr;
 	size_t doneDCap = 0;
+	int nApp = 0;
 	float2 *stagePos = nullptr, *stageForce = nullptr;  // device staging for adds
 	float2 *hostPos = nullptr, *hostForce = nullptr;    // pinned staging
 	size_t stageCap = 0;
+
+	// Per-step CUDA graphs, one per buffer parity (the step ping-pongs its
+	// particle and cell arrays), replayed while nothing but time advances.
+	cudaGraphExec_t graphs[2] = {nullptr, nullptr};
+	uint64_t graphKernels[2] = {0, 0};
+	int steadySteps = 0;  // updates since the scene table last changed
+	bool useGraphs = true;
 
 	cudaEvent_t ev[kEvCount] = {};
 	bool timed = false;
 	float emitterMs = 0.0f;
 	uint64_t launches = 0;
-	int stickyError = SPH_OK;
 	unsigned long long *prof = nullptr;
 
-	uint32_t maxNbSeed() const { return dom.max_neighbors; }
+	size_t totalParticles() const {
+		size_t t = 0;
+		for (const Scene &sc : scenes) t += sc.n;
+		return t;
+	}
 };
 
 namespace {
 
-int cuda_status(cudaError_t e) { return e == cudaSuccess ? SPH_OK : SPH_ERR_CUDA; }
 
-#define SPH_CUDA(call)                                 \
-	do {                                               \
-		cudaError_t e_ = (call);                       \
-		if (e_ != cudaSuccess) return SPH_ERR_CUDA;    \
+
+// Text of the last failing CUDA call on this thread (sph_last_error).
+thread_local char g_last_error[256] = "";
+
+int cuda_failed(cudaError_t e, const char *what, int line) {
+	snprintf(g_last_error, sizeof(g_last_error), "%s (%s) at sph_api.cu:%d: %s", cudaGetErrorName(e), what, line,
+	         cudaGetErrorString(e));
+	return SPH_ERR_CUDA;
+}
+
+int cuda_status(cudaError_t e) { return e == cudaSuccess ? SPH_OK : cuda_failed(e, "CUDA call", 0); }
+
+#define SPH_CUDA(call)                                                     \
+	do {                                                                   \
+		cudaError_t e_ = (call);                                           \
+		if (e_ != cudaSuccess) return cuda_failed(e_, #call, __LINE__);    \
+	} while (0)
+
+#define SPH_LAUNCHED(s)                                                     \
+	do {                                                                    \
+		(s)->launches++;                                                    \
+		cudaError_t e_ = cudaGetLastError();                                \
+		if (e_ != cudaSuccess) return cuda_failed(e_, "launch", __LINE__);  \
 	} while (0)
 
 template <typename T>
@@ -113,44 +155,107 @@ int dalloc(T **p, size_t count) {
 	return cuda_status(e);
 }
 
-StepParams step_params(const sph_sim *s, float dt) {
+int blocks_for(size_t items, int threads) { return (int)std::max<size_t>(1, (items + threads - 1) / threads); }
+
+// Step scalars of a scene, in FP32 exactly as the reference computes them.
+StepParams step_params(const Scene &sc, float dt) {
 	StepParams p{};
-	p.h2 = s->params.kernel_height * s->params.kernel_height;
-	p.invH = s->params.inv_kernel_height;
-	p.rho0 = s->params.rest_density;
-	p.k = s->params.stiffness;
-	p.kNear = s->params.near_stiffness;
-	p.sigma = s->params.linear_viscosity;
-	p.beta = s->params.quadratic_viscosity;
+	p.h2 = sc.params.kernel_height * sc.params.kernel_height;
+	p.invH = sc.params.inv_kernel_height;
+	p.rho0 = sc.params.rest_density;
+	p.k = sc.params.stiffness;
+	p.kNear = sc.params.near_stiffness;
+	p.sigma = sc.params.linear_viscosity;
+	p.beta = sc.params.quadratic_viscosity;
 	p.dt = dt;
 	p.invDt = 1.0f / dt;
 	p.dt2 = dt * dt;
-	p.extX = s->gravity.x + s->external.x;
-	p.extY = s->gravity.y + s->external.y;
-	p.halfW = s->dom.width * 0.5f;
-	p.halfH = s->dom.height * 0.5f;
-	p.cellSize = s->dom.cell_size;
-	p.gx = s->gx;
-	p.gy = s->gy;
-	p.ncell = s->ncell;
-	p.radius = s->dom.particle_radius;
-	p.margin = s->dom.collision_margin;
-	p.nbodies = (int)s->bodies.size();
+	p.extX = sc.gravity.x + sc.external.x;
+	p.extY = sc.gravity.y + sc.external.y;
+	p.halfW = sc.dom.width * 0.5f;
+	p.halfH = sc.dom.height * 0.5f;
+	p.cellSize = sc.dom.cell_size;
+	p.gx = sc.gx;
+	p.gy = sc.gy;
+	p.ncell = sc.ncell;
+	p.radius = sc.dom.particle_radius;
+	p.margin = sc.dom.collision_margin;
+	p.nbodies = (int)sc.bodies.size();
 	return p;
 }
 
 SimTables tables(sph_sim *s) {
 	SimTables t = s->T;
-	t.prof = s->prof;
-	t.profStride = s->prof ? (int)s->doneDCap : 0;
 	t.cellStart = s->cellStartA;
 	t.cellCount = s->cellCountA;
 	t.newStart = s->cellStartB;
 	t.newCount = s->cellCountB;
+	t.prof = s->prof;
+	t.profStride = s->prof ? (int)s->doneDCap : 0;
 	return t;
 }
 
-int blocks_for(size_t items, int threads) { return (int)std::max<size_t>(1, (items + threads - 1) / threads); }
+Totals totals(const sph_sim *s) {
+	Totals tt;
+	tt.n = (int)s->totalParticles();
+	tt.ncell = s->ncellTotal;
+	tt.nApp = s->nApp;
+	tt.nscenes = (int)s->scenes.size();
+	return tt;
+}
+
+void drop_graphs(sph_sim *s) {
+	for (int k = 0; k < 2; ++k) {
+		if (s->graphs[k]) cudaGraphExecDestroy(s->graphs[k]);
+		s->graphs[k] = nullptr;
+		s->graphKernels[k] = 0;
+	}
+	s->steadySteps = 0;
+}
+
+// Body tables of all scenes to the device (scene after scene) when they changed.
+int upload_bodies(sph_sim *s) {
+	if (!s->bodiesDirty) return SPH_OK;
+	std::vector<Body> all;
+	for (Scene &sc : s->scenes) {
+		sc.bodyBase = (int)all.size();
+		all.insert(all.end(), sc.bodies.begin(), sc.bodies.end());
+	}
+	if (all.size() > s->bodyCap) return SPH_ERR_CAPACITY;
+	// A pageable source: the call returns once the bytes are staged.
+	if (!all.empty())
+		SPH_CUDA(cudaMemcpyAsync(s->T.bodies, all.data(), all.size() * sizeof(Body), cudaMemcpyHostToDevice,
+		                         s->stream));
+	s->bodiesDirty = false;
+	s->sceneTableDirty = true;
+	return SPH_OK;
+}
+
+// Scene table (step scalars, offsets, counts) to the device when it changed.
+int upload_scenes(sph_sim *s, float dt) {
+	int rc = upload_bodies(s);
+	if (rc) return rc;
+	if (!s->sceneTableDirty && dt == s->tableDt) return SPH_OK;
+	std::vector<SceneDev> host(s->scenes.size());
+	for (size_t k = 0; k < s->scenes.size(); ++k) {
+		const Scene &sc = s->scenes[k];
+		SceneDev &d = host[k];
+		std::memset(&d, 0, sizeof(d));
+		d.p = step_params(sc, dt);
+		d.cellBase = sc.cellBase;
+		d.pBase = sc.pBase;
+		d.n = (int)sc.nDev;
+		d.n0 = (int)sc.n0;
+		d.bodyBase = sc.bodyBase;
+		d.nbSeed = sc.dom.max_neighbors;
+	}
+	SPH_CUDA(cudaMemcpyAsync(s->T.scenes, host.data(), host.size() * sizeof(SceneDev), cudaMemcpyHostToDevice,
+	                         s->stream));
+	drop_graphs(s);
+	s->sceneTableDirty = false;
+	s->tableDt = dt;
+	return SPH_OK;
+}
 
 int ensure_stage(sph_sim *s, size_t count) {
 	if (count <= s->stageCap) return SPH_OK;
@@ -172,32 +277,39 @@ int ensure_stage(sph_sim *s, size_t count) {
 // Pending AddParticle calls reach the device in order, before anything that
 // reads or changes device state.
 int flush_adds(sph_sim *s) {
-	const size_t count = s->pendPos.size();
-	if (count == 0) return SPH_OK;
-	int rc = ensure_stage(s, count);
-	if (rc != SPH_OK) return rc;
-	SPH_CUDA(cudaStreamSynchronize(s->stream));  // host staging is reused
-	std::memcpy(s->hostPos, s->pendPos.data(), count * sizeof(float2));
-	std::memcpy(s->hostForce, s->pendForce.data(), count * sizeof(float2));
-	SPH_CUDA(cudaMemcpyAsync(s->stagePos, s->hostPos, count * sizeof(float2), cudaMemcpyHostToDevice, s->stream));
-	SPH_CUDA(cudaMemcpyAsync(s->stageForce, s->hostForce, count * sizeof(float2), cudaMemcpyHostToDevice, s->stream));
-	StepParams sp = step_params(s, 1.0f);
-	k_add<<<blocks_for(count, kElemThreads), kElemThreads, 0, s->stream>>>(
-	    (int)s->nDev, (int)count, s->stagePos, s->stageForce, s->buf[s->cur].view(), tables(s), sp);
-	s->launches++;
-	SPH_CUDA(cudaGetLastError());
-	s->nDev += count;
-	s->pendPos.clear();
-	s->pendForce.clear();
+	for (size_t k = 0; k < s->scenes.size(); ++k) {
+		Scene &sc = s->scenes[k];
+		const size_t count = sc.pendPos.size();
+		if (count == 0) continue;
+		int rc = ensure_stage(s, count);
+		if (rc != SPH_OK) return rc;
+		// The cell of an added particle needs the scene's grid, not dt.
+		rc = upload_scenes(s, s->tableDt > 0.0f ? s->tableDt : 1.0f);
+		if (rc != SPH_OK) return rc;
+		SPH_CUDA(cudaStreamSynchronize(s->stream));  // host staging is reused
+		std::memcpy(s->hostPos, sc.pendPos.data(), count * sizeof(float2));
+		std::memcpy(s->hostForce, sc.pendForce.data(), count * sizeof(float2));
+		SPH_CUDA(cudaMemcpyAsync(s->stagePos, s->hostPos, count * sizeof(float2), cudaMemcpyHostToDevice, s->stream));
+		SPH_CUDA(
+		    cudaMemcpyAsync(s->stageForce, s->hostForce, count * sizeof(float2), cudaMemcpyHostToDevice, s->stream));
+		k_add<<<blocks_for(count, kElemThreads), kElemThreads, 0, s->stream>>>(
+		    sc.pBase + (int)sc.nDev, (int)count, (int)k, (int)sc.nDev, s->stagePos, s->stageForce,
+		    s->buf[s->cur].view(), tables(s));
+		SPH_LAUNCHED(s);
+		sc.nDev += count;
+		sc.pendPos.clear();
+		sc.pendForce.clear();
+		s->sceneTableDirty = true;
+	}
 	return SPH_OK;
 }
 
-int push_particle(sph_sim *s, float2 p, float2 f, size_t *index) {
-	if (s->n >= s->dom.max_particles) return SPH_ERR_CAPACITY;
-	s->pendPos.push_back(p);
-	s->pendForce.push_back(f);
-	if (index) *index = s->n;
-	s->n++;
+int push_particle(Scene &sc, float2 p, float2 f, size_t *index) {
+	if (sc.n >= sc.cap) return SPH_ERR_CAPACITY;
+	sc.pendPos.push_back(p);
+	sc.pendForce.push_back(f);
+	if (index) *index = sc.n;
+	sc.n++;
 	return SPH_OK;
 }
 
@@ -208,15 +320,15 @@ float2 random_direction() {
 	return make_float2(cosf(angle), sinf(angle));
 }
 
-float2 jitter(const sph_sim *s) {
+float2 jitter(const Scene &sc) {
 	float2 r = random_direction();
-	r = make_float2(r.x * s->dom.jitter_kernel_height, r.y * s->dom.jitter_kernel_height);
-	return make_float2(r.x * s->dom.jitter_scale, r.y * s->dom.jitter_scale);
+	r = make_float2(r.x * sc.dom.jitter_kernel_height, r.y * sc.dom.jitter_kernel_height);
+	return make_float2(r.x * sc.dom.jitter_scale, r.y * sc.dom.jitter_scale);
 }
 
 // UpdateEmitter (demo4.cpp:257-284).
-int update_emitter(sph_sim *s, Emitter &e, float dt) {
-	const float spacing = s->params.particle_spacing;
+int update_emitter(Scene &sc, Emitter &e, float dt) {
+	const float spacing = sc.params.particle_spacing;
 	const float invDt = 1.0f / dt;
 	if (!e.active) return SPH_OK;
 	const float rate = 1.0f / e.rate;
@@ -239,23 +351,13 @@ int update_emitter(sph_sim *s, Emitter &e, float dt) {
 			p = make_float2(h.x + p.x, h.y + p.y);
 			const float2 base = make_float2(e.position.x - offset.x, e.position.y - offset.y);
 			p = make_float2(base.x + p.x, base.y + p.y);
-			const float2 j = jitter(s);
+			const float2 j = jitter(sc);
 			p = make_float2(j.x + p.x, j.y + p.y);
-			int rc = push_particle(s, p, accel, nullptr);
+			int rc = push_particle(sc, p, accel, nullptr);
 			if (rc != SPH_OK) return rc;
 		}
 	}
 	if (e.totalElapsed >= e.duration) e.active = 0;
-	return SPH_OK;
-}
-
-int upload_bodies(sph_sim *s) {
-	if (!s->bodiesDirty) return SPH_OK;
-	if (!s->bodies.empty()) {
-		SPH_CUDA(cudaMemcpyAsync(s->T.bodies, s->bodies.data(), s->bodies.size() * sizeof(Body),
-		                         cudaMemcpyHostToDevice, s->stream));
-	}
-	s->bodiesDirty = false;
 	return SPH_OK;
 }
 
@@ -270,88 +372,453 @@ int check_device_errors(sph_sim *s) {
 		if (err & kErrTimeout) return SPH_ERR_TIMEOUT;
 		return SPH_ERR_DEVICE_OVERFLOW;
 	}
-	int sticky = s->stickyError;
-	s->stickyError = SPH_OK;
-	return sticky;
+	return SPH_OK;
 }
 
-#define SPH_LAUNCHED(s)                                 \
-	do {                                                \
-		(s)->launches++;                                \
-		cudaError_t e_ = cudaGetLastError();            \
-		if (e_ != cudaSuccess) return SPH_ERR_CUDA;     \
-	} while (0)
+// Appendix runs (particles added since the last update, kAppendixRun at a
+// time) of every scene as delta-sweep tasks after the canonical ones,
+// interleaved across scenes; each run waits for the previous run of its
+// scene, so a scene's appendix is relaxed in AddParticle order.
+int upload_appendix_tasks(sph_sim *s) {
+	const size_t S = s->scenes.size();
+	std::vector<int> runs(S), lastTask(S, -1);
+	int maxRuns = 0;
+	for (size_t k = 0; k < S; ++k) {
+		const Scene &sc = s->scenes[k];
+		runs[k] = (int)((sc.nDev - sc.n0 + kAppendixRun - 1) / kAppendixRun);
+		maxRuns = std::max(maxRuns, runs[k]);
+	}
+	s->nApp = 0;
+	if (maxRuns == 0) return SPH_OK;
+	std::vector<int> scene, run, prev;
+	for (int r = 0; r < maxRuns; ++r) {
+		for (size_t k = 0; k < S; ++k) {
+			if (r >= runs[k]) continue;
+			scene.push_back((int)k);
+			run.push_back(r);
+			prev.push_back(lastTask[k]);
+			lastTask[k] = s->ncellTotal + (int)scene.size() - 1;
+		}
+	}
+	if ((size_t)s->ncellTotal + scene.size() > s->doneDCap) return SPH_ERR_CAPACITY;
+	s->nApp = (int)scene.size();
+	const size_t bytes = scene.size() * sizeof(int);
+	SPH_CUDA(cudaMemcpyAsync(s->T.appScene, scene.data(), bytes, cudaMemcpyHostToDevice, s->stream));
+	SPH_CUDA(cudaMemcpyAsync(s->T.appRun, run.data(), bytes, cudaMemcpyHostToDevice, s->stream));
+	SPH_CUDA(cudaMemcpyAsync(s->T.appPrev, prev.data(), bytes, cudaMemcpyHostToDevice, s->stream));
+	return SPH_OK;
+}
 
-int run_step(sph_sim *s, float dt) {
-	const int n = (int)s->n;
-	const int n0 = (int)s->n0;
-	StepParams sp = step_params(s, dt);
+// Every launch, memset and stage event of one update, on the simulation's
+// stream (also what a per-step graph captures).
+int enqueue_step(sph_sim *s, bool capturing) {
+	const Totals tt = totals(s);
 	cudaStream_t st = s->stream;
 	BufferSet &A = s->buf[s->cur];
 	BufferSet &B = s->buf[1 - s->cur];
 	SimTables T = tables(s);
-	const int cellOrN = std::max(n, s->ncell);
+	const int cellOrN = std::max(tt.n, tt.ncell);
+	bool anyCanonical = false;
+	for (const Scene &sc : s->scenes) anyCanonical = anyCanonical || sc.n0 > 0;
+	// Under capture, stage events become event-record nodes of the graph.
+	auto mark = [&](int k) {
+		return capturing ? cudaEventRecordWithFlags(s->ev[k], st, cudaEventRecordExternal)
+		                 : cudaEventRecord(s->ev[k], st);
+	};
 
-	SPH_CUDA(cudaEventRecord(s->ev[kEvBegin], st));
-	k_integrate<<<blocks_for(cellOrN, kElemThreads), kElemThreads, 0, st>>>(n, A.view(), T, sp);
+	SPH_CUDA(mark(kEvBegin));
+	k_integrate<<<blocks_for(cellOrN, kElemThreads), kElemThreads, 0, st>>>(tt, A.view(), T);
 	SPH_LAUNCHED(s);
-	SPH_CUDA(cudaEventRecord(s->ev[kEvIntegrate], st));
+	SPH_CUDA(mark(kEvIntegrate));
 
-	if (n0 > 0) {
-		SPH_CUDA(cudaMemsetAsync(s->doneV, 0, sizeof(uint32_t) * s->ncell, st));
+	if (anyCanonical) {
+		SPH_CUDA(cudaMemsetAsync(s->doneV, 0, sizeof(uint32_t) * s->ncellTotal, st));
 		SPH_CUDA(cudaMemsetAsync(T.taskCounter, 0, sizeof(int), st));
-		k_viscosity<<<s->viscBlocks, kViscTaskWarps * kWarp, visc_smem_bytes(), st>>>(A.view(), [&] {
-			SimTables v = T;
-			v.done = s->doneV;
-			return v;
-		}(), sp);
+		SimTables v = T;
+		v.done = s->doneV;
+		k_viscosity<<<s->viscBlocks, kViscTaskWarps * kWarp, visc_smem_bytes(), st>>>(tt, A.view(), v);
 		SPH_LAUNCHED(s);
 	}
-	SPH_CUDA(cudaEventRecord(s->ev[kEvVisc], st));
+	SPH_CUDA(mark(kEvVisc));
 
-	k_predict<<<blocks_for(n, kElemThreads), kElemThreads, 0, st>>>(n, A.view(), T, sp);
+	k_predict<<<blocks_for(tt.n, kElemThreads), kElemThreads, 0, st>>>(tt, A.view(), T);
 	SPH_LAUNCHED(s);
-	SPH_CUDA(cudaEventRecord(s->ev[kEvPredict], st));
+	SPH_CUDA(mark(kEvPredict));
 
-	k_scan<<<1, kScanThreads, 0, st>>>(T, sp, s->maxNbSeed());
+	k_scan<<<1, kScanThreads, 0, st>>>(tt, T);
 	SPH_LAUNCHED(s);
-	k_scatter<<<blocks_for(n, kElemThreads), kElemThreads, 0, st>>>(n, n0, A.view(), T);
+	k_scatter<<<blocks_for(tt.n, kElemThreads), kElemThreads, 0, st>>>(tt, A.view(), T);
 	SPH_LAUNCHED(s);
-	k_grid_update<<<s->gridBlocks, kGridWarps * kWarp, 0, st>>>(n, A.view(), B.view(), T, sp);
+	k_grid_update<<<s->gridBlocks, kGridWarps * kWarp, 0, st>>>(tt, A.view(), B.view(), T);
 	SPH_LAUNCHED(s);
-	SPH_CUDA(cudaEventRecord(s->ev[kEvGrid], st));
+	SPH_CUDA(mark(kEvGrid));
 
-	k_density<<<s->densBlocks, kDensWarps * kWarp, dens_smem_bytes(), st>>>(n, B.view(), T, sp);
+	k_density<<<s->densBlocks, kDensWarps * kWarp, dens_smem_bytes(), st>>>(tt, B.view(), T);
 	SPH_LAUNCHED(s);
-	SPH_CUDA(cudaEventRecord(s->ev[kEvDensity], st));
+	SPH_CUDA(mark(kEvDensity));
 
-	const size_t runs = (size_t)(n - n0 + kAppendixRun - 1) / kAppendixRun;
-	SPH_CUDA(cudaMemsetAsync(s->doneD, 0, sizeof(uint32_t) * (s->ncell + runs), st));
+	SPH_CUDA(cudaMemsetAsync(s->doneD, 0, sizeof(uint32_t) * (s->ncellTotal + s->nApp), st));
 	SPH_CUDA(cudaMemsetAsync(T.taskCounter + 1, 0, sizeof(int), st));
 	{
 		SimTables d = T;
 		d.done = s->doneD;
-		k_delta<<<s->deltaBlocks, kDeltaTaskWarps * kWarp, delta_smem_bytes(), st>>>(n, n0, B.view(), d, sp);
+		k_delta<<<s->deltaBlocks, kDeltaTaskWarps * kWarp, delta_smem_bytes(), st>>>(tt, B.view(), d);
 		SPH_LAUNCHED(s);
 	}
-	SPH_CUDA(cudaEventRecord(s->ev[kEvDelta], st));
+	SPH_CUDA(mark(kEvDelta));
 
-	k_collide<<<blocks_for(cellOrN, kCollideThreads), kCollideThreads, 0, st>>>(n, A.view(), B.view(), T, sp);
+	k_collide<<<blocks_for(cellOrN, kCollideThreads), kCollideThreads, 0, st>>>(tt, A.view(), B.view(), T);
 	SPH_LAUNCHED(s);
-	SPH_CUDA(cudaEventRecord(s->ev[kEvCollide], st));
+	SPH_CUDA(mark(kEvCollide));
+	return SPH_OK;
+}
+
+// Capture one update into an executable graph (nothing runs).
+int capture_step(sph_sim *s, cudaGraphExec_t *out, uint64_t *kernels) {
+	SPH_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+	const uint64_t before = s->launches;
+	const int rc = enqueue_step(s, true);
+	cudaGraph_t g = nullptr;
+	const cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+	*kernels = s->launches - before;
+	s->launches = before;
+	if (rc != SPH_OK || e != cudaSuccess) {
+		if (g) cudaGraphDestroy(g);
+		cudaGetLastError();
+		return rc != SPH_OK ? rc : SPH_ERR_CUDA;
+	}
+	const cudaError_t ei = cudaGraphInstantiate(out, g, 0);
+	cudaGraphDestroy(g);
+	return cuda_status(ei);
+}
+
+int run_step(sph_sim *s, float dt) {
+	int rc = upload_scenes(s, dt);
+	if (rc) return rc;
+	rc = upload_appendix_tasks(s);
+	if (rc) return rc;
+	// A graph is captured once the same update has run eagerly (scene table,
+	// bodies and dt unchanged, no appendix), then replayed.
+	const bool replay = s->useGraphs && s->nApp == 0 && s->steadySteps >= 1;
+	if (replay) {
+		cudaGraphExec_t &g = s->graphs[s->cur];
+		if (!g) {
+			rc = capture_step(s, &g, &s->graphKernels[s->cur]);
+			if (rc) return rc;
+		}
+		SPH_CUDA(cudaGraphLaunch(g, s->stream));
+		s->launches += s->graphKernels[s->cur];
+	} else {
+		rc = enqueue_step(s, false);
+		if (rc) return rc;
+	}
+	if (s->nApp == 0) s->steadySteps++;
 
 	// The new cell arrays are the canonical ranges of the next step.
 	s->cur = 1 - s->cur;
 	std::swap(s->cellStartA, s->cellStartB);
 	std::swap(s->cellCountA, s->cellCountB);
-	s->n0 = s->n;
+	for (Scene &sc : s->scenes) {
+		if (sc.n0 != sc.nDev) s->sceneTableDirty = true;
+		sc.n0 = sc.nDev;
+	}
+	s->nApp = 0;
 	s->timed = true;
+	return SPH_OK;
+}
+
+bool valid_geometry(const sph_domain &d) {
+	if (!(d.cell_size > 0.0f) || !(d.width > 0.0f) || !(d.height > 0.0f)) return false;
+	const int gx = (int)(d.width / d.cell_size), gy = (int)(d.height / d.cell_size);
+	return gx > 0 && gy > 0 && (int64_t)gx * gy <= (1 << 26);
+}
+
+void init_scene(Scene &sc, const sph_domain &d, size_t cap) {
+	sc.dom = d;
+	sc.gx = (int)(d.width / d.cell_size);
+	sc.gy = (int)(d.height / d.cell_size);
+	sc.ncell = sc.gx * sc.gy;
+	sc.cap = cap;
+	sph_default_params(&sc.params);
+}
+
+std::vector<uint32_t> stats_seed(const sph_sim *s) {
+	// SPHStatistics() (sph.h:143-149): both minimums start at the cell capacity.
+	std::vector<uint32_t> seed(4 * s->scenes.size());
+	for (size_t k = 0; k < s->scenes.size(); ++k) {
+		seed[4 * k + 0] = s->scenes[k].dom.max_cell_particles;
+		seed[4 * k + 1] = 0;
+		seed[4 * k + 2] = s->scenes[k].dom.max_cell_particles;
+		seed[4 * k + 3] = 0;
+	}
+	return seed;
+}
+
+// Device memory and tables for the scenes described in s->scenes.
+int allocate(sph_sim *s) {
+	int64_t ncell = 0, pBase = 0;
+	for (Scene &sc : s->scenes) {
+		sc.cellBase = (int)ncell;
+		sc.pBase = (int)pBase;
+		ncell += sc.ncell;
+		pBase += (int64_t)sc.cap;
+		if (ncell > (1 << 28) || pBase > (1 << 30)) return SPH_ERR_CAPACITY;
+	}
+	s->ncellTotal = (int)ncell;
+	const size_t N = (size_t)pBase, C = (size_t)ncell, S = s->scenes.size();
+	int rc = SPH_OK;
+	if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) return SPH_ERR_CUDA;
+	for (int k = 0; k < kEvCount; ++k)
+		if (cudaEventCreate(&s->ev[k]) != cudaSuccess) return SPH_ERR_CUDA;
+	for (int b = 0; b < 2; ++b) {
+		BufferSet &B = s->buf[b];
+		if ((rc = dalloc(&B.pos, N)) || (rc = dalloc(&B.prev, N)) || (rc = dalloc(&B.vel, N)) ||
+		    (rc = dalloc(&B.acc, N)) || (rc = dalloc(&B.dens, N)) || (rc = dalloc(&B.press, N)) ||
+		    (rc = dalloc(&B.id, N)) || (rc = dalloc(&B.cellOf, N)))
+			return rc;
+	}
+	size_t bodies = 0;
+	for (const Scene &sc : s->scenes) bodies += sc.bodies.size();
+	s->bodyCap = s->batch ? std::max<size_t>(bodies, 1) : (size_t)kMaxBodies;
+	SimTables &T = s->T;
+	if ((rc = dalloc(&s->cellStartA, C)) || (rc = dalloc(&s->cellCountA, C)) || (rc = dalloc(&s->cellStartB, C)) ||
+	    (rc = dalloc(&s->cellCountB, C)) || (rc = dalloc(&T.taskOfCell, C)) || (rc = dalloc(&T.taskCell, C)) ||
+	    (rc = dalloc(&T.numberOrder, C)) || (rc = dalloc(&T.sceneOfCell, C)) || (rc = dalloc(&T.sceneOf, N)) ||
+	    (rc = dalloc(&T.scenes, S)) || (rc = dalloc(&T.appCount, C)) || (rc = dalloc(&T.appStart, C)) ||
+	    (rc = dalloc(&T.appIdx, N)) || (rc = dalloc(&T.appCursor, C)) || (rc = dalloc(&T.newCell, N)) ||
+	    (rc = dalloc(&T.enterCount, C)) || (rc = dalloc(&T.leaveCount, C)) || (rc = dalloc(&T.enterOffset, C)) ||
+	    (rc = dalloc(&T.enterCursor, C)) || (rc = dalloc(&T.enterList, N)) || (rc = dalloc(&T.moverCount, 2)) ||
+	    (rc = dalloc(&T.bbox, 4 * C)) || (rc = dalloc(&T.newIdx, N)) || (rc = dalloc(&T.newLabel, N)) ||
+	    (rc = dalloc(&T.taskCounter, 2)) || (rc = dalloc(&T.stats, 4 * S)) || (rc = dalloc(&T.error, 1)) ||
+	    (rc = dalloc(&T.abort, 1)) || (rc = dalloc(&T.bodies, s->bodyCap)) || (rc = dalloc(&s->doneV, C)))
+		return rc;
+	// Appendix runs: at most one partial run per scene beyond N / kAppendixRun.
+	const size_t appCap = (N + kAppendixRun - 1) / kAppendixRun + S + 1;
+	s->doneDCap = C + appCap;
+	if ((rc = dalloc(&s->doneD, s->doneDCap)) || (rc = dalloc(&T.appScene, appCap)) ||
+	    (rc = dalloc(&T.appRun, appCap)) || (rc = dalloc(&T.appPrev, appCap)))
+		return rc;
+	T.moverList = nullptr;
+
+	// Per scene: colour-major cell rank -- colour (y%3, x%3), then sub-colour
+	// ((y/3)%2, (x/3)%2), then row-major.  Cells of one colour are >= 3
+	// apart; within a colour, the sub-colour order keeps conflicts between
+	// cells that particles move across short.  Particles are numbered scene
+	// after scene in that order.  The sweep tasks interleave the scenes by
+	// relative rank, so that every scene's ordered sweep advances at once.
+	std::vector<int> numberOrder, sceneOfCell(C), taskCell(C), taskOfCell(C);
+	std::vector<std::pair<double, int>> interleave;
+	numberOrder.reserve(C);
+	interleave.reserve(C);
+	for (size_t k = 0; k < S; ++k) {
+		const Scene &sc = s->scenes[k];
+		std::vector<int> order(sc.ncell);
+		for (int c = 0; c < sc.ncell; ++c) order[c] = c;
+		const int gx = sc.gx;
+		auto key = [gx](int c) {
+			const int x = c % gx, y = c / gx;
+			return (int64_t)(((y % 3) * 3 + (x % 3)) * 4 + ((y / 3) % 2) * 2 + ((x / 3) % 2)) * (int64_t)(1 << 26) + c;
+		};
+		std::sort(order.begin(), order.end(), [&](int a, int b) { return key(a) < key(b); });
+		for (int r = 0; r < sc.ncell; ++r) {
+			const int g = sc.cellBase + order[r];
+			numberOrder.push_back(g);
+			sceneOfCell[g] = (int)k;
+			interleave.push_back({(double)r / (double)sc.ncell, g});
+		}
+	}
+	// Stable: equal fractions keep scene order; within a scene the rank
+	// order is kept because the fraction grows with the rank.
+	std::stable_sort(interleave.begin(), interleave.end(),
+	                 [](const std::pair<double, int> &a, const std::pair<double, int> &b) { return a.first < b.first; });
+	for (size_t t = 0; t < C; ++t) {
+		taskCell[t] = interleave[t].second;
+		taskOfCell[interleave[t].second] = (int)t;
+	}
+	std::vector<int> sceneOf(std::max<size_t>(N, 1), 0);
+	for (size_t k = 0; k < S; ++k)
+		for (size_t j = 0; j < s->scenes[k].cap; ++j) sceneOf[s->scenes[k].pBase + j] = (int)k;
+	const std::vector<uint32_t> seed = stats_seed(s);
+	if (cudaMemcpy(T.numberOrder, numberOrder.data(), C * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+	    cudaMemcpy(T.sceneOfCell, sceneOfCell.data(), C * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+	    cudaMemcpy(T.taskCell, taskCell.data(), C * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+	    cudaMemcpy(T.taskOfCell, taskOfCell.data(), C * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+	    cudaMemcpy(T.sceneOf, sceneOf.data(), sceneOf.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+	    cudaMemcpy(T.stats, seed.data(), seed.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+		return SPH_ERR_CUDA;
+
+	cudaDeviceProp prop;
+	if (cudaGetDeviceProperties(&prop, s->device) != cudaSuccess) return SPH_ERR_CUDA;
+	s->numSMs = prop.multiProcessorCount;
+	if (cudaFuncSetAttribute(k_viscosity, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)visc_smem_bytes()) !=
+	        cudaSuccess ||
+	    cudaFuncSetAttribute(k_delta, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)delta_smem_bytes()) !=
+	        cudaSuccess ||
+	    cudaFuncSetAttribute(k_density, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dens_smem_bytes()) !=
+	        cudaSuccess)
+		return SPH_ERR_CUDA;
+	int occ = 0;
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_viscosity, kViscTaskWarps * kWarp, visc_smem_bytes()) !=
+	        cudaSuccess ||
+	    occ < 1)
+		return SPH_ERR_CUDA;
+	s->viscBlocks = occ * s->numSMs;
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_delta, kDeltaTaskWarps * kWarp, delta_smem_bytes()) !=
+	        cudaSuccess ||
+	    occ < 1)
+		return SPH_ERR_CUDA;
+	s->deltaBlocks = occ * s->numSMs;
+	s->densBlocks = std::max(1, std::min(blocks_for(C, kDensWarps), 64 * s->numSMs));
+	s->gridBlocks = std::max(1, std::min(blocks_for(C, kGridWarps), 64 * s->numSMs));
+	return SPH_OK;
+}
+
+int create_common(sph_sim *s, int device) {
+	int devices = 0;
+	if (cudaGetDeviceCount(&devices) != cudaSuccess || devices == 0) return SPH_ERR_NO_DEVICE;
+	if (device < 0 || device >= devices) return SPH_ERR_INVALID_ARGUMENT;
+	SPH_CUDA(cudaSetDevice(device));
+	s->device = device;
+	return allocate(s);
+}
+
+// Scene 0 of a single-scene simulation: what the reference interface mutates.
+Scene *single(sph_sim *s) { return (s && !s->batch) ? &s->scenes[0] : nullptr; }
+int not_single(sph_sim *s) { return s ? SPH_ERR_NOT_SUPPORTED : SPH_ERR_INVALID_ARGUMENT; }
+
+int push_body(sph_sim *s, const Body &b) {
+	Scene *sc = single(s);
+	if (!sc) return not_single(s);
+	if (sc->bodies.size() >= (size_t)kMaxBodies) return SPH_ERR_CAPACITY;
+	sc->bodies.push_back(b);
+	s->bodiesDirty = true;
+	return SPH_OK;
+}
+
+Body plane_body(sph_vec2 normal, float distance) {
+	Body b{};
+	b.type = kBodyPlane;
+	b.ax = normal.x;
+	b.ay = normal.y;
+	b.r = distance;
+	return b;
+}
+
+Body circle_body(sph_vec2 pos, float radius) {
+	Body b{};
+	b.type = kBodyCircle;
+	b.ax = pos.x;
+	b.ay = pos.y;
+	b.r = radius;
+	return b;
+}
+
+Body segment_body(sph_vec2 a, sph_vec2 bb) {
+	Body b{};
+	b.type = kBodySegment;
+	b.ax = a.x;
+	b.ay = a.y;
+	b.bx = bb.x;
+	b.by = bb.y;
+	return b;
+}
+
+Body polygon_body(size_t count, const sph_vec2 *verts) {
+	Body b{};
+	b.type = kBodyPolygon;
+	b.vertexCount = (int)count;
+	for (size_t k = 0; k < count; ++k) {
+		b.verts[2 * k] = verts[k].x;
+		b.verts[2 * k + 1] = verts[k].y;
+	}
+	return b;
+}
+
+int body_from_desc(const sph_body_desc &d, Body *out) {
+	switch (d.type) {
+		case SPH_BODY_PLANE: *out = plane_body(d.a, d.value); return SPH_OK;
+		case SPH_BODY_CIRCLE: *out = circle_body(d.a, d.value); return SPH_OK;
+		case SPH_BODY_SEGMENT: *out = segment_body(d.a, d.b); return SPH_OK;
+		case SPH_BODY_POLYGON:
+			if (d.vertex_count > (size_t)kMaxPoly) return SPH_ERR_CAPACITY;
+			*out = polygon_body(d.vertex_count, d.verts);
+			return SPH_OK;
+		default: return SPH_ERR_INVALID_ARGUMENT;
+	}
+}
+
+int read_scene(sph_sim *s, size_t scene, size_t count, sph_vec2 *pos, sph_vec2 *prev, sph_vec2 *vel, sph_vec2 *acc,
+               sph_vec2 *dens, sph_vec2 *press) {
+	if (!s || scene >= s->scenes.size()) return SPH_ERR_INVALID_ARGUMENT;
+	int rc = flush_adds(s);
+	if (rc) return rc;
+	const Scene &sc = s->scenes[scene];
+	if (count > sc.n) return SPH_ERR_INVALID_ARGUMENT;
+	const int n = (int)sc.n;
+	BufferSet &A = s->buf[s->cur];
+	BufferSet &Z = s->buf[1 - s->cur];  // free between updates: scratch
+	struct Item {
+		float2 *src, *scratch;
+		sph_vec2 *dst;
+	} items[] = {{A.pos, Z.pos, pos}, {A.prev, Z.prev, prev}, {A.vel, Z.vel, vel},
+	             {A.acc, Z.acc, acc}, {A.dens, Z.dens, dens}, {A.press, Z.press, press}};
+	for (const Item &it : items) {
+		if (!it.dst || count == 0) continue;
+		float2 *dst = it.scratch + sc.pBase;
+		k_gather_by_id<<<blocks_for(n, kElemThreads), kElemThreads, 0, s->stream>>>(sc.pBase, n, A.id, it.src, dst);
+		SPH_LAUNCHED(s);
+		SPH_CUDA(cudaMemcpyAsync(it.dst, dst, count * sizeof(float2), cudaMemcpyDeviceToHost, s->stream));
+	}
+	return check_device_errors(s);
+}
+
+int scene_info(sph_sim *s, size_t scene, size_t *count, size_t *canonical, int *gx, int *gy) {
+	if (!s || scene >= s->scenes.size()) return SPH_ERR_INVALID_ARGUMENT;
+	int rc = flush_adds(s);
+	if (rc) return rc;
+	const Scene &sc = s->scenes[scene];
+	if (count) *count = sc.n;
+	if (canonical) *canonical = sc.n0;
+	if (gx) *gx = sc.gx;
+	if (gy) *gy = sc.gy;
+	return SPH_OK;
+}
+
+// The state of one scene in scene-local numbers and cells.
+int dump_scene(sph_sim *s, size_t scene, const sph_state_view *v) {
+	if (!s || !v || scene >= s->scenes.size()) return SPH_ERR_INVALID_ARGUMENT;
+	int rc = flush_adds(s);
+	if (rc) return rc;
+	const Scene &sc = s->scenes[scene];
+	if (v->count != sc.n) return SPH_ERR_INVALID_ARGUMENT;
+	const size_t n = sc.n, p0 = (size_t)sc.pBase, c0 = (size_t)sc.cellBase;
+	BufferSet &A = s->buf[s->cur];
+	cudaStream_t st = s->stream;
+	auto d2h = [&](void *dst, const void *src, size_t bytes) -> int {
+		if (!dst || bytes == 0) return SPH_OK;
+		return cuda_status(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st));
+	};
+	if ((rc = d2h(v->pos, A.pos + p0, n * 8)) || (rc = d2h(v->prev, A.prev + p0, n * 8)) ||
+	    (rc = d2h(v->vel, A.vel + p0, n * 8)) || (rc = d2h(v->acc, A.acc + p0, n * 8)) ||
+	    (rc = d2h(v->dens, A.dens + p0, n * 8)) || (rc = d2h(v->press, A.press + p0, n * 8)) ||
+	    (rc = d2h(v->id, A.id + p0, n * 4)) || (rc = d2h(v->cell, A.cellOf + p0, n * 4)) ||
+	    (rc = d2h(v->cell_start, s->cellStartA + c0, sc.ncell * 4)) ||
+	    (rc = d2h(v->cell_count, s->cellCountA + c0, sc.ncell * 4)))
+		return rc;
+	rc = check_device_errors(s);
+	if (rc) return rc;
+	if (v->cell && c0 != 0)
+		for (size_t k = 0; k < n; ++k) v->cell[k] -= (int32_t)c0;
+	if (v->cell_start && p0 != 0)
+		for (int c = 0; c < sc.ncell; ++c) v->cell_start[c] -= (int32_t)p0;
 	return SPH_OK;
 }
 
 }  // namespace
 
 extern "C" {
+
+const char *sph_last_error(void) { return g_last_error; }
 
 const char *sph_status_string(int status) {
 	switch (status) {
@@ -402,99 +869,67 @@ int sph_default_params(sph_params *p) {
 int sph_create(const sph_domain *domain, int device, sph_sim **out) {
 	if (!domain || !out) return SPH_ERR_INVALID_ARGUMENT;
 	*out = nullptr;
-	if (!(domain->cell_size > 0.0f) || !(domain->width > 0.0f) || !(domain->height > 0.0f) ||
-	    domain->max_particles == 0 || domain->max_particles > (1u << 30))
+	if (!valid_geometry(*domain) || domain->max_particles == 0 || domain->max_particles > (1u << 30))
 		return SPH_ERR_INVALID_ARGUMENT;
-	int devices = 0;
-	if (cudaGetDeviceCount(&devices) != cudaSuccess || devices == 0) return SPH_ERR_NO_DEVICE;
-	if (device < 0 || device >= devices) return SPH_ERR_INVALID_ARGUMENT;
-	SPH_CUDA(cudaSetDevice(device));
 	sph_sim *s = new (std::nothrow) sph_sim();
 	if (!s) return SPH_ERR_CAPACITY;
-	s->device = device;
-	s->dom = *domain;
-	s->gx = (int)(domain->width / domain->cell_size);
-	s->gy = (int)(domain->height / domain->cell_size);
-	if (s->gx <= 0 || s->gy <= 0 || (int64_t)s->gx * s->gy > (1 << 26)) {
-		delete s;
-		return SPH_ERR_INVALID_ARGUMENT;
-	}
-	s->ncell = s->gx * s->gy;
-	sph_default_params(&s->params);
-	int rc = SPH_OK;
-	auto fail = [&](int code) {
+	s->scenes.resize(1);
+	init_scene(s->scenes[0], *domain, domain->max_particles);
+	int rc = create_common(s, device);
+	if (rc == SPH_OK) rc = cuda_status(cudaStreamSynchronize(s->stream));
+	if (rc != SPH_OK) {
 		sph_destroy(s);
-		return code;
-	};
-	if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(SPH_ERR_CUDA);
-	for (int k = 0; k < kEvCount; ++k)
-		if (cudaEventCreate(&s->ev[k]) != cudaSuccess) return fail(SPH_ERR_CUDA);
-	const size_t N = domain->max_particles, C = (size_t)s->ncell;
-	for (int b = 0; b < 2; ++b) {
-		BufferSet &B = s->buf[b];
-		if ((rc = dalloc(&B.pos, N)) || (rc = dalloc(&B.prev, N)) || (rc = dalloc(&B.vel, N)) ||
-		    (rc = dalloc(&B.acc, N)) || (rc = dalloc(&B.dens, N)) || (rc = dalloc(&B.press, N)) ||
-		    (rc = dalloc(&B.id, N)) || (rc = dalloc(&B.cellOf, N)))
-			return fail(rc);
+		return rc;
 	}
-	SimTables &T = s->T;
-	if ((rc = dalloc(&s->cellStartA, C)) || (rc = dalloc(&s->cellCountA, C)) || (rc = dalloc(&s->cellStartB, C)) ||
-	    (rc = dalloc(&s->cellCountB, C)) || (rc = dalloc(&T.rankOfCell, C)) || (rc = dalloc(&T.cellOfRank, C)) ||
-	    (rc = dalloc(&T.appCount, C)) || (rc = dalloc(&T.appStart, C)) || (rc = dalloc(&T.appIdx, N)) ||
-	    (rc = dalloc(&T.appCursor, C)) || (rc = dalloc(&T.newCell, N)) || (rc = dalloc(&T.enterCount, C)) ||
-	    (rc = dalloc(&T.leaveCount, C)) || (rc = dalloc(&T.enterOffset, C)) || (rc = dalloc(&T.enterCursor, C)) ||
-	    (rc = dalloc(&T.enterList, N)) || (rc = dalloc(&T.moverCount, 2)) || (rc = dalloc(&T.bbox, 4 * C)) ||
-	    (rc = dalloc(&T.newIdx, N)) || (rc = dalloc(&T.newLabel, N)) || (rc = dalloc(&T.taskCounter, 2)) ||
-	    (rc = dalloc(&T.stats, 4)) || (rc = dalloc(&T.error, 1)) || (rc = dalloc(&T.abort, 1)) ||
-	    (rc = dalloc(&T.bodies, kMaxBodies)) || (rc = dalloc(&s->doneV, C)))
-		return fail(rc);
-	s->doneDCap = C + (N + kAppendixRun - 1) / kAppendixRun + 1;
-	if ((rc = dalloc(&s->doneD, s->doneDCap))) return fail(rc);
-	T.moverList = nullptr;
-
-	// Colour-major cell rank: colour (y%3, x%3), then sub-colour
-	// ((y/3)%2, (x/3)%2), then row-major.  Cells of one colour are >= 3 apart;
-	// within a colour, the sub-colour order keeps conflicts between cells that
-	// particles move across short.
-	std::vector<int> order(C), rank(C);
-	for (size_t c = 0; c < C; ++c) order[c] = (int)c;
-	const int gx = s->gx;
-	auto key = [gx](int c) {
-		const int x = c % gx, y = c / gx;
-		return (int64_t)(((y % 3) * 3 + (x % 3)) * 4 + ((y / 3) % 2) * 2 + ((x / 3) % 2)) * (int64_t)(1 << 26) + c;
-	};
-	std::sort(order.begin(), order.end(), [&](int a, int b) { return key(a) < key(b); });
-	for (size_t r = 0; r < C; ++r) rank[order[r]] = (int)r;
-	if (cudaMemcpy(T.cellOfRank, order.data(), C * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
-	    cudaMemcpy(T.rankOfCell, rank.data(), C * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
-		return fail(SPH_ERR_CUDA);
-
-	cudaDeviceProp prop;
-	if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return fail(SPH_ERR_CUDA);
-	s->numSMs = prop.multiProcessorCount;
-	if (cudaFuncSetAttribute(k_viscosity, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)visc_smem_bytes()) !=
-	        cudaSuccess ||
-	    cudaFuncSetAttribute(k_delta, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)delta_smem_bytes()) !=
-	        cudaSuccess ||
-	    cudaFuncSetAttribute(k_density, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dens_smem_bytes()) !=
-	        cudaSuccess)
-		return fail(SPH_ERR_CUDA);
-	int occ = 0;
-	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_viscosity, kViscTaskWarps * kWarp, visc_smem_bytes()) !=
-	        cudaSuccess ||
-	    occ < 1)
-		return fail(SPH_ERR_CUDA);
-	s->viscBlocks = occ * s->numSMs;
-	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_delta, kDeltaTaskWarps * kWarp, delta_smem_bytes()) !=
-	        cudaSuccess ||
-	    occ < 1)
-		return fail(SPH_ERR_CUDA);
-	s->deltaBlocks = occ * s->numSMs;
-	s->densBlocks = std::max(1, std::min(blocks_for(C, kDensWarps), 64 * s->numSMs));
-	s->gridBlocks = std::max(1, std::min(blocks_for(C, kGridWarps), 64 * s->numSMs));
-	sph_reset_stats(s);
-	if (cudaStreamSynchronize(s->stream) != cudaSuccess) return fail(SPH_ERR_CUDA);
 	*out = s;
+	return SPH_OK;
+}
+
+int sph_batch_create(const sph_scene_desc *descs, size_t scene_count, int device, sph_sim **out) {
+	if (!descs || !out || scene_count == 0) return SPH_ERR_INVALID_ARGUMENT;
+	*out = nullptr;
+	for (size_t k = 0; k < scene_count; ++k) {
+		const sph_scene_desc &d = descs[k];
+		if (!valid_geometry(d.domain) || (d.particle_count > 0 && !d.positions) || (d.body_count > 0 && !d.bodies) ||
+		    d.particle_count > (size_t)(1u << 30))
+			return SPH_ERR_INVALID_ARGUMENT;
+	}
+	sph_sim *s = new (std::nothrow) sph_sim();
+	if (!s) return SPH_ERR_CAPACITY;
+	s->batch = true;
+	s->scenes.resize(scene_count);
+	int rc = SPH_OK;
+	for (size_t k = 0; rc == SPH_OK && k < scene_count; ++k) {
+		const sph_scene_desc &d = descs[k];
+		Scene &sc = s->scenes[k];
+		init_scene(sc, d.domain, d.particle_count);
+		sc.params = d.params;
+		sc.gravity = d.gravity;
+		for (size_t b = 0; rc == SPH_OK && b < d.body_count; ++b) {
+			Body body;
+			rc = body_from_desc(d.bodies[b], &body);
+			if (rc == SPH_OK && sc.bodies.size() >= (size_t)kMaxBodies) rc = SPH_ERR_CAPACITY;
+			if (rc == SPH_OK) sc.bodies.push_back(body);
+		}
+		for (size_t j = 0; rc == SPH_OK && j < d.particle_count; ++j) {
+			const float2 f = d.forces ? make_float2(d.forces[j].x, d.forces[j].y) : make_float2(0.0f, 0.0f);
+			push_particle(sc, make_float2(d.positions[j].x, d.positions[j].y), f, nullptr);
+		}
+	}
+	if (rc == SPH_OK) rc = create_common(s, device);
+	if (rc == SPH_OK) rc = flush_adds(s);
+	if (rc == SPH_OK) rc = check_device_errors(s);
+	if (rc != SPH_OK) {
+		sph_destroy(s);
+		return rc;
+	}
+	*out = s;
+	return SPH_OK;
+}
+
+int sph_batch_scene_count(sph_sim *s, size_t *out) {
+	if (!s || !out) return SPH_ERR_INVALID_ARGUMENT;
+	*out = s->scenes.size();
 	return SPH_OK;
 }
 
@@ -502,23 +937,21 @@ int sph_destroy(sph_sim *s) {
 	if (!s) return SPH_ERR_INVALID_ARGUMENT;
 	cudaSetDevice(s->device);
 	if (s->stream) cudaStreamSynchronize(s->stream);
+	drop_graphs(s);
 	for (int b = 0; b < 2; ++b) {
 		BufferSet &B = s->buf[b];
-		cudaFree(B.pos);
-		cudaFree(B.prev);
-		cudaFree(B.vel);
-		cudaFree(B.acc);
-		cudaFree(B.dens);
-		cudaFree(B.press);
-		cudaFree(B.id);
-		cudaFree(B.cellOf);
+		void *ptrs[] = {B.pos, B.prev, B.vel, B.acc, B.dens, B.press, B.id, B.cellOf};
+		for (void *p : ptrs)
+			if (p) cudaFree(p);
 	}
 	SimTables &T = s->T;
-	void *ptrs[] = {s->cellStartA, s->cellCountA, s->cellStartB, s->cellCountB, T.rankOfCell, T.cellOfRank,
-	                T.appCount,    T.appStart,    T.appIdx,      T.appCursor,   T.newCell,     T.enterCount,
-	                T.leaveCount,  T.enterOffset, T.enterCursor, T.enterList,   T.moverCount,  T.bbox,
-	                T.newIdx,      T.newLabel, T.taskCounter, T.stats,      T.error,       T.abort,
-	                T.bodies,      s->doneV,      s->doneD,      s->stagePos,   s->stageForce, s->prof};
+	void *ptrs[] = {s->cellStartA, s->cellCountA, s->cellStartB, s->cellCountB, T.taskOfCell,  T.taskCell,
+	                T.numberOrder, T.sceneOfCell, T.sceneOf,     T.scenes,      T.appScene,    T.appRun,
+	                T.appPrev,     T.appCount,    T.appStart,    T.appIdx,      T.appCursor,   T.newCell,
+	                T.enterCount,  T.leaveCount,  T.enterOffset, T.enterCursor, T.enterList,   T.moverCount,
+	                T.bbox,        T.newIdx,      T.newLabel,    T.taskCounter, T.stats,       T.error,
+	                T.abort,       T.bodies,      s->doneV,      s->doneD,      s->stagePos,   s->stageForce,
+	                s->prof};
 	for (void *p : ptrs)
 		if (p) cudaFree(p);
 	if (s->hostPos) cudaFreeHost(s->hostPos);
@@ -534,9 +967,8 @@ int sph_reset_stats(sph_sim *s) {
 	if (!s) return SPH_ERR_INVALID_ARGUMENT;
 	int rc = flush_adds(s);
 	if (rc) return rc;
-	// SPHStatistics() (sph.h:143-149): both minimums start at the cell capacity.
-	const uint32_t seed[4] = {s->dom.max_cell_particles, 0u, s->dom.max_cell_particles, 0u};
-	SPH_CUDA(cudaMemcpyAsync(s->T.stats, seed, sizeof(seed), cudaMemcpyHostToDevice, s->stream));
+	const std::vector<uint32_t> seed = stats_seed(s);
+	SPH_CUDA(cudaMemcpyAsync(s->T.stats, seed.data(), seed.size() * 4, cudaMemcpyHostToDevice, s->stream));
 	SPH_CUDA(cudaStreamSynchronize(s->stream));
 	s->timed = false;
 	s->emitterMs = 0.0f;
@@ -544,100 +976,70 @@ int sph_reset_stats(sph_sim *s) {
 }
 
 int sph_clear_bodies(sph_sim *s) {
-	if (!s) return SPH_ERR_INVALID_ARGUMENT;
-	s->bodies.clear();
+	Scene *sc = single(s);
+	if (!sc) return not_single(s);
+	sc->bodies.clear();
 	s->bodiesDirty = true;
 	return SPH_OK;
 }
 
 int sph_clear_particles(sph_sim *s) {
-	if (!s) return SPH_ERR_INVALID_ARGUMENT;
-	s->pendPos.clear();
-	s->pendForce.clear();
-	SPH_CUDA(cudaMemsetAsync(s->cellCountA, 0, sizeof(int) * s->ncell, s->stream));
-	SPH_CUDA(cudaMemsetAsync(s->cellStartA, 0, sizeof(int) * s->ncell, s->stream));
-	SPH_CUDA(cudaMemsetAsync(s->T.appCount, 0, sizeof(int) * s->ncell, s->stream));
-	s->n = s->n0 = s->nDev = 0;
+	Scene *sc = single(s);
+	if (!sc) return not_single(s);
+	sc->pendPos.clear();
+	sc->pendForce.clear();
+	SPH_CUDA(cudaMemsetAsync(s->cellCountA, 0, sizeof(int) * s->ncellTotal, s->stream));
+	SPH_CUDA(cudaMemsetAsync(s->cellStartA, 0, sizeof(int) * s->ncellTotal, s->stream));
+	SPH_CUDA(cudaMemsetAsync(s->T.appCount, 0, sizeof(int) * s->ncellTotal, s->stream));
+	sc->n = sc->n0 = sc->nDev = 0;
+	s->sceneTableDirty = true;
 	return SPH_OK;
 }
 
 int sph_clear_emitters(sph_sim *s) {
-	if (!s) return SPH_ERR_INVALID_ARGUMENT;
-	s->emitters.clear();
+	Scene *sc = single(s);
+	if (!sc) return not_single(s);
+	sc->emitters.clear();
 	return SPH_OK;
 }
 
-static int push_body(sph_sim *s, const Body &b) {
-	if (s->bodies.size() >= (size_t)kMaxBodies) return SPH_ERR_CAPACITY;
-	s->bodies.push_back(b);
-	s->bodiesDirty = true;
-	return SPH_OK;
-}
+int sph_add_plane(sph_sim *s, sph_vec2 normal, float distance) { return push_body(s, plane_body(normal, distance)); }
 
-int sph_add_plane(sph_sim *s, sph_vec2 normal, float distance) {
-	if (!s) return SPH_ERR_INVALID_ARGUMENT;
-	Body b{};
-	b.type = kBodyPlane;
-	b.ax = normal.x;
-	b.ay = normal.y;
-	b.r = distance;
-	return push_body(s, b);
-}
+int sph_add_circle(sph_sim *s, sph_vec2 pos, float radius) { return push_body(s, circle_body(pos, radius)); }
 
-int sph_add_circle(sph_sim *s, sph_vec2 pos, float radius) {
-	if (!s) return SPH_ERR_INVALID_ARGUMENT;
-	Body b{};
-	b.type = kBodyCircle;
-	b.ax = pos.x;
-	b.ay = pos.y;
-	b.r = radius;
-	return push_body(s, b);
-}
-
-int sph_add_line_segment(sph_sim *s, sph_vec2 a, sph_vec2 bb) {
-	if (!s) return SPH_ERR_INVALID_ARGUMENT;
-	Body b{};
-	b.type = kBodySegment;
-	b.ax = a.x;
-	b.ay = a.y;
-	b.bx = bb.x;
-	b.by = bb.y;
-	return push_body(s, b);
-}
+int sph_add_line_segment(sph_sim *s, sph_vec2 a, sph_vec2 b) { return push_body(s, segment_body(a, b)); }
 
 int sph_add_polygon(sph_sim *s, size_t count, const sph_vec2 *verts) {
 	if (!s || (count > 0 && !verts)) return SPH_ERR_INVALID_ARGUMENT;
 	if (count > (size_t)kMaxPoly) return SPH_ERR_CAPACITY;
-	Body b{};
-	b.type = kBodyPolygon;
-	b.vertexCount = (int)count;
-	for (size_t k = 0; k < count; ++k) {
-		b.verts[2 * k] = verts[k].x;
-		b.verts[2 * k + 1] = verts[k].y;
-	}
-	return push_body(s, b);
+	return push_body(s, polygon_body(count, verts));
 }
 
 int sph_add_particle(sph_sim *s, sph_vec2 position, sph_vec2 force, size_t *out_index) {
-	if (!s) return SPH_ERR_INVALID_ARGUMENT;
-	return push_particle(s, make_float2(position.x, position.y), make_float2(force.x, force.y), out_index);
+	Scene *sc = single(s);
+	if (!sc) return not_single(s);
+	return push_particle(*sc, make_float2(position.x, position.y), make_float2(force.x, force.y), out_index);
 }
 
 int sph_add_particles(sph_sim *s, size_t count, const sph_vec2 *positions, const sph_vec2 *forces,
                       size_t *first_index) {
-	if (!s || (count > 0 && !positions)) return SPH_ERR_INVALID_ARGUMENT;
-	if (s->n + count > s->dom.max_particles) return SPH_ERR_CAPACITY;
-	if (first_index) *first_index = s->n;
+	Scene *sc = single(s);
+	if (!sc) return not_single(s);
+	if (count > 0 && !positions) return SPH_ERR_INVALID_ARGUMENT;
+	if (sc->n + count > sc->cap) return SPH_ERR_CAPACITY;
+	if (first_index) *first_index = sc->n;
 	for (size_t k = 0; k < count; ++k) {
 		const float2 f = forces ? make_float2(forces[k].x, forces[k].y) : make_float2(0.0f, 0.0f);
-		push_particle(s, make_float2(positions[k].x, positions[k].y), f, nullptr);
+		push_particle(*sc, make_float2(positions[k].x, positions[k].y), f, nullptr);
 	}
 	return SPH_OK;
 }
 
 int sph_add_volume(sph_sim *s, sph_vec2 center, sph_vec2 force, int count_x, int count_y, float spacing) {
-	if (!s || count_x < 0 || count_y < 0) return SPH_ERR_INVALID_ARGUMENT;
-	if (s->n + (size_t)count_x * (size_t)count_y > s->dom.max_particles) return SPH_ERR_CAPACITY;
+	Scene *sc = single(s);
+	if (!sc) return not_single(s);
+	if (count_x < 0 || count_y < 0) return SPH_ERR_INVALID_ARGUMENT;
+	if (sc->n + (size_t)count_x * (size_t)count_y > sc->cap) return SPH_ERR_CAPACITY;
 	// AddVolume (demo4.cpp:169-181), same operation order.
 	float2 offset = make_float2((float)count_x * spacing, (float)count_y * spacing);
 	offset = make_float2(offset.x * 0.5f, offset.y * 0.5f);
@@ -649,9 +1051,9 @@ int sph_add_volume(sph_sim *s, sph_vec2 center, sph_vec2 force, int count_x, int
 			p = make_float2(hs + p.x, hs + p.y);
 			const float2 base = make_float2(center.x - offset.x, center.y - offset.y);
 			p = make_float2(base.x + p.x, base.y + p.y);
-			const float2 j = jitter(s);
+			const float2 j = jitter(*sc);
 			p = make_float2(j.x + p.x, j.y + p.y);
-			push_particle(s, p, f, nullptr);
+			push_particle(*sc, p, f, nullptr);
 		}
 	}
 	return SPH_OK;
@@ -659,8 +1061,9 @@ int sph_add_volume(sph_sim *s, sph_vec2 center, sph_vec2 force, int count_x, int
 
 int sph_add_emitter(sph_sim *s, sph_vec2 position, sph_vec2 direction, float radius, float speed, float rate,
                     float duration) {
-	if (!s) return SPH_ERR_INVALID_ARGUMENT;
-	if (s->emitters.size() >= 8) return SPH_ERR_CAPACITY;  // kSPHMaxEmitterCount
+	Scene *sc = single(s);
+	if (!sc) return not_single(s);
+	if (sc->emitters.size() >= 8) return SPH_ERR_CAPACITY;  // kSPHMaxEmitterCount
 	Emitter e{};
 	e.position = position;
 	e.direction = direction;
@@ -671,7 +1074,7 @@ int sph_add_emitter(sph_sim *s, sph_vec2 position, sph_vec2 direction, float rad
 	e.elapsed = 0;
 	e.totalElapsed = 0;
 	e.active = 1;
-	s->emitters.push_back(e);
+	sc->emitters.push_back(e);
 	return SPH_OK;
 }
 
@@ -682,9 +1085,11 @@ int sph_update(sph_sim *s, float dt) {
 	int rc = flush_adds(s);
 	if (rc) return rc;
 	const auto t0 = std::chrono::high_resolution_clock::now();
-	for (Emitter &e : s->emitters) {
-		rc = update_emitter(s, e, dt);
-		if (rc) return rc;
+	for (Scene &sc : s->scenes) {
+		for (Emitter &e : sc.emitters) {
+			rc = update_emitter(sc, e, dt);
+			if (rc) return rc;
+		}
 	}
 	rc = flush_adds(s);
 	if (rc) return rc;
@@ -692,11 +1097,13 @@ int sph_update(sph_sim *s, float dt) {
 	                   std::chrono::high_resolution_clock::now() - t0)
 	                   .count() *
 	               (1.0f / 1000000);
-	rc = upload_bodies(s);
-	if (rc) return rc;
-	if (s->n == 0) {
-		const uint32_t seed[2] = {s->dom.max_neighbors, 0u};
-		SPH_CUDA(cudaMemcpyAsync(s->T.stats, seed, sizeof(seed), cudaMemcpyHostToDevice, s->stream));
+	if (s->totalParticles() == 0) {
+		// NeighborSearch restarts the neighbour statistics even with no particles.
+		for (size_t k = 0; k < s->scenes.size(); ++k) {
+			const uint32_t seed[2] = {s->scenes[k].dom.max_neighbors, 0u};
+			SPH_CUDA(cudaMemcpyAsync(s->T.stats + 4 * k, seed, sizeof(seed), cudaMemcpyHostToDevice, s->stream));
+		}
+		SPH_CUDA(cudaStreamSynchronize(s->stream));
 		s->timed = false;
 		return SPH_OK;
 	}
@@ -704,53 +1111,63 @@ int sph_update(sph_sim *s, float dt) {
 }
 
 int sph_add_external_forces(sph_sim *s, sph_vec2 f) {
-	if (!s) return SPH_ERR_INVALID_ARGUMENT;
-	s->external = sph_vec2{f.x + s->external.x, f.y + s->external.y};
+	Scene *sc = single(s);
+	if (!sc) return not_single(s);
+	sc->external = sph_vec2{f.x + sc->external.x, f.y + sc->external.y};
+	s->sceneTableDirty = true;
 	return SPH_OK;
 }
 
 int sph_clear_external_force(sph_sim *s) {
-	if (!s) return SPH_ERR_INVALID_ARGUMENT;
-	s->external = sph_vec2{0.0f, 0.0f};
+	Scene *sc = single(s);
+	if (!sc) return not_single(s);
+	sc->external = sph_vec2{0.0f, 0.0f};
+	s->sceneTableDirty = true;
 	return SPH_OK;
 }
 
 int sph_get_particle_count(sph_sim *s, size_t *out) {
 	if (!s || !out) return SPH_ERR_INVALID_ARGUMENT;
-	*out = s->n;
+	*out = s->totalParticles();
 	return SPH_OK;
 }
 
 int sph_set_gravity(sph_sim *s, sph_vec2 g) {
-	if (!s) return SPH_ERR_INVALID_ARGUMENT;
-	s->gravity = g;
+	Scene *sc = single(s);
+	if (!sc) return not_single(s);
+	sc->gravity = g;
+	s->sceneTableDirty = true;
 	return SPH_OK;
 }
 
 int sph_get_params(sph_sim *s, sph_params *out) {
 	if (!s || !out) return SPH_ERR_INVALID_ARGUMENT;
-	*out = s->params;
+	*out = s->scenes[0].params;
 	return SPH_OK;
 }
 
 int sph_set_params(sph_sim *s, const sph_params *p) {
-	if (!s || !p) return SPH_ERR_INVALID_ARGUMENT;
-	s->params = *p;
+	if (!p) return SPH_ERR_INVALID_ARGUMENT;
+	Scene *sc = single(s);
+	if (!sc) return not_single(s);
+	sc->params = *p;
+	s->sceneTableDirty = true;
 	return SPH_OK;
 }
 
-int sph_get_stats(sph_sim *s, sph_stats *out) {
-	if (!s || !out) return SPH_ERR_INVALID_ARGUMENT;
+int sph_batch_get_stats(sph_sim *s, size_t scene, sph_stats *out) {
+	if (!s || !out || scene >= s->scenes.size()) return SPH_ERR_INVALID_ARGUMENT;
 	int rc = flush_adds(s);
 	if (rc) return rc;
 	rc = check_device_errors(s);
 	uint32_t st[4];
-	SPH_CUDA(cudaMemcpy(st, s->T.stats, sizeof(st), cudaMemcpyDeviceToHost));
+	SPH_CUDA(cudaMemcpy(st, s->T.stats + 4 * scene, sizeof(st), cudaMemcpyDeviceToHost));
 	out->min_particle_neighbor_count = st[0];
 	out->max_particle_neighbor_count = st[1];
 	out->min_cell_particle_count = st[2];
 	out->max_cell_particle_count = st[3];
 	out->time_emitters = s->emitterMs;
+	// Stage times cover the whole update (every scene of a batch).
 	float t[kEvCount] = {};
 	if (s->timed) {
 		for (int k = 1; k < kEvCount; ++k) {
@@ -767,6 +1184,8 @@ int sph_get_stats(sph_sim *s, sph_stats *out) {
 	out->time_collisions = t[kEvCollide];
 	return rc;
 }
+
+int sph_get_stats(sph_sim *s, sph_stats *out) { return sph_batch_get_stats(s, 0, out); }
 
 int sph_set_multithreading(sph_sim *s, int value) {
 	if (!s) return SPH_ERR_INVALID_ARGUMENT;
@@ -794,78 +1213,48 @@ int sph_get_worker_thread_count(sph_sim *s, size_t *out) {
 
 int sph_read_particles(sph_sim *s, size_t count, sph_vec2 *pos, sph_vec2 *prev, sph_vec2 *vel, sph_vec2 *acc,
                        sph_vec2 *dens, sph_vec2 *press) {
-	if (!s) return SPH_ERR_INVALID_ARGUMENT;
-	if (count > s->n) return SPH_ERR_INVALID_ARGUMENT;
-	int rc = flush_adds(s);
-	if (rc) return rc;
-	const int n = (int)s->n;
-	BufferSet &A = s->buf[s->cur];
-	BufferSet &Z = s->buf[1 - s->cur];  // free between updates: scratch
-	struct Item {
-		float2 *src, *scratch;
-		sph_vec2 *dst;
-	} items[] = {{A.pos, Z.pos, pos}, {A.prev, Z.prev, prev}, {A.vel, Z.vel, vel},
-	             {A.acc, Z.acc, acc}, {A.dens, Z.dens, dens}, {A.press, Z.press, press}};
-	for (const Item &it : items) {
-		if (!it.dst || count == 0) continue;
-		k_gather_by_id<<<blocks_for(n, kElemThreads), kElemThreads, 0, s->stream>>>(n, A.id, it.src, it.scratch);
-		SPH_LAUNCHED(s);
-		SPH_CUDA(cudaMemcpyAsync(it.dst, it.scratch, count * sizeof(float2), cudaMemcpyDeviceToHost, s->stream));
-	}
-	return check_device_errors(s);
+	return read_scene(s, 0, count, pos, prev, vel, acc, dens, press);
+}
+
+int sph_batch_read_particles(sph_sim *s, size_t scene, size_t count, sph_vec2 *pos, sph_vec2 *vel, sph_vec2 *dens,
+                             sph_vec2 *press) {
+	return read_scene(s, scene, count, pos, nullptr, vel, nullptr, dens, press);
 }
 
 int sph_state_info(sph_sim *s, size_t *count, size_t *canonical, int *gx, int *gy) {
-	if (!s) return SPH_ERR_INVALID_ARGUMENT;
-	int rc = flush_adds(s);
-	if (rc) return rc;
-	if (count) *count = s->n;
-	if (canonical) *canonical = s->n0;
-	if (gx) *gx = s->gx;
-	if (gy) *gy = s->gy;
-	return SPH_OK;
+	return scene_info(s, 0, count, canonical, gx, gy);
 }
 
-int sph_dump_state(sph_sim *s, const sph_state_view *v) {
-	if (!s || !v) return SPH_ERR_INVALID_ARGUMENT;
-	int rc = flush_adds(s);
-	if (rc) return rc;
-	if (v->count != s->n) return SPH_ERR_INVALID_ARGUMENT;
-	const size_t n = s->n;
-	BufferSet &A = s->buf[s->cur];
-	cudaStream_t st = s->stream;
-	auto d2h = [&](void *dst, const void *src, size_t bytes) -> int {
-		if (!dst || bytes == 0) return SPH_OK;
-		return cuda_status(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st));
-	};
-	if ((rc = d2h(v->pos, A.pos, n * 8)) || (rc = d2h(v->prev, A.prev, n * 8)) || (rc = d2h(v->vel, A.vel, n * 8)) ||
-	    (rc = d2h(v->acc, A.acc, n * 8)) || (rc = d2h(v->dens, A.dens, n * 8)) ||
-	    (rc = d2h(v->press, A.press, n * 8)) || (rc = d2h(v->id, A.id, n * 4)) ||
-	    (rc = d2h(v->cell, A.cellOf, n * 4)) || (rc = d2h(v->cell_start, s->cellStartA, s->ncell * 4)) ||
-	    (rc = d2h(v->cell_count, s->cellCountA, s->ncell * 4)))
-		return rc;
-	return check_device_errors(s);
+int sph_batch_state_info(sph_sim *s, size_t scene, size_t *count, size_t *canonical, int *gx, int *gy) {
+	return scene_info(s, scene, count, canonical, gx, gy);
 }
+
+int sph_dump_state(sph_sim *s, const sph_state_view *v) { return dump_scene(s, 0, v); }
+
+int sph_batch_dump_state(sph_sim *s, size_t scene, const sph_state_view *v) { return dump_scene(s, scene, v); }
 
 int sph_load_state(sph_sim *s, const sph_state_view *v) {
-	if (!s || !v) return SPH_ERR_INVALID_ARGUMENT;
+	if (!v) return SPH_ERR_INVALID_ARGUMENT;
+	Scene *scp = single(s);
+	if (!scp) return not_single(s);
+	Scene &sc = *scp;
 	if (!v->pos || !v->prev || !v->vel || !v->acc || !v->dens || !v->press || !v->id || !v->cell ||
 	    !v->cell_start || !v->cell_count)
 		return SPH_ERR_INVALID_ARGUMENT;
-	if (v->count > s->dom.max_particles || v->canonical_count > v->count) return SPH_ERR_INVALID_ARGUMENT;
-	if (v->grid_x != s->gx || v->grid_y != s->gy) return SPH_ERR_INVALID_ARGUMENT;
+	if (v->count > sc.cap || v->canonical_count > v->count) return SPH_ERR_INVALID_ARGUMENT;
+	if (v->grid_x != sc.gx || v->grid_y != sc.gy) return SPH_ERR_INVALID_ARGUMENT;
 	const size_t n = v->count;
 	// Validate the cell tables so that no kernel can index out of range.
 	size_t total = 0;
-	for (int c = 0; c < s->ncell; ++c) {
+	for (int c = 0; c < sc.ncell; ++c) {
 		if (v->cell_count[c] < 0 || v->cell_start[c] < 0) return SPH_ERR_INVALID_ARGUMENT;
 		if ((size_t)v->cell_start[c] + (size_t)v->cell_count[c] > v->canonical_count) return SPH_ERR_INVALID_ARGUMENT;
 		total += (size_t)v->cell_count[c];
 	}
 	if (total != v->canonical_count) return SPH_ERR_INVALID_ARGUMENT;
-	std::vector<int> app(s->ncell, 0);
+	std::vector<int> app(sc.ncell, 0);
 	for (size_t k = 0; k < n; ++k) {
-		if (v->cell[k] < 0 || v->cell[k] >= s->ncell) return SPH_ERR_INVALID_ARGUMENT;
+		if (v->cell[k] < 0 || v->cell[k] >= sc.ncell) return SPH_ERR_INVALID_ARGUMENT;
 		if (k >= v->canonical_count) app[v->cell[k]]++;
 	}
 	for (size_t k = 0; k < v->canonical_count; ++k) {
@@ -873,8 +1262,8 @@ int sph_load_state(sph_sim *s, const sph_state_view *v) {
 		if ((int)k < v->cell_start[c] || (int)k >= v->cell_start[c] + v->cell_count[c])
 			return SPH_ERR_INVALID_ARGUMENT;
 	}
-	s->pendPos.clear();
-	s->pendForce.clear();
+	sc.pendPos.clear();
+	sc.pendForce.clear();
 	BufferSet &A = s->buf[s->cur];
 	cudaStream_t st = s->stream;
 	auto h2d = [&](void *dst, const void *src, size_t bytes) -> int {
@@ -885,13 +1274,14 @@ int sph_load_state(sph_sim *s, const sph_state_view *v) {
 	if ((rc = h2d(A.pos, v->pos, n * 8)) || (rc = h2d(A.prev, v->prev, n * 8)) || (rc = h2d(A.vel, v->vel, n * 8)) ||
 	    (rc = h2d(A.acc, v->acc, n * 8)) || (rc = h2d(A.dens, v->dens, n * 8)) ||
 	    (rc = h2d(A.press, v->press, n * 8)) || (rc = h2d(A.id, v->id, n * 4)) ||
-	    (rc = h2d(A.cellOf, v->cell, n * 4)) || (rc = h2d(s->cellStartA, v->cell_start, s->ncell * 4)) ||
-	    (rc = h2d(s->cellCountA, v->cell_count, s->ncell * 4)))
+	    (rc = h2d(A.cellOf, v->cell, n * 4)) || (rc = h2d(s->cellStartA, v->cell_start, sc.ncell * 4)) ||
+	    (rc = h2d(s->cellCountA, v->cell_count, sc.ncell * 4)))
 		return rc;
-	SPH_CUDA(cudaMemcpyAsync(s->T.appCount, app.data(), s->ncell * 4, cudaMemcpyHostToDevice, st));
+	SPH_CUDA(cudaMemcpyAsync(s->T.appCount, app.data(), sc.ncell * 4, cudaMemcpyHostToDevice, st));
 	SPH_CUDA(cudaStreamSynchronize(st));  // `app` is a host temporary
-	s->n = s->nDev = n;
-	s->n0 = v->canonical_count;
+	sc.n = sc.nDev = n;
+	sc.n0 = v->canonical_count;
+	s->sceneTableDirty = true;
 	return SPH_OK;
 }
 
@@ -922,8 +1312,9 @@ int sph_synchronize(sph_sim *s) {
 
 // Diagnostics (not part of the reference interface): per-task timestamps of
 // the two ordered sweeps of the next updates.
-extern "C" int sph_profile_tasks(sph_sim *s, int enable) {
+int sph_profile_tasks(sph_sim *s, int enable) {
 	if (!s) return SPH_ERR_INVALID_ARGUMENT;
+	drop_graphs(s);  // graphs hold the timestamp buffer's address
 	if (enable && !s->prof) {
 		SPH_CUDA(cudaMalloc(&s->prof, sizeof(unsigned long long) * 8 * s->doneDCap));
 		SPH_CUDA(cudaMemset(s->prof, 0, sizeof(unsigned long long) * 8 * s->doneDCap));
@@ -934,13 +1325,21 @@ extern "C" int sph_profile_tasks(sph_sim *s, int enable) {
 	return SPH_OK;
 }
 
-extern "C" int sph_profile_read(sph_sim *s, unsigned long long *out, size_t capacity, size_t *stride) {
+int sph_profile_read(sph_sim *s, unsigned long long *out, size_t capacity, size_t *stride) {
 	if (!s || !stride) return SPH_ERR_INVALID_ARGUMENT;
 	*stride = s->doneDCap;
 	if (!s->prof || !out) return SPH_OK;
 	const size_t total = std::min(capacity, (size_t)8 * s->doneDCap);
 	SPH_CUDA(cudaStreamSynchronize(s->stream));
 	SPH_CUDA(cudaMemcpy(out, s->prof, total * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+	return SPH_OK;
+}
+
+int sph_use_graphs(sph_sim *s, int enable) {
+	if (!s) return SPH_ERR_INVALID_ARGUMENT;
+	SPH_CUDA(cudaStreamSynchronize(s->stream));
+	drop_graphs(s);
+	s->useGraphs = enable != 0;
 	return SPH_OK;
 }
 

@@ -71,6 +71,28 @@ struct StepParams {
 	int nbodies;
 };
 
+// One scene of a simulation.  A simulation holds one or more independent
+// scenes in one arena: scene s owns particle numbers pBase .. pBase+n-1
+// (canonical ones first, then the appendix) and global cells
+// cellBase .. cellBase+p.ncell-1 (its own grid, numbered y*gx+x).
+struct SceneDev {
+	StepParams p;
+	int cellBase;
+	int pBase;
+	int n, n0;
+	int bodyBase;
+	uint32_t nbSeed;  // neighbour-count statistics seed (kSPHMaxParticleNeighborCount)
+	int pad[2];
+};
+
+// Totals of one update over all scenes.
+struct Totals {
+	int n;          // particles
+	int ncell;      // cells (= canonical sweep tasks)
+	int nApp;       // appendix runs (delta-sweep tasks after the canonical ones)
+	int nscenes;
+};
+
 // Particle arrays of one buffer set, in the internal numbering.
 struct Particles {
 	float2 *pos, *prev, *vel, *acc, *dens, *press;
@@ -82,8 +104,12 @@ struct Particles {
 // (after the last update) are numbers cellStart[c] .. +cellCount[c]-1, cells
 // in colour-major rank order; numbers >= n0 are the appendix.
 struct SimTables {
-	int *cellStart, *cellCount;        // canonical ranges, by cell id
-	int *rankOfCell, *cellOfRank;
+	int *cellStart, *cellCount;        // canonical ranges, by global cell
+	int *taskOfCell, *taskCell;        // global cell <-> sweep task (scenes interleaved)
+	int *numberOrder;                  // global cells in numbering order (scene-major, colour rank)
+	int *sceneOfCell, *sceneOf;        // scene of a global cell / of a particle number
+	SceneDev *scenes;
+	int *appScene, *appRun, *appPrev;  // appendix run tasks: scene, run, previous task of the scene (-1)
 	int *appCount, *appStart, *appIdx, *appCursor;  // appendix members per cell
 	int *newCell;                      // cell after predict, per particle
 	int *enterCount, *leaveCount, *enterOffset, *enterCursor, *enterList;
@@ -94,7 +120,7 @@ struct SimTables {
 	int *newLabel;  // old number -> new number
 	uint32_t *done;                    // per sweep task
 	int *taskCounter;                  // [0] viscosity, [1] delta
-	uint32_t *stats;                   // minNb, maxNb, minCell, maxCell
+	uint32_t *stats;                   // per scene: minNb, maxNb, minCell, maxCell
 	uint32_t *error;
 	uint32_t *abort;
 	Body *bodies;

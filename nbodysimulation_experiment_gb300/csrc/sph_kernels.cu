@@ -14,17 +14,22 @@
 //                   sph.h:483-495)
 //   k_collide       body collisions + velocity + renumbering (demo4.cpp:411-450)
 //
+// Every kernel covers all scenes of the simulation at once (one launch per
+// stage): particle numbers and cells carry their scene, whose step scalars,
+// grid and bodies live in the scene table.
+//
 // The two pairwise passes of the reference are serial Gauss-Seidel sweeps in
 // particle-number order: a particle's updates land in its neighbours
 // immediately.  They are reproduced exactly by running them as dataflow
-// "sweeps": a task is a run of consecutively numbered particles processed in
-// order by one warp, tasks are claimed in increasing order, and a task first
-// waits (bounded) until every earlier task whose footprint can overlap its own
-// has finished.  Two particles' footprints overlap only when their cells are
-// at most two apart, so with particles numbered cell by cell in a
-// 3x3-colour-major cell order most tasks are independent.  All waits are
-// bounded; a timeout raises kErrTimeout and an abort flag that releases every
-// other wait, so a kernel always terminates.
+// "sweeps": a task is a run of consecutively numbered particles of one scene
+// processed in order by one thread block, tasks are claimed in increasing
+// order, and a task first waits (bounded) until every earlier task of its
+// scene whose footprint can overlap its own has finished.  Two particles'
+// footprints overlap only when their cells are at most two apart, so with
+// particles numbered cell by cell in a 3x3-colour-major cell order most tasks
+// are independent; tasks of different scenes never wait on each other.  All
+// waits are bounded; a timeout raises kErrTimeout and an abort flag that
+// releases every other wait, so a kernel always terminates.
 //
 // Arithmetic: the library is compiled with --fmad=false and IEEE division and
 // square root, and every expression below follows the reference's operation
@@ -59,6 +64,8 @@ __device__ __forceinline__ unsigned lanemask_lt() {
 	return m;
 }
 
+// Diagnostics: %globaltimer stamps per task (coarse; for task ordering, not
+// for sub-microsecond durations).
 __device__ __forceinline__ void stamp(const SimTables &T, int sweep, int task, int slot, int lane) {
 	if (T.prof != nullptr && lane == 0 && task < T.profStride)
 		T.prof[((size_t)sweep * T.profStride + task) * 4 + slot] = global_ns();
@@ -86,8 +93,9 @@ __device__ __forceinline__ void warp_wait(const uint32_t *flag, uint32_t *abortF
 	}
 }
 
+// Cell of a position within its scene's grid (SPHComputeCellPos + clamp,
+// sph.h:450-463): IEEE divide, truncation.
 __device__ __forceinline__ int cell_of(float2 p, const StepParams &s) {
-	// SPHComputeCellPos + clamp (sph.h:450-463): IEEE divide, truncation.
 	int x = (int)((p.x + s.halfW) / s.cellSize);
 	int y = (int)((p.y + s.halfH) / s.cellSize);
 	x = min(max(x, 0), s.gx - 1);
@@ -105,9 +113,10 @@ __device__ __forceinline__ int rect_dist(int ax0, int ay0, int ax1, int ay1, int
 
 // ---------------------------------------------------------------------------
 // Integrate forces (demo4.cpp:302-309) and reset the per-step cell tables.
-__global__ void k_integrate(int n, Particles P, SimTables T, StepParams s) {
+__global__ void k_integrate(Totals tt, Particles P, SimTables T) {
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i < n) {
+	if (i < tt.n) {
+		const StepParams &s = T.scenes[T.sceneOf[i]].p;
 		float2 a = P.acc[i];
 		float2 v = P.vel[i];
 		a.x = s.extX + a.x;  // acceleration += gravity + externalForce
@@ -117,12 +126,14 @@ __global__ void k_integrate(int n, Particles P, SimTables T, StepParams s) {
 		P.vel[i] = v;
 		P.acc[i] = make_float2(0.0f, 0.0f);
 	}
-	if (i < s.ncell) {
+	if (i < tt.ncell) {
+		const SceneDev &sc = T.scenes[T.sceneOfCell[i]];
+		const int local = i - sc.cellBase;
 		T.enterCount[i] = 0;
 		T.leaveCount[i] = 0;
 		T.enterCursor[i] = 0;
 		T.appCursor[i] = 0;
-		const int cx = i % s.gx, cy = i / s.gx;
+		const int cx = local % sc.p.gx, cy = local / sc.p.gx;
 		T.bbox[4 * i + 0] = cx;
 		T.bbox[4 * i + 1] = cy;
 		T.bbox[4 * i + 2] = cx;
@@ -135,14 +146,14 @@ __global__ void k_integrate(int n, Particles P, SimTables T, StepParams s) {
 }
 
 // ---------------------------------------------------------------------------
-// Viscosity sweep.  Task t = canonical cell cellOfRank[t]; its particles share
+// Viscosity sweep.  Task t = canonical cell taskCell[t]; its particles share
 // one stale neighbour list: the first (list-time) members of the 3x3 block of
 // cells around it, y-major then x, each cell in array order (demo4.cpp:
-// 188-201).  The whole block (positions and velocities) is staged in shared
-// memory, the task's particles are processed in number order, and the block's
-// velocities are written back.  Two tasks conflict iff their cells are at most
-// two apart; every task waits for the earlier conflicting ones.
-
+// 188-201).  The block's positions and velocities are staged in shared
+// memory, the task's particles are processed in number order, and the
+// block's velocities are written back.  Two tasks conflict iff they belong to
+// one scene and their cells are at most two apart; every task waits for the
+// earlier conflicting ones.
 // One task per block: warp 0 runs the ordered velocity chain of particle k
 // while warps 1..3 compute the compacted pair geometry of particle k+1
 // (positions do not change during this pass, so the geometry of every
@@ -272,29 +283,32 @@ __device__ __forceinline__ void visc_chain(ViscSmem &S, int buf, int slot, const
 
 }  // namespace
 
-__global__ void __launch_bounds__(kViscTaskWarps * kWarp, 4) k_viscosity(Particles P, SimTables T, StepParams s) {
+__global__ void __launch_bounds__(kViscTaskWarps * kWarp, 4) k_viscosity(Totals tt, Particles P, SimTables T) {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	ViscSmem &S = *reinterpret_cast<ViscSmem *>(smem_raw);
 	const int tid = threadIdx.x, warp = tid / kWarp;
-	const int gx = s.gx, gy = s.gy;
 	for (;;) {
 		if (tid == 0) S.task = atomicAdd(&T.taskCounter[0], 1);
 		__syncthreads();
 		const int t = S.task;
 		__syncthreads();
-		if (t >= s.ncell) break;
+		if (t >= tt.ncell) break;
 		stamp(T, 0, t, 0, tid);
-		const int c = T.cellOfRank[t];
+		const int c = T.taskCell[t];
 		const int cnt = T.cellCount[c];
 		if (cnt > 0) {
-			const int cx = c % gx, cy = c / gx;
-			// Wait for earlier tasks within Chebyshev distance 2 (warp 0).
+			const SceneDev &sc = T.scenes[T.sceneOfCell[c]];
+			const StepParams s = sc.p;
+			const int base = sc.cellBase, gx = s.gx, gy = s.gy;
+			const int cx = (c - base) % gx, cy = (c - base) / gx;
+			// Wait for earlier tasks of the scene within Chebyshev distance 2
+			// (warp 0).
 			if (warp == 0) {
 				const uint32_t *flag = nullptr;
 				const int x = cx + tid % 5 - 2, y = cy + tid / 5 - 2;
 				if (tid < 25 && tid != 12 && x >= 0 && x < gx && y >= 0 && y < gy) {
-					const int c2 = y * gx + x;
-					const int r2 = T.rankOfCell[c2];
+					const int c2 = base + y * gx + x;
+					const int r2 = T.taskOfCell[c2];
 					if (r2 < t && T.cellCount[c2] > 0) flag = &T.done[r2];
 				}
 				warp_wait(flag, T.abort, T.error);
@@ -309,7 +323,7 @@ __global__ void __launch_bounds__(kViscTaskWarps * kWarp, 4) k_viscosity(Particl
 				const int x = cx + q % 3 - 1, y = cy + q / 3 - 1;
 				int st = 0, nn = 0;
 				if (x >= 0 && x < gx && y >= 0 && y < gy) {
-					const int c2 = y * gx + x;
+					const int c2 = base + y * gx + x;
 					st = T.cellStart[c2];
 					nn = T.cellCount[c2];
 				}
@@ -321,11 +335,11 @@ __global__ void __launch_bounds__(kViscTaskWarps * kWarp, 4) k_viscosity(Particl
 			if (L > kStageCap) {
 				if (tid == 0) atomicOr(T.error, kErrStageOverflow);
 			} else {
-				for (int base = 0; base < L; base += 4 * kVT) {
+				for (int b0 = 0; b0 < L; b0 += 4 * kVT) {
 					float2 xp[4], vp[4];
 #pragma unroll
 					for (int u = 0; u < 4; ++u) {
-						const int e = base + u * kVT + tid;
+						const int e = b0 + u * kVT + tid;
 						if (e < L) {
 							const int src = seg_src<9>(e, segOff, segStart);
 							xp[u] = __ldcg(&P.pos[src]);
@@ -334,7 +348,7 @@ __global__ void __launch_bounds__(kViscTaskWarps * kWarp, 4) k_viscosity(Particl
 					}
 #pragma unroll
 					for (int u = 0; u < 4; ++u) {
-						const int e = base + u * kVT + tid;
+						const int e = b0 + u * kVT + tid;
 						if (e < L) {
 							S.pos[e] = xp[u];
 							S.vel[e] = vp[u];
@@ -368,22 +382,25 @@ __global__ void __launch_bounds__(kViscTaskWarps * kWarp, 4) k_viscosity(Particl
 // Predict (demo4.cpp:329-337) and the new cell (demo4.cpp:347).  Movers
 // extend the bounding box of new cells of their old cell, count as leaving
 // their old cell and entering their new cell.
-__global__ void k_predict(int n, Particles P, SimTables T, StepParams s) {
+__global__ void k_predict(Totals tt, Particles P, SimTables T) {
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i >= n) return;
+	if (i >= tt.n) return;
+	const SceneDev &sc = T.scenes[T.sceneOf[i]];
 	const float2 x = P.pos[i];
 	const float2 v = P.vel[i];
 	P.prev[i] = x;
-	const float2 xn = make_float2(v.x * s.dt + x.x, v.y * s.dt + x.y);
+	const float2 xn = make_float2(v.x * sc.p.dt + x.x, v.y * sc.p.dt + x.y);
 	P.pos[i] = xn;
-	const int nc = cell_of(xn, s);
+	const int local = cell_of(xn, sc.p);
+	const int nc = sc.cellBase + local;
 	T.newCell[i] = nc;
 	const int oc = P.cellOf[i];
 	if (nc != oc) {
 		atomicAdd(&T.enterCount[nc], 1);
 		atomicAdd(&T.leaveCount[oc], 1);
-		const int nx = nc % s.gx, ny = nc / s.gx;
-		const int ox = oc % s.gx, oy = oc / s.gx;
+		const int gx = sc.p.gx;
+		const int nx = local % gx, ny = local / gx;
+		const int ox = (oc - sc.cellBase) % gx, oy = (oc - sc.cellBase) / gx;
 		atomicMin(&T.bbox[4 * oc + 0], nx);
 		atomicMin(&T.bbox[4 * oc + 1], ny);
 		atomicMax(&T.bbox[4 * oc + 2], nx);
@@ -395,8 +412,8 @@ __global__ void k_predict(int n, Particles P, SimTables T, StepParams s) {
 
 // ---------------------------------------------------------------------------
 // Exclusive scans over cells (single block).  Each thread owns a contiguous
-// run of cells (or ranks), sums it, the block scans the run totals, and each
-// thread writes its run's prefixes.
+// run of cells (in `order` if given), sums it, the block scans the run
+// totals, and each thread writes its run's prefixes.
 __device__ void block_exscan_runs(int ncell, const int *in, const int *order, int *out) {
 	__shared__ int sums[kScanThreads];
 	const int tid = threadIdx.x;
@@ -421,28 +438,29 @@ __device__ void block_exscan_runs(int ncell, const int *in, const int *order, in
 	__syncthreads();
 }
 
-__global__ void __launch_bounds__(kScanThreads) k_scan(SimTables T, StepParams s, uint32_t nbSeed) {
-	const int ncell = s.ncell;
-	for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+__global__ void __launch_bounds__(kScanThreads) k_scan(Totals tt, SimTables T) {
+	for (int c = threadIdx.x; c < tt.ncell; c += blockDim.x) {
 		T.newCount[c] = T.cellCount[c] + T.appCount[c] - T.leaveCount[c] + T.enterCount[c];
 	}
 	__syncthreads();
-	block_exscan_runs(ncell, T.appCount, nullptr, T.appStart);
-	block_exscan_runs(ncell, T.enterCount, nullptr, T.enterOffset);
-	block_exscan_runs(ncell, T.newCount, T.cellOfRank, T.newStart);
-	if (threadIdx.x == 0) {
+	block_exscan_runs(tt.ncell, T.appCount, nullptr, T.appStart);
+	block_exscan_runs(tt.ncell, T.enterCount, nullptr, T.enterOffset);
+	// The new numbering: scenes in order, cells in colour rank order.
+	block_exscan_runs(tt.ncell, T.newCount, T.numberOrder, T.newStart);
+	for (int sc = threadIdx.x; sc < tt.nscenes; sc += blockDim.x) {
 		// Neighbour-count statistics restart every search (demo4.cpp:369-370).
-		T.stats[0] = nbSeed;
-		T.stats[1] = 0;
+		T.stats[4 * sc + 0] = T.scenes[sc].nbSeed;
+		T.stats[4 * sc + 1] = 0;
 	}
 }
 
 // Appendix members and movers into per-cell lists (order fixed later).
-__global__ void k_scatter(int n, int n0, Particles P, SimTables T) {
+__global__ void k_scatter(Totals tt, Particles P, SimTables T) {
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i >= n) return;
+	if (i >= tt.n) return;
+	const SceneDev &sc = T.scenes[T.sceneOf[i]];
 	const int oc = P.cellOf[i];
-	if (i >= n0) {
+	if (i - sc.pBase >= sc.n0) {
 		const int slot = T.appStart[oc] + atomicAdd(&T.appCursor[oc], 1);
 		T.appIdx[slot] = i;
 	}
@@ -478,19 +496,20 @@ __device__ void insertion_sort(int *a, int n) {
 	}
 }
 
-__global__ void __launch_bounds__(kGridWarps * kWarp) k_grid_update(int n, Particles P, Particles Q, SimTables T,
-                                                                      StepParams s) {
+__global__ void __launch_bounds__(kGridWarps * kWarp) k_grid_update(Totals tt, Particles P, Particles Q, SimTables T) {
 	__shared__ GridWarp W[kGridWarps];
 	GridWarp &S = W[threadIdx.x / kWarp];
 	const int lane = threadIdx.x & (kWarp - 1);
+	const int n = tt.n;
 	const int warpsTotal = gridDim.x * kGridWarps;
-	for (int c = blockIdx.x * kGridWarps + threadIdx.x / kWarp; c < s.ncell; c += warpsTotal) {
+	for (int c = blockIdx.x * kGridWarps + threadIdx.x / kWarp; c < tt.ncell; c += warpsTotal) {
 		const int cs = T.cellStart[c], cc = T.cellCount[c];
 		const int as = T.appStart[c], ac = T.appCount[c];
 		const int eo = T.enterOffset[c], ec = T.enterCount[c];
 		const int init = cc + ac;
 		const int outStart = T.newStart[c], outCount = T.newCount[c];
 		if (init == 0 && ec == 0) continue;
+		uint32_t *stats = T.stats + 4 * T.sceneOfCell[c];
 		if (init + ec > kCellCap || outCount > kCellCap) {
 			// Over capacity: keep memory consistent (members in some order)
 			// and report; the result of this update is not meaningful.
@@ -560,8 +579,8 @@ __global__ void __launch_bounds__(kGridWarps * kWarp) k_grid_update(int n, Parti
 				hi = max(hi, cnt);
 			}
 			if (nl + ec > 0) {
-				atomicMin(&T.stats[2], (uint32_t)lo);
-				atomicMax(&T.stats[3], (uint32_t)hi);
+				atomicMin(&stats[2], (uint32_t)lo);
+				atomicMax(&stats[3], (uint32_t)hi);
 			}
 			if (cnt != outCount) atomicOr(T.error, kErrIndex);
 		}
@@ -592,15 +611,19 @@ struct DensWarp {
 	float2 pos[kStageCap];
 };
 
-__global__ void __launch_bounds__(kDensWarps * kWarp) k_density(int n, Particles Q, SimTables T, StepParams s) {
+__global__ void __launch_bounds__(kDensWarps * kWarp) k_density(Totals tt, Particles Q, SimTables T) {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	DensWarp &S = reinterpret_cast<DensWarp *>(smem_raw)[threadIdx.x / kWarp];
 	const int lane = threadIdx.x & (kWarp - 1);
 	const int warpsTotal = gridDim.x * kDensWarps;
-	for (int c = blockIdx.x * kDensWarps + threadIdx.x / kWarp; c < s.ncell; c += warpsTotal) {
+	for (int c = blockIdx.x * kDensWarps + threadIdx.x / kWarp; c < tt.ncell; c += warpsTotal) {
 		const int cnt = T.newCount[c];
 		if (cnt == 0) continue;
-		const int cx = c % s.gx, cy = c / s.gx;
+		const int sid = T.sceneOfCell[c];
+		const SceneDev &sc = T.scenes[sid];
+		const StepParams &s = sc.p;
+		const int base = sc.cellBase;
+		const int cx = (c - base) % s.gx, cy = (c - base) / s.gx;
 		int segStart[9], segOff[9];
 		int L = 0, own = 0;
 #pragma unroll
@@ -608,7 +631,7 @@ __global__ void __launch_bounds__(kDensWarps * kWarp) k_density(int n, Particles
 			const int x = cx + q % 3 - 1, y = cy + q / 3 - 1;
 			int st = 0, nn = 0;
 			if (x >= 0 && x < s.gx && y >= 0 && y < s.gy) {
-				const int c2 = y * s.gx + x;
+				const int c2 = base + y * s.gx + x;
 				st = T.newStart[c2];
 				nn = T.newCount[c2];
 			}
@@ -618,25 +641,23 @@ __global__ void __launch_bounds__(kDensWarps * kWarp) k_density(int n, Particles
 			L += nn;
 		}
 		if (lane == 0) {
-			atomicMin(&T.stats[0], (uint32_t)L);
-			atomicMax(&T.stats[1], (uint32_t)L);
+			atomicMin(&T.stats[4 * sid + 0], (uint32_t)L);
+			atomicMax(&T.stats[4 * sid + 1], (uint32_t)L);
 		}
 		if (L > kStageCap) {
 			if (lane == 0) atomicOr(T.error, kErrStageOverflow);
 			continue;
 		}
-		for (int base = 0; base < L; base += 4 * kWarp) {
+		for (int b0 = 0; b0 < L; b0 += 4 * kWarp) {
 			float2 xp[4];
 #pragma unroll
 			for (int u = 0; u < 4; ++u) {
-				const int e = base + u * kWarp + lane;
-				if (e < L) {
-					xp[u] = Q.pos[seg_src<9>(e, segOff, segStart)];
-				}
+				const int e = b0 + u * kWarp + lane;
+				if (e < L) xp[u] = Q.pos[seg_src<9>(e, segOff, segStart)];
 			}
 #pragma unroll
 			for (int u = 0; u < 4; ++u) {
-				const int e = base + u * kWarp + lane;
+				const int e = b0 + u * kWarp + lane;
 				if (e < L) S.pos[e] = xp[u];
 			}
 		}
@@ -668,13 +689,12 @@ __global__ void __launch_bounds__(kDensWarps * kWarp) k_density(int n, Particles
 
 // ---------------------------------------------------------------------------
 // Delta sweep (double-density relaxation, demo4.cpp:239-255).  Tasks in
-// number order: canonical cells in rank order, then the appendix in runs of
-// kAppendixRun consecutive numbers.  A particle's list is the 3x3 block of
-// NEW cells around its new cell.  A task stages the new cells of its
-// bounding box grown by one, processes its particles in order, and writes
-// back only cells inside its particles' 3x3 blocks.  Earlier tasks whose
-// bounding boxes come within two cells are waited for.
-
+// number order per scene: canonical cells in rank order, then the scene's
+// appendix in runs of kAppendixRun consecutive numbers.  A particle's list is
+// the 3x3 block of NEW cells around its new cell.  A task stages the new
+// cells of its bounding box grown by one, processes its particles in order,
+// and writes back only cells inside its particles' 3x3 blocks.  Earlier tasks
+// of the scene whose bounding boxes come within two cells are waited for.
 // One task per block of kDeltaTaskWarps warps: the whole block stages the
 // task's region, and for each particle scans the list, compacts the in-range
 // pairs and evaluates them in parallel; one thread then adds the halves to
@@ -705,18 +725,18 @@ struct Region {
 // new-number order, where each cell is a contiguous range.  Collective over
 // the block; returns false (uniformly) if the region does not fit.
 __device__ __forceinline__ bool stage_region(DeltaSmem &S, Region &R, const Particles &Q, const SimTables &T,
-                                             const StepParams &s, int tid) {
+                                             const StepParams &s, int cellBase, int tid) {
 	R.w = R.x1 - R.x0 + 1;
 	R.ncells = R.w * (R.y1 - R.y0 + 1);
 	if (R.ncells > kRegionCells) return false;
 	if (tid < kWarp) {
 		const int lane = tid;
 		int carry = 0;
-		for (int base = 0; base < R.ncells; base += kWarp) {
-			const int q = base + lane;
+		for (int b0 = 0; b0 < R.ncells; b0 += kWarp) {
+			const int q = b0 + lane;
 			int nn = 0, st = 0;
 			if (q < R.ncells) {
-				const int c2 = (R.y0 + q / R.w) * s.gx + (R.x0 + q % R.w);
+				const int c2 = cellBase + (R.y0 + q / R.w) * s.gx + (R.x0 + q % R.w);
 				nn = T.newCount[c2];
 				st = T.newStart[c2];
 			}
@@ -738,11 +758,11 @@ __device__ __forceinline__ bool stage_region(DeltaSmem &S, Region &R, const Part
 	__syncthreads();
 	R.L = S.segOff[R.ncells];
 	if (R.L > kDeltaStageCap) return false;
-	for (int base = 0; base < R.L; base += 4 * kDT) {
+	for (int b0 = 0; b0 < R.L; b0 += 4 * kDT) {
 		float2 xp[4];
 #pragma unroll
 		for (int u = 0; u < 4; ++u) {
-			const int e = base + u * kDT + tid;
+			const int e = b0 + u * kDT + tid;
 			if (e < R.L) {
 				int lo = 0, hi = R.ncells;
 				while (hi - lo > 1) {
@@ -754,7 +774,7 @@ __device__ __forceinline__ bool stage_region(DeltaSmem &S, Region &R, const Part
 		}
 #pragma unroll
 		for (int u = 0; u < 4; ++u) {
-			const int e = base + u * kDT + tid;
+			const int e = b0 + u * kDT + tid;
 			if (e < R.L) S.pos[e] = xp[u];
 		}
 	}
@@ -776,9 +796,9 @@ __device__ __forceinline__ void write_back_owned(DeltaSmem &S, const Region &R, 
 // consecutive, so the particle's list (y-major, then x, then cell order) is
 // three contiguous ranges of staged slots.  Collective over the block.
 __device__ __forceinline__ void relax_particle(DeltaSmem &S, const Region &R, int nc, int jk, float2 pk,
-                                               const SimTables &T, const StepParams &s, int tid) {
+                                               const SimTables &T, const StepParams &s, int cellBase, int tid) {
 	const int lane = tid & (kWarp - 1), warp = tid / kWarp;
-	const int x = nc % s.gx, y = nc / s.gx;
+	const int x = (nc - cellBase) % s.gx, y = (nc - cellBase) / s.gx;
 	const int xa = max(x - 1, 0), xb = min(x + 1, s.gx - 1);
 	int off0 = 0, off1 = 0, off2 = 0, len0 = 0, len1 = 0, len2 = 0;
 #pragma unroll
@@ -809,14 +829,14 @@ __device__ __forceinline__ void relax_particle(DeltaSmem &S, const Region &R, in
 	const int l01 = len0 + len1;
 	float2 dx = make_float2(0.0f, 0.0f);  // thread 0
 	int m = 0, parity = 0;
-	for (int base = 0; base < L; base += 2 * kDT) {
+	for (int b0 = 0; b0 < L; b0 += 2 * kDT) {
 		bool in[2];
 		int slot[2];
 		float2 xj[2];
 		float r2[2];
 #pragma unroll
 		for (int u = 0; u < 2; ++u) {
-			const int e = base + warp * 2 * kWarp + u * kWarp + lane;
+			const int e = b0 + warp * 2 * kWarp + u * kWarp + lane;
 			in[u] = false;
 			slot[u] = 0;
 			xj[u] = make_float2(0.f, 0.f);
@@ -847,7 +867,7 @@ __device__ __forceinline__ void relax_particle(DeltaSmem &S, const Region &R, in
 			    make_float4(__int_as_float(slot[1]), xj[1].x, xj[1].y, r2[1]);
 		m += total;
 		parity ^= 1;
-		if (m > kDeltaChainCap - 2 * kDT || base + 2 * kDT >= L) {
+		if (m > kDeltaChainCap - 2 * kDT || b0 + 2 * kDT >= L) {
 			__syncthreads();
 			for (int q = tid; q < m; q += kDT) {
 				const float4 cd = S.cand[q];
@@ -897,15 +917,14 @@ __device__ __forceinline__ void relax_particle(DeltaSmem &S, const Region &R, in
 // it fits, otherwise one 3x3 region per particle.  Per-particle inputs (new
 // cell, new number, pressure) are prefetched in chunks, off the serial path.
 __device__ __forceinline__ void relax_group(DeltaSmem &S, int p0, int p1, int bx0, int by0, int bx1, int by1,
-                                            const Particles &Q, const SimTables &T, const StepParams &s, int tid,
-                                            int task) {
+                                            const Particles &Q, const SimTables &T, const StepParams &s,
+                                            int cellBase, int tid) {
 	Region R;
 	R.x0 = max(bx0 - 1, 0);
 	R.y0 = max(by0 - 1, 0);
 	R.x1 = min(bx1 + 1, s.gx - 1);
 	R.y1 = min(by1 + 1, s.gy - 1);
-	const bool staged = stage_region(S, R, Q, T, s, tid);
-	stamp(T, 1, task, 2, staged ? tid : 1);
+	const bool staged = stage_region(S, R, Q, T, s, cellBase, tid);
 	for (int c0 = p0; c0 < p1; c0 += kPrefetch) {
 		const int c1 = min(p1, c0 + kPrefetch);
 		for (int k = c0 + tid; k < c1; k += kDT) {
@@ -919,21 +938,21 @@ __device__ __forceinline__ void relax_group(DeltaSmem &S, int p0, int p1, int bx
 			const int nc = S.pnc[k - c0], jk = S.pjk[k - c0];
 			const float2 pk = S.ppk[k - c0];
 			if (staged) {
-				relax_particle(S, R, nc, jk, pk, T, s, tid);
+				relax_particle(S, R, nc, jk, pk, T, s, cellBase, tid);
 				continue;
 			}
 			Region R1;
-			const int x = nc % s.gx, y = nc / s.gx;
+			const int x = (nc - cellBase) % s.gx, y = (nc - cellBase) / s.gx;
 			R1.x0 = max(x - 1, 0);
 			R1.y0 = max(y - 1, 0);
 			R1.x1 = min(x + 1, s.gx - 1);
 			R1.y1 = min(y + 1, s.gy - 1);
-			if (!stage_region(S, R1, Q, T, s, tid)) {
+			if (!stage_region(S, R1, Q, T, s, cellBase, tid)) {
 				if (tid == 0) atomicOr(T.error, kErrStageOverflow);
 				__syncthreads();
 				continue;
 			}
-			relax_particle(S, R1, nc, jk, pk, T, s, tid);
+			relax_particle(S, R1, nc, jk, pk, T, s, cellBase, tid);
 			write_back_owned(S, R1, Q, tid);
 			__syncthreads();
 		}
@@ -942,11 +961,13 @@ __device__ __forceinline__ void relax_group(DeltaSmem &S, int p0, int p1, int bx
 	if (staged) write_back_owned(S, R, Q, tid);
 }
 
-// Wait for canonical tasks (old cells) near [bx0,bx1]x[by0,by1] whose
-// new-cell bounding boxes come within two cells of it and whose rank is
-// below `limitRank`.  Collective over the block.
-__device__ __forceinline__ void wait_canonical(int bx0, int by0, int bx1, int by1, int moveMax, int limitRank,
-                                               int selfCell, const SimTables &T, const StepParams &s, int tid) {
+// Wait for canonical tasks of the scene (old cells) near [bx0,bx1]x[by0,by1]
+// whose new-cell bounding boxes come within two cells of it and whose task
+// index is below `limit`.  Collective over the block; waits are converged
+// per warp.
+__device__ __forceinline__ void wait_canonical(int bx0, int by0, int bx1, int by1, int moveMax, int limit,
+                                               int selfCell, const SimTables &T, const StepParams &s,
+                                               int cellBase, int tid) {
 	const int rad = 2 + moveMax;
 	const int x0 = max(bx0 - rad, 0), x1 = min(bx1 + rad, s.gx - 1);
 	const int y0 = max(by0 - rad, 0), y1 = min(by1 + rad, s.gy - 1);
@@ -956,9 +977,9 @@ __device__ __forceinline__ void wait_canonical(int bx0, int by0, int bx1, int by
 		const int q = q0 + tid;
 		const uint32_t *flag = nullptr;
 		if (q < total) {
-			const int c2 = (y0 + q / w) * s.gx + (x0 + q % w);
-			const int r2 = T.rankOfCell[c2];
-			if (c2 != selfCell && r2 < limitRank && T.cellCount[c2] > 0) {
+			const int c2 = cellBase + (y0 + q / w) * s.gx + (x0 + q % w);
+			const int r2 = T.taskOfCell[c2];
+			if (c2 != selfCell && r2 < limit && T.cellCount[c2] > 0) {
 				const int4 b = *reinterpret_cast<const int4 *>(&T.bbox[4 * c2]);
 				if (rect_dist(b.x, b.y, b.z, b.w, bx0, by0, bx1, by1) <= 2) flag = &T.done[r2];
 			}
@@ -970,13 +991,11 @@ __device__ __forceinline__ void wait_canonical(int bx0, int by0, int bx1, int by
 
 }  // namespace
 
-__global__ void __launch_bounds__(kDeltaTaskWarps * kWarp, 4) k_delta(int n, int n0, Particles Q, SimTables T,
-                                                                       StepParams s) {
+__global__ void __launch_bounds__(kDeltaTaskWarps * kWarp, 4) k_delta(Totals tt, Particles Q, SimTables T) {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	DeltaSmem &S = *reinterpret_cast<DeltaSmem *>(smem_raw);
 	const int tid = threadIdx.x;
-	const int runs = (n - n0 + kAppendixRun - 1) / kAppendixRun;
-	const int ntask = s.ncell + runs;
+	const int ntask = tt.ncell + tt.nApp;
 	const int moveMax = T.moverCount[1];
 	for (;;) {
 		if (tid == 0) S.task = atomicAdd(&T.taskCounter[1], 1);
@@ -985,28 +1004,36 @@ __global__ void __launch_bounds__(kDeltaTaskWarps * kWarp, 4) k_delta(int n, int
 		__syncthreads();
 		if (t >= ntask) break;
 		stamp(T, 1, t, 0, tid);
-		if (t < s.ncell) {
-			const int c = T.cellOfRank[t];
+		if (t < tt.ncell) {
+			const int c = T.taskCell[t];
 			const int p0 = T.cellStart[c], cnt = T.cellCount[c];
 			if (cnt > 0) {
+				const SceneDev &sc = T.scenes[T.sceneOfCell[c]];
+				const StepParams s = sc.p;
 				const int4 b = *reinterpret_cast<const int4 *>(&T.bbox[4 * c]);
-				wait_canonical(b.x, b.y, b.z, b.w, moveMax, t, c, T, s, tid);
+				wait_canonical(b.x, b.y, b.z, b.w, moveMax, t, c, T, s, sc.cellBase, tid);
 				stamp(T, 1, t, 1, tid);
-				relax_group(S, p0, p0 + cnt, b.x, b.y, b.z, b.w, Q, T, s, tid, t);
+				relax_group(S, p0, p0 + cnt, b.x, b.y, b.z, b.w, Q, T, s, sc.cellBase, tid);
 				__syncthreads();
 				__threadfence();
 			}
 		} else {
-			const int run = t - s.ncell;
-			const int p0 = n0 + run * kAppendixRun;
-			const int p1 = min(n, p0 + kAppendixRun);
+			// Appendix run: particles added since the last update, swept run
+			// after run within their scene, after all canonical tasks.
+			const int a = t - tt.ncell;
+			const SceneDev &sc = T.scenes[T.appScene[a]];
+			const StepParams s = sc.p;
+			const int base = sc.cellBase;
+			const int p0 = sc.pBase + sc.n0 + T.appRun[a] * kAppendixRun;
+			const int p1 = min(sc.pBase + sc.n, p0 + kAppendixRun);
+			const int prev = T.appPrev[a];
 			int bx0 = s.gx, by0 = s.gy, bx1 = -1, by1 = -1;
 			for (int k = p0 + tid; k < p1; k += kDT) {
-				const int nc = T.newCell[k];
-				bx0 = min(bx0, nc % s.gx);
-				bx1 = max(bx1, nc % s.gx);
-				by0 = min(by0, nc / s.gx);
-				by1 = max(by1, nc / s.gx);
+				const int lc = T.newCell[k] - base;
+				bx0 = min(bx0, lc % s.gx);
+				bx1 = max(bx1, lc % s.gx);
+				by0 = min(by0, lc / s.gx);
+				by1 = max(by1, lc / s.gx);
 			}
 			// Block-wide min/max of the run's new cells (kAppendixRun <= 32:
 			// only warp 0 holds values).
@@ -1030,12 +1057,10 @@ __global__ void __launch_bounds__(kDeltaTaskWarps * kWarp, 4) k_delta(int n, int
 			bx1 = S.warpCnt[1][0];
 			by1 = S.warpCnt[1][1];
 			__syncthreads();
-			// All canonical tasks precede the appendix; the appendix itself
-			// is swept run after run.
-			wait_canonical(bx0, by0, bx1, by1, moveMax, s.ncell, -1, T, s, tid);
-			if (tid < kWarp) warp_wait(tid == 0 && run > 0 ? &T.done[t - 1] : nullptr, T.abort, T.error);
+			wait_canonical(bx0, by0, bx1, by1, moveMax, tt.ncell, -1, T, s, base, tid);
+			if (tid < kWarp) warp_wait(tid == 0 && prev >= 0 ? &T.done[prev] : nullptr, T.abort, T.error);
 			__syncthreads();
-			relax_group(S, p0, p1, bx0, by0, bx1, by1, Q, T, s, tid, t);
+			relax_group(S, p0, p1, bx0, by0, bx1, by1, Q, T, s, base, tid);
 			__syncthreads();
 			__threadfence();
 		}
@@ -1045,7 +1070,6 @@ __global__ void __launch_bounds__(kDeltaTaskWarps * kWarp, 4) k_delta(int n, int
 	}
 }
 
-// ---------------------------------------------------------------------------
 // Collisions (demo4.cpp:411-444, sph.h:514-681), velocity (demo4.cpp:446-450)
 // and the renumbering into canonical order: the particle at position j of
 // new cell c gets number newStart[c] + j.
@@ -1180,18 +1204,17 @@ __device__ void solve_polygon(float2 &p, const Body &b, const StepParams &s) {
 
 }  // namespace
 
-__global__ void __launch_bounds__(kCollideThreads) k_collide(int n, Particles P, Particles Q, SimTables T, StepParams s) {
-	__shared__ Body bodies[kMaxBodies];
-	for (int b = threadIdx.x; b < s.nbodies; b += blockDim.x) bodies[b] = T.bodies[b];
-	__syncthreads();
+__global__ void __launch_bounds__(kCollideThreads) k_collide(Totals tt, Particles P, Particles Q, SimTables T) {
 	// j: new number.  Positions, densities and pressures are already in new
 	// order; the rest is gathered from the old number.
 	const int j = blockIdx.x * blockDim.x + threadIdx.x;
-	if (j < s.ncell) T.appCount[j] = 0;
-	if (j >= n) return;
+	if (j < tt.ncell) T.appCount[j] = 0;
+	if (j >= tt.n) return;
+	const SceneDev &sc = T.scenes[T.sceneOf[j]];
+	const StepParams &s = sc.p;
 	float2 x = Q.pos[j];
 	for (int b = 0; b < s.nbodies; ++b) {
-		const Body &bd = bodies[b];
+		const Body &bd = T.bodies[sc.bodyBase + b];
 		switch (bd.type) {
 			case kBodyPlane: solve_plane(x, bd, s); break;
 			case kBodyCircle: solve_circle(x, bd, s); break;
@@ -1201,7 +1224,7 @@ __global__ void __launch_bounds__(kCollideThreads) k_collide(int n, Particles P,
 		}
 	}
 	int o = T.newIdx[j];
-	if (o < 0 || o >= n) {
+	if (o < 0 || o >= tt.n) {
 		atomicOr(T.error, kErrIndex);
 		o = 0;
 	}
@@ -1215,12 +1238,13 @@ __global__ void __launch_bounds__(kCollideThreads) k_collide(int n, Particles P,
 }
 
 // ---------------------------------------------------------------------------
-// AddParticle (demo4.cpp:142-153) for a batch of numbers [first, first+count):
-// the new particles join the appendix of their cell.
-__global__ void k_add(int first, int count, const float2 *pos, const float2 *force, Particles P, SimTables T,
-                      StepParams s) {
+// AddParticle (demo4.cpp:142-153) for a batch of numbers [first, first+count)
+// of scene `scene`: the new particles join the appendix of their cell.
+__global__ void k_add(int first, int count, int scene, int firstId, const float2 *pos, const float2 *force,
+                      Particles P, SimTables T) {
 	const int j = blockIdx.x * blockDim.x + threadIdx.x;
 	if (j >= count) return;
+	const SceneDev &sc = T.scenes[scene];
 	const int i = first + j;
 	const float2 x = pos[j];
 	P.pos[i] = x;
@@ -1229,21 +1253,22 @@ __global__ void k_add(int first, int count, const float2 *pos, const float2 *for
 	P.acc[i] = force[j];
 	P.dens[i] = make_float2(0.f, 0.f);
 	P.press[i] = make_float2(0.f, 0.f);
-	P.id[i] = i;
-	const int c = cell_of(x, s);
+	P.id[i] = firstId + j;
+	T.sceneOf[i] = scene;
+	const int c = sc.cellBase + cell_of(x, sc.p);
 	P.cellOf[i] = c;
 	const int before = atomicAdd(&T.appCount[c], 1);
 	const uint32_t now = (uint32_t)(T.cellCount[c] + before + 1);
-	atomicMin(&T.stats[2], now);
-	atomicMax(&T.stats[3], now);
+	atomicMin(&T.stats[4 * scene + 2], now);
+	atomicMax(&T.stats[4 * scene + 3], now);
 }
 
-// Scatter internal numbering -> AddParticle order for host reads.
-__global__ void k_gather_by_id(int n, const int *id, const float2 *src, float2 *dst) {
-	const int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i >= n) return;
-	const int k = id[i];
-	if (k >= 0 && k < n) dst[k] = src[i];
+// Scatter numbers [first, first+count) into AddParticle order for host reads.
+__global__ void k_gather_by_id(int first, int count, const int *id, const float2 *src, float2 *dst) {
+	const int j = blockIdx.x * blockDim.x + threadIdx.x;
+	if (j >= count) return;
+	const int k = id[first + j];
+	if (k >= 0 && k < count) dst[k] = src[first + j];
 }
 
 size_t visc_smem_bytes() { return sizeof(ViscSmem); }

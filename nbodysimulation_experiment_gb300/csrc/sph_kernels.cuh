@@ -21,17 +21,17 @@ size_t visc_smem_bytes();
 size_t delta_smem_bytes();
 size_t dens_smem_bytes();
 
-__global__ void k_integrate(int n, Particles P, SimTables T, StepParams s);
-__global__ void k_viscosity(Particles P, SimTables T, StepParams s);
-__global__ void k_predict(int n, Particles P, SimTables T, StepParams s);
-__global__ void k_scan(SimTables T, StepParams s, uint32_t nbSeed);
-__global__ void k_scatter(int n, int n0, Particles P, SimTables T);
-__global__ void k_grid_update(int n, Particles P, Particles Q, SimTables T, StepParams s);
-__global__ void k_density(int n, Particles Q, SimTables T, StepParams s);
-__global__ void k_delta(int n, int n0, Particles Q, SimTables T, StepParams s);
-__global__ void k_collide(int n, Particles P, Particles Q, SimTables T, StepParams s);
-__global__ void k_add(int first, int count, const float2 *pos, const float2 *force, Particles P, SimTables T,
-                      StepParams s);
-__global__ void k_gather_by_id(int n, const int *id, const float2 *src, float2 *dst);
+__global__ void k_integrate(Totals tt, Particles P, SimTables T);
+__global__ void k_viscosity(Totals tt, Particles P, SimTables T);
+__global__ void k_predict(Totals tt, Particles P, SimTables T);
+__global__ void k_scan(Totals tt, SimTables T);
+__global__ void k_scatter(Totals tt, Particles P, SimTables T);
+__global__ void k_grid_update(Totals tt, Particles P, Particles Q, SimTables T);
+__global__ void k_density(Totals tt, Particles Q, SimTables T);
+__global__ void k_delta(Totals tt, Particles Q, SimTables T);
+__global__ void k_collide(Totals tt, Particles P, Particles Q, SimTables T);
+__global__ void k_add(int first, int count, int scene, int firstId, const float2 *pos, const float2 *force,
+                      Particles P, SimTables T);
+__global__ void k_gather_by_id(int first, int count, const int *id, const float2 *src, float2 *dst);
 
 }  // namespace sphgb

@@ -16,6 +16,8 @@ Scenes:
   four walls, 8 seeded circles with radii in [2h, 6h] and 4 seeded line
   segments, all outside the block.
 * ``block_1m``         -- 1024x1024 jittered block in a 204.8 x 115.2 box.
+* ``batch_scenes``     -- 512 independent boxes with log-uniform particle
+  counts in [1,024, 65,536], each a jittered block plus 0-4 circles.
 """
 from __future__ import annotations
 
@@ -135,11 +137,17 @@ def dam_break_4096(seed: int = 1234) -> Scene:
 
 
 def _block_scene(name: str, side: int, width: float, height: float, n_circles: int, n_segments: int,
-                 seed: int) -> Scene:
+                 seed: int, count: Optional[int] = None) -> Scene:
+    """A side x side jittered block at the lower left of the box (the first
+    ``count`` lattice points when given: rows of ``side``), walls, seeded
+    circles and segments clear of the block."""
     hw, hh = width * 0.5, height * 0.5
     x0, y0 = -hw + 0.1, -hh + 0.1
-    pos = jittered_lattice(side, side, x0, y0, seed=seed)
-    extent = float(side) * float(SPACING)
+    rows = side if count is None else -(-count // side)
+    pos = jittered_lattice(side, rows, x0, y0, seed=seed)
+    if count is not None:
+        pos = np.ascontiguousarray(pos[:count])
+    extent = float(max(side, rows)) * float(SPACING)
     rng = np.random.default_rng(seed + 1)
     block = (x0 - 0.2, y0 - 0.2, x0 + extent + 0.2, y0 + extent + 0.2)
 
@@ -189,6 +197,27 @@ def scaled_block(side: int, seed: int = 1234, obstacles: bool = True) -> Scene:
     height = width * 9.0 / 16.0
     return _block_scene("block_%d" % (side * side), side, width, height, 8 if obstacles else 0,
                         4 if obstacles else 0, seed)
+
+
+def block_n(count: int, seed: int = 1234, n_circles: int = 0, n_segments: int = 0) -> Scene:
+    """``count`` particles as a near-square jittered block (rows of
+    ceil(sqrt(count))) in a 16:9 box four block-widths wide (at least 16)."""
+    side = int(np.ceil(np.sqrt(count)))
+    extent = side * float(SPACING)
+    width = max(16.0, 4.0 * extent)
+    height = width * 9.0 / 16.0
+    return _block_scene("block_n%d" % count, side, width, height, n_circles, n_segments, seed, count=count)
+
+
+def batch_scenes(count: int = 512, seed: int = 4242, n_min: int = 1024, n_max: int = 65536) -> List[Scene]:
+    """Independent box scenes for the batched step: particle counts
+    log-uniform in [n_min, n_max], each a jittered block plus 0-4 seeded
+    circles (no segments), all seeded from ``seed``."""
+    rng = np.random.default_rng(seed)
+    ns = np.exp(rng.uniform(np.log(n_min), np.log(n_max), count))
+    ns = np.clip(np.rint(ns).astype(np.int64), n_min, n_max)
+    circles = rng.integers(0, 5, count)
+    return [block_n(int(n), seed=seed * 1000 + k, n_circles=int(c)) for k, (n, c) in enumerate(zip(ns, circles))]
 
 
 SCENES = {

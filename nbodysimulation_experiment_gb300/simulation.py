@@ -87,10 +87,32 @@ class StateView(ctypes.Structure):
     ]
 
 
+class BodyDesc(ctypes.Structure):
+    """``sph_body_desc``: one collision body of a batched scene."""
+
+    _fields_ = [("type", _c.c_int), ("vertex_count", _c.c_size_t), ("a", Vec2), ("b", Vec2),
+                ("value", _c.c_float), ("verts", Vec2 * 8)]
+
+
+class SceneDesc(ctypes.Structure):
+    """``sph_scene_desc``: one scene of a batch (domain, parameters, gravity,
+    particles in AddParticle order, bodies)."""
+
+    _fields_ = [("domain", Domain), ("params", Params), ("gravity", Vec2), ("particle_count", _c.c_size_t),
+                ("positions", _c.c_void_p), ("forces", _c.c_void_p), ("body_count", _c.c_size_t),
+                ("bodies", _c.c_void_p)]
+
+
+SPH_BODY_PLANE, SPH_BODY_CIRCLE, SPH_BODY_SEGMENT, SPH_BODY_POLYGON = 1, 2, 3, 4
+
+
 class SphError(RuntimeError):
     def __init__(self, status: int, what: str):
         self.status = status
-        super().__init__("%s failed: %s (status %d)" % (what, _status_string(status), status))
+        detail = ""
+        if status == SPH_ERR_CUDA and _LIB is not None:
+            detail = ": " + _LIB.sph_last_error().decode(errors="replace")
+        super().__init__("%s failed: %s (status %d)%s" % (what, _status_string(status), status, detail))
 
 
 _LIB = None
@@ -156,6 +178,13 @@ def load_library(build_if_missing: bool = True):
         "sph_device_arrays": [vp, P(vp), P(vp), P(vp), P(vp)],
         "sph_synchronize": [vp],
         "sph_kernel_launches": [vp, P(_c.c_uint64)],
+        "sph_use_graphs": [vp, _c.c_int],
+        "sph_batch_create": [vp, _c.c_size_t, _c.c_int, P(vp)],
+        "sph_batch_scene_count": [vp, P(_c.c_size_t)],
+        "sph_batch_read_particles": [vp, _c.c_size_t, _c.c_size_t, vp, vp, vp, vp],
+        "sph_batch_get_stats": [vp, _c.c_size_t, P(Stats)],
+        "sph_batch_state_info": [vp, _c.c_size_t, P(_c.c_size_t), P(_c.c_size_t), P(_c.c_int), P(_c.c_int)],
+        "sph_batch_dump_state": [vp, _c.c_size_t, P(StateView)],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -163,13 +192,16 @@ def load_library(build_if_missing: bool = True):
         fn.restype = _c.c_int
     lib.sph_status_string.argtypes = [_c.c_int]
     lib.sph_status_string.restype = _c.c_char_p
+    lib.sph_last_error.argtypes = []
+    lib.sph_last_error.restype = _c.c_char_p
     _LIB = lib
     return lib
 
 
 #: Exported C symbols, in the order include/sph_gb300.h declares them.
 C_SYMBOLS = (
-    "sph_reference_domain", "sph_default_params", "sph_status_string", "sph_create", "sph_destroy",
+    "sph_reference_domain", "sph_default_params", "sph_status_string", "sph_last_error", "sph_create",
+    "sph_destroy",
     "sph_reset_stats", "sph_clear_bodies", "sph_clear_particles", "sph_clear_emitters", "sph_add_plane",
     "sph_add_circle", "sph_add_line_segment", "sph_add_polygon", "sph_add_particle", "sph_add_particles",
     "sph_add_volume", "sph_add_emitter", "sph_update", "sph_add_external_forces", "sph_clear_external_force",
@@ -177,6 +209,8 @@ C_SYMBOLS = (
     "sph_set_multithreading", "sph_is_multithreading_supported", "sph_is_multithreading",
     "sph_get_worker_thread_count", "sph_read_particles", "sph_state_info", "sph_dump_state", "sph_load_state",
     "sph_get_stream", "sph_device_arrays", "sph_synchronize", "sph_kernel_launches",
+    "sph_use_graphs", "sph_batch_create", "sph_batch_scene_count", "sph_batch_read_particles", "sph_batch_get_stats",
+    "sph_batch_state_info", "sph_batch_dump_state",
 )
 
 
@@ -203,6 +237,21 @@ def _v(x, y) -> Vec2:
 
 def _f2(a: np.ndarray) -> np.ndarray:
     return np.ascontiguousarray(a, dtype=np.float32).reshape(-1, 2)
+
+
+def _state_arrays(n: int, n0: int, gx: int, gy: int):
+    """Host arrays for one dump and the ``StateView`` pointing at them."""
+    st = {k: np.zeros((n, 2), np.float32) for k in ("pos", "prev", "vel", "acc", "dens", "press")}
+    st["id"] = np.zeros(n, np.int32)
+    st["cell"] = np.zeros(n, np.int32)
+    st["cell_start"] = np.zeros(gx * gy, np.int32)
+    st["cell_count"] = np.zeros(gx * gy, np.int32)
+    v = StateView(count=n, canonical_count=n0, grid_x=gx, grid_y=gy)
+    for k in ("pos", "prev", "vel", "acc", "dens", "press", "id", "cell", "cell_start", "cell_count"):
+        setattr(v, k, st[k].ctypes.data)
+    st["canonical_count"] = n0
+    st["grid"] = (gx, gy)
+    return st, v
 
 
 class Simulation:
@@ -350,17 +399,8 @@ class Simulation:
     def dump_state(self) -> Dict[str, np.ndarray]:
         """Full state in the internal numbering (see sph_dump_state)."""
         n, n0, gx, gy = self.state_info()
-        st = {k: np.zeros((n, 2), np.float32) for k in ("pos", "prev", "vel", "acc", "dens", "press")}
-        st["id"] = np.zeros(n, np.int32)
-        st["cell"] = np.zeros(n, np.int32)
-        st["cell_start"] = np.zeros(gx * gy, np.int32)
-        st["cell_count"] = np.zeros(gx * gy, np.int32)
-        v = StateView(count=n, canonical_count=n0, grid_x=gx, grid_y=gy)
-        for k in ("pos", "prev", "vel", "acc", "dens", "press", "id", "cell", "cell_start", "cell_count"):
-            setattr(v, k, st[k].ctypes.data)
+        st, v = _state_arrays(n, n0, gx, gy)
         self._call("sph_dump_state", _c.byref(v))
-        st["canonical_count"] = n0
-        st["grid"] = (gx, gy)
         return st
 
     def load_state(self, st: Dict[str, np.ndarray]) -> None:
@@ -387,3 +427,137 @@ class Simulation:
         out = _c.c_uint64()
         self._call("sph_kernel_launches", _c.byref(out))
         return out.value
+
+    def use_graphs(self, enable: bool = True):
+        """Replay repeated updates from a per-step CUDA graph (default on)."""
+        self._call("sph_use_graphs", 1 if enable else 0)
+
+
+def _scene_desc(scene, keep: list) -> SceneDesc:
+    """A ``SceneDesc`` for an object with the ``scenes.Scene`` fields; the
+    arrays it points into are appended to ``keep``."""
+    d = SceneDesc()
+    d.domain = scene.domain()
+    d.params = Params.from_array(scene.params)
+    d.gravity = _v(*scene.gravity)
+    pos = _f2(scene.positions)
+    keep.append(pos)
+    d.particle_count = len(pos)
+    d.positions = pos.ctypes.data if len(pos) else None
+    d.forces = None
+    bodies = []
+    for nx, ny, dist in scene.planes:
+        bodies.append(BodyDesc(type=SPH_BODY_PLANE, a=_v(nx, ny), value=float(dist)))
+    for x, y, r in scene.circles:
+        bodies.append(BodyDesc(type=SPH_BODY_CIRCLE, a=_v(x, y), value=float(r)))
+    for ax, ay, bx, by in scene.segments:
+        bodies.append(BodyDesc(type=SPH_BODY_SEGMENT, a=_v(ax, ay), b=_v(bx, by)))
+    for verts in getattr(scene, "polygons", ()):
+        b = BodyDesc(type=SPH_BODY_POLYGON, vertex_count=len(verts))
+        for k, (x, y) in enumerate(verts):
+            b.verts[k] = _v(x, y)
+        bodies.append(b)
+    arr = (BodyDesc * max(len(bodies), 1))(*bodies)
+    keep.append(arr)
+    d.body_count = len(bodies)
+    d.bodies = _c.addressof(arr) if bodies else None
+    return d
+
+
+class BatchSimulation:
+    """Many independent Demo4 scenes advanced by one update (the batched
+    form of the step; no single reference counterpart).  Each scene's update
+    equals a single-scene ``Simulation`` holding the same state, bit for bit.
+    Scenes are fixed at creation: bodies first in the order planes, circles,
+    segments, polygons (as ``Scene.apply`` adds them), then particles."""
+
+    def __init__(self, scenes, device: int = 0):
+        self._lib = load_library()
+        keep: list = []
+        descs = [_scene_desc(sc, keep) for sc in scenes]
+        arr = (SceneDesc * len(descs))(*descs)
+        h = _c.c_void_p()
+        _check(self._lib.sph_batch_create(_c.addressof(arr), len(descs), int(device), _c.byref(h)),
+               "sph_batch_create")
+        self._h = h
+        self.counts = [int(d.particle_count) for d in descs]
+        self.grids = [d.domain.grid() for d in descs]
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.sph_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _call(self, name: str, *args) -> None:
+        _check(getattr(self._lib, name)(self._h, *args), name)
+
+    @property
+    def scene_count(self) -> int:
+        out = _c.c_size_t()
+        self._call("sph_batch_scene_count", _c.byref(out))
+        return out.value
+
+    def update(self, delta_time: float):
+        self._call("sph_update", float(np.float32(delta_time)))
+
+    def get_particle_count(self) -> int:
+        out = _c.c_size_t()
+        self._call("sph_get_particle_count", _c.byref(out))
+        return out.value
+
+    def get_stats(self, scene: int) -> Stats:
+        s = Stats()
+        self._call("sph_batch_get_stats", int(scene), _c.byref(s))
+        return s
+
+    def read_particles(self, scene: int, fields: Sequence[str] = ("pos", "vel", "dens", "press")
+                       ) -> Dict[str, np.ndarray]:
+        """One scene's arrays in its AddParticle order, as (n, 2) float32."""
+        n = self.counts[scene]
+        out = {f: np.zeros((n, 2), np.float32) for f in fields}
+        ptr = lambda f: out[f].ctypes.data_as(_c.c_void_p) if f in out else None
+        self._call("sph_batch_read_particles", int(scene), n, ptr("pos"), ptr("vel"), ptr("dens"), ptr("press"))
+        return out
+
+    def state_info(self, scene: int) -> Tuple[int, int, int, int]:
+        n, n0 = _c.c_size_t(), _c.c_size_t()
+        gx, gy = _c.c_int(), _c.c_int()
+        self._call("sph_batch_state_info", int(scene), _c.byref(n), _c.byref(n0), _c.byref(gx), _c.byref(gy))
+        return n.value, n0.value, gx.value, gy.value
+
+    def dump_state(self, scene: int) -> Dict[str, np.ndarray]:
+        """One scene's state in scene-local numbers and cells (the layout of
+        ``Simulation.dump_state``)."""
+        n, n0, gx, gy = self.state_info(scene)
+        st, v = _state_arrays(n, n0, gx, gy)
+        self._call("sph_batch_dump_state", int(scene), _c.byref(v))
+        return st
+
+    def stream(self) -> int:
+        out = _c.c_void_p()
+        self._call("sph_get_stream", _c.byref(out))
+        return out.value or 0
+
+    def synchronize(self):
+        self._call("sph_synchronize")
+
+    def kernel_launches(self) -> int:
+        out = _c.c_uint64()
+        self._call("sph_kernel_launches", _c.byref(out))
+        return out.value
+
+    def use_graphs(self, enable: bool = True):
+        """Replay repeated updates from a per-step CUDA graph (default on)."""
+        self._call("sph_use_graphs", 1 if enable else 0)

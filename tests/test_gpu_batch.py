@@ -1,0 +1,128 @@
+"""Batched scenes and per-step graphs, through the C ABI.
+
+A batch advances independent scenes with one launch per stage.  Its
+contract is that every scene evolves exactly as a single-scene simulation
+holding the same scene does -- which the parity tests tie to the reference's
+own update -- so each test compares a batch scene against its own
+single-scene run, bit for bit, over many updates (the state is compared in
+the internal numbering: positions, velocities, densities, ids, cells and the
+cell tables).  Graph replay is checked the same way against eager launches.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import nbodysimulation_experiment_gb300 as pkg
+from nbodysimulation_experiment_gb300 import scenes, simulation
+
+pytestmark = pytest.mark.gpu
+
+STATE_KEYS = ("pos", "prev", "vel", "acc", "dens", "press", "id", "cell", "cell_start", "cell_count")
+
+
+def _single_run(scene, steps, graphs=True):
+    sim = pkg.Simulation(scene.domain())
+    sim.use_graphs(graphs)
+    scene.apply(sim)
+    for _ in range(steps):
+        sim.update(float(scenes.DT))
+    st = sim.dump_state()
+    stats = sim.get_stats()
+    sim.close()
+    return st, stats
+
+
+def _assert_same_state(a, b, what):
+    assert a["canonical_count"] == b["canonical_count"], what
+    for k in STATE_KEYS:
+        assert np.array_equal(a[k], b[k]), (what, k)
+
+
+def test_batch_scenes_equal_single_scene_runs():
+    mix = scenes.batch_scenes(count=5, seed=7, n_min=1024, n_max=6000) + [scenes.dam_break_4096()]
+    steps = 40
+    batch = pkg.BatchSimulation(mix)
+    assert batch.scene_count == len(mix)
+    assert batch.get_particle_count() == sum(s.n for s in mix)
+    for _ in range(steps):
+        batch.update(float(scenes.DT))
+    for k, sc in enumerate(mix):
+        want, want_stats = _single_run(sc, steps)
+        got = batch.dump_state(k)
+        _assert_same_state(got, want, sc.name)
+        st = batch.get_stats(k)
+        for f in ("min_particle_neighbor_count", "max_particle_neighbor_count", "min_cell_particle_count",
+                  "max_cell_particle_count"):
+            assert getattr(st, f) == getattr(want_stats, f), (sc.name, f)
+        rd = batch.read_particles(k)
+        pos = np.zeros_like(got["pos"])
+        pos[got["id"]] = got["pos"]
+        assert np.array_equal(rd["pos"], pos)
+    batch.close()
+
+
+def test_graph_replay_equals_eager_launches():
+    scene = scenes.scaled_block(48)
+    eager, _ = _single_run(scene, 25, graphs=False)
+    graphed, _ = _single_run(scene, 25, graphs=True)
+    _assert_same_state(graphed, eager, "graphs")
+
+
+def test_graph_is_dropped_when_the_scene_changes():
+    """Changing gravity, parameters or adding particles between replays must
+    take effect in the next update (the captured graph holds none of it)."""
+    scene = scenes.scaled_block(32)
+    runs = []
+    for graphs in (False, True):
+        scene.max_particles = scene.n + 64
+        sim = pkg.Simulation(scene.domain())
+        sim.use_graphs(graphs)
+        scene.apply(sim)
+        for k in range(12):
+            if k == 4:
+                sim.set_gravity((1.0, -5.0))
+            if k == 7:
+                sim.add_particles(np.array([[0.0, 0.0], [0.1, 0.05]], np.float32))
+            if k == 9:
+                p = sim.get_params()
+                p.stiffness = 0.5
+                sim.set_params(p)
+            sim.update(float(scenes.DT))
+        runs.append(sim.dump_state())
+        sim.close()
+    scene.max_particles = None
+    _assert_same_state(runs[1], runs[0], "graph invalidation")
+
+
+def test_batch_rejects_single_scene_mutators():
+    batch = pkg.BatchSimulation(scenes.batch_scenes(count=2, seed=3, n_min=1024, n_max=2048))
+    lib = pkg.load_library()
+    v = simulation.Vec2(0.0, 0.0)
+    idx = ctypes.c_size_t()
+    assert lib.sph_add_particle(batch._h, v, v, ctypes.byref(idx)) == simulation.SPH_ERR_NOT_SUPPORTED
+    assert lib.sph_set_gravity(batch._h, v) == simulation.SPH_ERR_NOT_SUPPORTED
+    assert lib.sph_add_circle(batch._h, v, ctypes.c_float(1.0)) == simulation.SPH_ERR_NOT_SUPPORTED
+    st = simulation.Stats()
+    assert lib.sph_batch_get_stats(batch._h, 2, ctypes.byref(st)) == simulation.SPH_ERR_INVALID_ARGUMENT
+    batch.close()
+
+
+def test_full_batch_of_512_scenes():
+    """The 512-scene workload (log-uniform 1,024..65,536 particles, about 8.1M
+    in all): a few updates stay finite and keep every scene's particles, and
+    sampled scenes equal their single-scene runs."""
+    mix = scenes.batch_scenes()
+    steps = 4
+    batch = pkg.BatchSimulation(mix)
+    for _ in range(steps):
+        batch.update(float(scenes.DT))
+    batch.synchronize()
+    rng = np.random.default_rng(0)
+    for k in sorted(rng.choice(len(mix), 3, replace=False).tolist()) + [int(np.argmax([s.n for s in mix]))]:
+        got = batch.dump_state(k)
+        assert np.all(np.isfinite(got["pos"]))
+        assert np.array_equal(np.sort(got["id"]), np.arange(mix[k].n))
+        want, _ = _single_run(mix[k], steps)
+        _assert_same_state(got, want, mix[k].name)
+    batch.close()
