@@ -226,6 +226,42 @@ def bench_batched(torch, pkg, scenes, device: int, steps: int, warmup: int):
                         "each a jittered block + 0-4 circles, 4 walls, plain step, FP32; inputs > L2"}
 
 
+def bench_block_1m(torch, pkg, scenes, device: int, steps: int, warmup: int, springs: bool):
+    """The 1,048,576-particle block (1024x1024 jittered lattice in a
+    204.8 x 115.2 box, four walls), plain or with viscoelastic springs
+    (yield ratio 0.1, plasticity 0.3, stiffness 0.3, at most 16 per
+    particle); event-timed updates on the simulation's stream."""
+    scene = scenes.block_1m()
+    sim = pkg.Simulation(scene.domain(), device=device)
+    scene.apply(sim)
+    if springs:
+        sim.set_springs(True, yield_ratio=0.1, plasticity=0.3, stiffness=0.3, max_per_particle=16)
+    dt = float(scenes.DT)
+    stream = torch.cuda.ExternalStream(sim.stream())
+    for _ in range(warmup):
+        sim.update(dt)
+    sim.synchronize()
+    ms, spring_ms = [], []
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        sim.update(dt)
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+        spring_ms.append(sim.get_stats().time_neighbor_search)
+    out = {"value": scene.n * steps / (sum(ms) / 1e3), "unit": UNIT, "ms_per_step": statistics.mean(ms),
+           "steps": steps, "warmup": warmup, "particles": scene.n, "springs": springs}
+    if springs:
+        out["spring_phase_ms"] = statistics.mean(spring_ms)
+        out["spring_count"] = sim.spring_count()
+    sim.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -236,6 +272,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--batch-steps", type=int, default=20, help="timed updates of the 512-scene batch")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--block-steps", type=int, default=10, help="timed updates of the 1M-particle block")
+    ap.add_argument("--no-block", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
@@ -333,6 +371,11 @@ def main():
         batched = bench_batched(torch, pkg, scenes, local, args.batch_steps, 3)
         batched["vs_plain"] = batched["value"] / value
 
+    block = None
+    if not args.no_block:
+        block = {"plain": bench_block_1m(torch, pkg, scenes, local, args.block_steps, 3, False),
+                 "springs": bench_block_1m(torch, pkg, scenes, local, args.block_steps, 3, True)}
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         from oracle.oracle import OracleSim, build as build_oracle
@@ -359,6 +402,7 @@ def main():
                          "kernel_ms": 1e3 * mean_delta_s},
             "cpu_baseline": cpu,
             "batched": batched,
+            "block_1m": block,
             "clocks": clocks,
         }
         print(json.dumps(line), flush=True)

@@ -213,6 +213,38 @@ int sph_kernel_launches(sph_sim *sim, uint64_t *out);
  * kernel one by one instead.  Results are identical either way.  Default 1. */
 int sph_use_graphs(sph_sim *sim, int enable);
 
+/* ---- Viscoelastic springs (no reference counterpart) ----------------------
+ * Springs with plasticity after Clavet et al. 2005 ("Particle-based
+ * viscoelastic fluid simulation", Algorithms 3 and 4), in a deterministic
+ * parallel form run between the neighbour search and density: existing
+ * springs within h are adjusted (tolerable deformation yield_ratio * L,
+ * rate plasticity), springs whose rest length exceeds h are removed, free
+ * slots go to the nearest in-range neighbours without a spring (ordered by
+ * distance, then AddParticle index) and a spring is added where both ends
+ * chose each other (rest length h, adjusted at once); then every particle
+ * moves by -D/2 of each of its springs, D = dt^2 stiffness (1 - L/h) (L - r)
+ * r_hat, from the positions before the phase.  At most max_per_particle
+ * (<= 16) springs per particle.  Off by default; single-scene simulations
+ * only.  Enabling allocates the spring arrays (128 B per particle per buffer
+ * set). */
+typedef struct sph_spring_params {
+	int enabled;
+	float yield_ratio;     /* gamma */
+	float plasticity;      /* alpha */
+	float stiffness;       /* k_spring */
+	int max_per_particle;  /* <= 16 */
+} sph_spring_params;
+int sph_set_springs(sph_sim *sim, const sph_spring_params *params);
+/* Springs after the last update (each counted once). */
+int sph_get_spring_count(sph_sim *sim, uint64_t *out);
+/* Spring tables in the internal numbering of sph_dump_state: per particle a
+ * count and 16 slots of partner number (-1 past the count) and rest length.
+ * `count` must equal the particle count.  sph_load_state clears the springs;
+ * sph_load_springs (after it) sets them. */
+int sph_dump_springs(sph_sim *sim, size_t count, int32_t *spring_count, int32_t *partner, float *rest);
+int sph_load_springs(sph_sim *sim, size_t count, const int32_t *spring_count, const int32_t *partner,
+                     const float *rest);
+
 /* ---- Batched scenes (no single reference counterpart) ---------------------
  * Many independent Demo4 scenes advanced together: one sph_update(sim, dt)
  * advances every scene by dt with one launch per stage over all of them.

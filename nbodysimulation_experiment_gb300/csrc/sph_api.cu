@@ -37,6 +37,8 @@ struct Emitter {
 struct BufferSet {
 	float2 *pos = nullptr, *prev = nullptr, *vel = nullptr, *acc = nullptr, *dens = nullptr, *press = nullptr;
 	int *id = nullptr, *cellOf = nullptr;
+	int *springN = nullptr, *springP = nullptr;  // allocated when springs are first enabled
+	float *springL = nullptr;
 	Particles view() const {
 		Particles p;
 		p.pos = pos;
@@ -47,11 +49,25 @@ struct BufferSet {
 		p.press = press;
 		p.id = id;
 		p.cellOf = cellOf;
+		p.springN = springN;
+		p.springP = springP;
+		p.springL = springL;
 		return p;
 	}
 };
 
-enum Stage { kEvBegin, kEvIntegrate, kEvVisc, kEvPredict, kEvGrid, kEvDensity, kEvDelta, kEvCollide, kEvCount };
+enum Stage {
+	kEvBegin,
+	kEvIntegrate,
+	kEvVisc,
+	kEvPredict,
+	kEvGrid,
+	kEvSprings,
+	kEvDensity,
+	kEvDelta,
+	kEvCollide,
+	kEvCount
+};
 
 // One scene: the state Demo4::ParticleSimulation keeps on the host.
 struct Scene {
@@ -67,6 +83,7 @@ struct Scene {
 	size_t nDev = 0;  // particles already on the device
 	size_t cap = 0;   // particle capacity
 	int cellBase = 0, pBase = 0, bodyBase = 0;  // offsets into the shared arrays
+	sph_spring_params springs{};
 	std::vector<float2> pendPos, pendForce;
 };
 
@@ -82,7 +99,9 @@ struct sph_sim {
 
 	std::vector<Scene> scenes;
 	int ncellTotal = 0;
+	size_t capTotal = 0;
 	size_t bodyCap = 0;
+	int springBlocks = 0;
 	bool sceneTableDirty = true;
 	bool bodiesDirty = true;
 	float tableDt = 0.0f;
@@ -181,6 +200,12 @@ StepParams step_params(const Scene &sc, float dt) {
 	p.radius = sc.dom.particle_radius;
 	p.margin = sc.dom.collision_margin;
 	p.nbodies = (int)sc.bodies.size();
+	p.springs = sc.springs.enabled ? 1 : 0;
+	p.springMax = sc.springs.max_per_particle;
+	p.h = sc.params.kernel_height;
+	p.springYield = sc.springs.yield_ratio;
+	p.springDtAlpha = dt * sc.springs.plasticity;
+	p.springK = sc.springs.stiffness;
 	return p;
 }
 
@@ -453,6 +478,20 @@ int enqueue_step(sph_sim *s, bool capturing) {
 	SPH_LAUNCHED(s);
 	SPH_CUDA(mark(kEvGrid));
 
+	bool anySprings = false;
+	for (const Scene &sc : s->scenes) anySprings = anySprings || sc.springs.enabled;
+	if (anySprings) {
+		k_springs_select<<<s->springBlocks, kSpringWarps * kWarp, springs_smem_bytes(), st>>>(tt, A.view(),
+		                                                                                      B.view(), T);
+		SPH_LAUNCHED(s);
+		k_springs_commit<<<blocks_for(tt.n, kElemThreads), kElemThreads, 0, st>>>(tt, B.view(), T);
+		SPH_LAUNCHED(s);
+		k_springs_apply<<<blocks_for(tt.n, kElemThreads), kElemThreads, 0, st>>>(tt, B.view(), T);
+		SPH_LAUNCHED(s);
+		SPH_CUDA(cudaMemcpyAsync(B.pos, T.springPos, sizeof(float2) * tt.n, cudaMemcpyDeviceToDevice, st));
+	}
+	SPH_CUDA(mark(kEvSprings));
+
 	k_density<<<s->densBlocks, kDensWarps * kWarp, dens_smem_bytes(), st>>>(tt, B.view(), T);
 	SPH_LAUNCHED(s);
 	SPH_CUDA(mark(kEvDensity));
@@ -565,6 +604,7 @@ int allocate(sph_sim *s) {
 		if (ncell > (1 << 28) || pBase > (1 << 30)) return SPH_ERR_CAPACITY;
 	}
 	s->ncellTotal = (int)ncell;
+	s->capTotal = (size_t)pBase;
 	const size_t N = (size_t)pBase, C = (size_t)ncell, S = s->scenes.size();
 	int rc = SPH_OK;
 	if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) return SPH_ERR_CUDA;
@@ -655,7 +695,9 @@ int allocate(sph_sim *s) {
 	    cudaFuncSetAttribute(k_delta, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)delta_smem_bytes()) !=
 	        cudaSuccess ||
 	    cudaFuncSetAttribute(k_density, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dens_smem_bytes()) !=
-	        cudaSuccess)
+	        cudaSuccess ||
+	    cudaFuncSetAttribute(k_springs_select, cudaFuncAttributeMaxDynamicSharedMemorySize,
+	                         (int)springs_smem_bytes()) != cudaSuccess)
 		return SPH_ERR_CUDA;
 	int occ = 0;
 	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_viscosity, kViscTaskWarps * kWarp, visc_smem_bytes()) !=
@@ -669,6 +711,7 @@ int allocate(sph_sim *s) {
 		return SPH_ERR_CUDA;
 	s->deltaBlocks = occ * s->numSMs;
 	s->densBlocks = std::max(1, std::min(blocks_for(C, kDensWarps), 64 * s->numSMs));
+	s->springBlocks = std::max(1, std::min(blocks_for(C, kSpringWarps), 64 * s->numSMs));
 	s->gridBlocks = std::max(1, std::min(blocks_for(C, kGridWarps), 64 * s->numSMs));
 	return SPH_OK;
 }
@@ -940,7 +983,7 @@ int sph_destroy(sph_sim *s) {
 	drop_graphs(s);
 	for (int b = 0; b < 2; ++b) {
 		BufferSet &B = s->buf[b];
-		void *ptrs[] = {B.pos, B.prev, B.vel, B.acc, B.dens, B.press, B.id, B.cellOf};
+		void *ptrs[] = {B.pos, B.prev, B.vel, B.acc, B.dens, B.press, B.id, B.cellOf, B.springN, B.springP, B.springL};
 		for (void *p : ptrs)
 			if (p) cudaFree(p);
 	}
@@ -951,7 +994,7 @@ int sph_destroy(sph_sim *s) {
 	                T.enterCount,  T.leaveCount,  T.enterOffset, T.enterCursor, T.enterList,   T.moverCount,
 	                T.bbox,        T.newIdx,      T.newLabel,    T.taskCounter, T.stats,       T.error,
 	                T.abort,       T.bodies,      s->doneV,      s->doneD,      s->stagePos,   s->stageForce,
-	                s->prof};
+	                s->prof,       T.accN,        T.accP,        T.springPos,   T.springTotal};
 	for (void *p : ptrs)
 		if (p) cudaFree(p);
 	if (s->hostPos) cudaFreeHost(s->hostPos);
@@ -1178,7 +1221,9 @@ int sph_batch_get_stats(sph_sim *s, size_t scene, sph_stats *out) {
 	out->time_viscosity_forces = t[kEvVisc];
 	out->time_predict = t[kEvPredict];
 	out->time_update_grid = t[kEvGrid];
-	out->time_neighbor_search = 0.0f;  // the grid update builds the neighbour structure
+	// The grid update builds the neighbour structure; this slot holds the
+	// spring phase, which runs on the fresh lists (0 when springs are off).
+	out->time_neighbor_search = t[kEvSprings];
 	out->time_density_and_pressure = t[kEvDensity];
 	out->time_delta_positions = t[kEvDelta];
 	out->time_collisions = t[kEvCollide];
@@ -1278,6 +1323,7 @@ int sph_load_state(sph_sim *s, const sph_state_view *v) {
 	    (rc = h2d(s->cellCountA, v->cell_count, sc.ncell * 4)))
 		return rc;
 	SPH_CUDA(cudaMemcpyAsync(s->T.appCount, app.data(), sc.ncell * 4, cudaMemcpyHostToDevice, st));
+	if (A.springN && n) SPH_CUDA(cudaMemsetAsync(A.springN, 0, n * sizeof(int), st));  // sph_load_springs sets them
 	SPH_CUDA(cudaStreamSynchronize(st));  // `app` is a host temporary
 	sc.n = sc.nDev = n;
 	sc.n0 = v->canonical_count;
@@ -1332,6 +1378,104 @@ int sph_profile_read(sph_sim *s, unsigned long long *out, size_t capacity, size_
 	const size_t total = std::min(capacity, (size_t)8 * s->doneDCap);
 	SPH_CUDA(cudaStreamSynchronize(s->stream));
 	SPH_CUDA(cudaMemcpy(out, s->prof, total * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+	return SPH_OK;
+}
+
+int sph_set_springs(sph_sim *s, const sph_spring_params *p) {
+	if (!p) return SPH_ERR_INVALID_ARGUMENT;
+	Scene *sc = single(s);
+	if (!sc) return not_single(s);
+	if (p->enabled && (p->max_per_particle < 0 || p->max_per_particle > kSprings || !(p->yield_ratio >= 0.0f) ||
+	                   !(p->plasticity >= 0.0f)))
+		return SPH_ERR_INVALID_ARGUMENT;
+	if (p->enabled && !s->buf[0].springN) {
+		const size_t N = s->capTotal, S = s->scenes.size();
+		SPH_CUDA(cudaStreamSynchronize(s->stream));
+		int rc;
+		for (int b = 0; b < 2; ++b) {
+			BufferSet &B = s->buf[b];
+			if ((rc = dalloc(&B.springN, N)) || (rc = dalloc(&B.springP, N * kSprings)) ||
+			    (rc = dalloc(&B.springL, N * kSprings)))
+				return rc;
+		}
+		if ((rc = dalloc(&s->T.accN, N)) || (rc = dalloc(&s->T.accP, N * kSprings)) ||
+		    (rc = dalloc(&s->T.springPos, N)) || (rc = dalloc(&s->T.springTotal, S)))
+			return rc;
+	}
+	if (p->enabled && !sc->springs.enabled) {
+		// Springs start empty whenever they are switched on.
+		for (int b = 0; b < 2; ++b)
+			SPH_CUDA(cudaMemsetAsync(s->buf[b].springN, 0, s->capTotal * sizeof(int), s->stream));
+	}
+	sc->springs = *p;
+	s->sceneTableDirty = true;
+	return SPH_OK;
+}
+
+int sph_get_spring_count(sph_sim *s, uint64_t *out) {
+	if (!s || !out) return SPH_ERR_INVALID_ARGUMENT;
+	*out = 0;
+	if (!s->T.springTotal) return SPH_OK;
+	int rc = check_device_errors(s);
+	if (rc) return rc;
+	std::vector<unsigned long long> t(s->scenes.size());
+	SPH_CUDA(cudaMemcpy(t.data(), s->T.springTotal, t.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+	unsigned long long total = 0;
+	for (unsigned long long v : t) total += v;
+	*out = total / 2;  // each spring is stored at both ends
+	return SPH_OK;
+}
+
+int sph_dump_springs(sph_sim *s, size_t count, int32_t *spring_count, int32_t *partner, float *rest) {
+	Scene *sc = single(s);
+	if (!sc) return not_single(s);
+	int rc = flush_adds(s);
+	if (rc) return rc;
+	if (count != sc->n) return SPH_ERR_INVALID_ARGUMENT;
+	const BufferSet &A = s->buf[s->cur];
+	std::vector<int32_t> cnt(count), part(count * kSprings);
+	std::vector<float> len(count * kSprings);
+	if (A.springN && count) {
+		SPH_CUDA(cudaMemcpyAsync(cnt.data(), A.springN, count * 4, cudaMemcpyDeviceToHost, s->stream));
+		SPH_CUDA(cudaMemcpyAsync(part.data(), A.springP, count * kSprings * 4, cudaMemcpyDeviceToHost, s->stream));
+		SPH_CUDA(cudaMemcpyAsync(len.data(), A.springL, count * kSprings * 4, cudaMemcpyDeviceToHost, s->stream));
+	}
+	rc = check_device_errors(s);
+	if (rc) return rc;
+	for (size_t i = 0; i < count; ++i) {
+		const int c = std::min(std::max(cnt[i], 0), kSprings);
+		if (spring_count) spring_count[i] = c;
+		for (int q = 0; q < kSprings; ++q) {
+			if (partner) partner[i * kSprings + q] = q < c ? part[i * kSprings + q] : -1;
+			if (rest) rest[i * kSprings + q] = q < c ? len[i * kSprings + q] : 0.0f;
+		}
+	}
+	return SPH_OK;
+}
+
+int sph_load_springs(sph_sim *s, size_t count, const int32_t *spring_count, const int32_t *partner,
+                     const float *rest) {
+	Scene *sc = single(s);
+	if (!sc) return not_single(s);
+	if (!spring_count || !partner || !rest) return SPH_ERR_INVALID_ARGUMENT;
+	BufferSet &A = s->buf[s->cur];
+	if (!A.springN) return SPH_ERR_NOT_SUPPORTED;  // springs were never enabled
+	int rc = flush_adds(s);
+	if (rc) return rc;
+	if (count != sc->n) return SPH_ERR_INVALID_ARGUMENT;
+	for (size_t i = 0; i < count; ++i) {
+		if (spring_count[i] < 0 || spring_count[i] > kSprings) return SPH_ERR_INVALID_ARGUMENT;
+		for (int q = 0; q < spring_count[i]; ++q) {
+			const int32_t p = partner[i * kSprings + q];
+			if (p < 0 || (size_t)p >= count || (size_t)p == i) return SPH_ERR_INVALID_ARGUMENT;
+		}
+	}
+	if (count) {
+		SPH_CUDA(cudaMemcpyAsync(A.springN, spring_count, count * 4, cudaMemcpyHostToDevice, s->stream));
+		SPH_CUDA(cudaMemcpyAsync(A.springP, partner, count * kSprings * 4, cudaMemcpyHostToDevice, s->stream));
+		SPH_CUDA(cudaMemcpyAsync(A.springL, rest, count * kSprings * 4, cudaMemcpyHostToDevice, s->stream));
+	}
+	SPH_CUDA(cudaStreamSynchronize(s->stream));
 	return SPH_OK;
 }
 

@@ -34,6 +34,8 @@ constexpr int kMaxPoly = 8;      // kMaxScenarioPolygonCount, sph.h:161
 // Appendix particles (added since the last update) are swept serially in runs
 // of this many consecutive numbers.
 constexpr int kAppendixRun = 32;
+// Spring slots per particle (viscoelastic springs, not in the reference).
+constexpr int kSprings = 16;
 
 // Error bits raised by kernels into SimTables::error.
 enum : uint32_t {
@@ -69,6 +71,13 @@ struct StepParams {
 	float radius;   // kSPHParticleCollisionRadius
 	float margin;   // kSPHCollisionMargin
 	int nbodies;
+	// Viscoelastic springs (Clavet et al. 2005; not in the reference).
+	int springs;          // 0 = off
+	int springMax;        // slots a particle may fill (<= kSprings)
+	float h;              // kernel height: initial and maximum rest length
+	float springYield;    // gamma: tolerable deformation = gamma * L
+	float springDtAlpha;  // dt * plasticity alpha
+	float springK;        // spring stiffness
 };
 
 // One scene of a simulation.  A simulation holds one or more independent
@@ -98,6 +107,11 @@ struct Particles {
 	float2 *pos, *prev, *vel, *acc, *dens, *press;
 	int *id;      // AddParticle index
 	int *cellOf;  // linear cell of the last grid insertion
+	// Springs (null when off): per particle a count and kSprings slots of
+	// partner number and rest length, [particle][slot]; every spring is
+	// stored at both ends with the same rest length.
+	int *springN, *springP;
+	float *springL;
 };
 
 // Grid and scheduling tables.  Canonical numbering: the particles of cell c
@@ -124,6 +138,11 @@ struct SimTables {
 	uint32_t *error;
 	uint32_t *abort;
 	Body *bodies;
+	// Spring phase scratch (null when off): chosen candidates per particle
+	// (count, kSprings new numbers), positions after the phase, springs per scene.
+	int *accN, *accP;
+	float2 *springPos;
+	unsigned long long *springTotal;
 	// Diagnostics: when non-null, sweep tasks record %globaltimer stamps
 	// (claimed, dependencies met, staged, done) at prof[(sweep * profStride + task) * 4].
 	unsigned long long *prof;

@@ -451,6 +451,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(Totals tt, SimTables T) {
 		// Neighbour-count statistics restart every search (demo4.cpp:369-370).
 		T.stats[4 * sc + 0] = T.scenes[sc].nbSeed;
 		T.stats[4 * sc + 1] = 0;
+		if (T.springTotal) T.springTotal[sc] = 0;
 	}
 }
 
@@ -1254,6 +1255,7 @@ __global__ void k_add(int first, int count, int scene, int firstId, const float2
 	P.dens[i] = make_float2(0.f, 0.f);
 	P.press[i] = make_float2(0.f, 0.f);
 	P.id[i] = firstId + j;
+	if (P.springN) P.springN[i] = 0;
 	T.sceneOf[i] = scene;
 	const int c = sc.cellBase + cell_of(x, sc.p);
 	P.cellOf[i] = c;

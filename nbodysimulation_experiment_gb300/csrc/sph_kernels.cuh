@@ -12,6 +12,7 @@ constexpr int kGridWarps = 4;
 constexpr int kScanThreads = 1024;
 constexpr int kElemThreads = 256;  // elementwise kernels
 constexpr int kCollideThreads = 256;
+constexpr int kSpringWarps = 4;
 
 struct ViscSmem;
 struct DeltaSmem;
@@ -20,6 +21,7 @@ struct DensWarp;
 size_t visc_smem_bytes();
 size_t delta_smem_bytes();
 size_t dens_smem_bytes();
+size_t springs_smem_bytes();
 
 __global__ void k_integrate(Totals tt, Particles P, SimTables T);
 __global__ void k_viscosity(Totals tt, Particles P, SimTables T);
@@ -33,5 +35,8 @@ __global__ void k_collide(Totals tt, Particles P, Particles Q, SimTables T);
 __global__ void k_add(int first, int count, int scene, int firstId, const float2 *pos, const float2 *force,
                       Particles P, SimTables T);
 __global__ void k_gather_by_id(int first, int count, const int *id, const float2 *src, float2 *dst);
+__global__ void k_springs_select(Totals tt, Particles P, Particles Q, SimTables T);
+__global__ void k_springs_commit(Totals tt, Particles Q, SimTables T);
+__global__ void k_springs_apply(Totals tt, Particles Q, SimTables T);
 
 }  // namespace sphgb

@@ -1,0 +1,241 @@
+// Viscoelastic springs with plasticity (Clavet et al. 2005, "Particle-based
+// viscoelastic fluid simulation", Algorithms 3 and 4).  The reference's
+// Demo4 step has no springs; this is the deterministic parallel form of the
+// paper's two loops, run after the grid update (new numbering, predicted
+// positions) and before density:
+//
+//  k_springs_select  per particle: adjust existing springs within h, drop
+//                    those whose rest length exceeds h, and choose the nearest
+//                    in-range candidates without a spring for the free slots,
+//                    ordered by (r^2, AddParticle index);
+//  k_springs_commit  add a spring where both ends chose each other (rest
+//                    length h, adjusted like the others);
+//  k_springs_apply   move every particle by -D/2 of each of its springs,
+//                    D = dt^2 k (1 - L/h) (L - r) r_hat, from the positions
+//                    before the phase (Jacobi), summed in slot order.
+//
+// Every spring is stored at both ends.  Both ends compute the same length r
+// (the two difference vectors are exact negations), so they keep equal rest
+// lengths and drop the spring together.  Spring partners are particle
+// numbers, remapped to the new numbering here.
+#include <cuda_runtime.h>
+
+#include "sph_internal.cuh"
+#include "sph_kernels.cuh"
+
+namespace sphgb {
+
+namespace {
+
+constexpr unsigned kFullMask = 0xffffffffu;
+
+// Rest length of a spring of length r < h after plasticity (Algorithm 4).
+__device__ __forceinline__ float plastic(float L, float r, const StepParams &s) {
+	const float d = s.springYield * L;
+	if (r > L + d) return L + s.springDtAlpha * ((r - L) - d);
+	if (r < L - d) return L - s.springDtAlpha * ((L - d) - r);
+	return L;
+}
+
+// Candidate order: nearer first, then the smaller AddParticle index.
+__device__ __forceinline__ bool before(float r2a, int ta, float r2b, int tb) {
+	return r2a < r2b || (r2a == r2b && ta < tb);
+}
+
+template <int NSEG>
+__device__ __forceinline__ int seg_number(int e, const int (&off)[NSEG], const int (&start)[NSEG]) {
+	int src = start[0] + e;
+#pragma unroll
+	for (int q = 1; q < NSEG; ++q) src = (e >= off[q]) ? start[q] + (e - off[q]) : src;
+	return src;
+}
+
+}  // namespace
+
+// One warp per new cell: the 3x3 block of new cells (positions, numbers'
+// AddParticle indices) is staged once; each lane handles one particle of the
+// cell.  The candidate scan runs over the block in the same order for every
+// lane, so the warp stays converged apart from the insertions.
+struct SpringWarp {
+	float2 pos[kStageCap];
+	int tag[kStageCap];
+	int ex[kWarp][kSprings];     // existing partners (new numbers) per lane
+	float kr2[kWarp][kSprings];  // chosen candidates per lane, sorted
+	int ktag[kWarp][kSprings];
+	int kj[kWarp][kSprings];
+};
+
+size_t springs_smem_bytes() { return sizeof(SpringWarp) * kSpringWarps; }
+
+__global__ void __launch_bounds__(kSpringWarps * kWarp) k_springs_select(Totals tt, Particles P, Particles Q,
+                                                                        SimTables T) {
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	SpringWarp &S = reinterpret_cast<SpringWarp *>(smem_raw)[threadIdx.x / kWarp];
+	const int lane = threadIdx.x & (kWarp - 1);
+	const int warpsTotal = gridDim.x * kSpringWarps;
+	for (int c = blockIdx.x * kSpringWarps + threadIdx.x / kWarp; c < tt.ncell; c += warpsTotal) {
+		const int cnt = T.newCount[c];
+		if (cnt == 0) continue;
+		const SceneDev &sc = T.scenes[T.sceneOfCell[c]];
+		const StepParams &s = sc.p;
+		if (!s.springs) continue;
+		const int base = sc.cellBase;
+		const int cx = (c - base) % s.gx, cy = (c - base) / s.gx;
+		int segStart[9], segOff[9];
+		int L = 0;
+#pragma unroll
+		for (int q = 0; q < 9; ++q) {
+			const int x = cx + q % 3 - 1, y = cy + q / 3 - 1;
+			int st = 0, nn = 0;
+			if (x >= 0 && x < s.gx && y >= 0 && y < s.gy) {
+				const int c2 = base + y * s.gx + x;
+				st = T.newStart[c2];
+				nn = T.newCount[c2];
+			}
+			segStart[q] = st;
+			segOff[q] = L;
+			L += nn;
+		}
+		if (L > kStageCap) {
+			if (lane == 0) atomicOr(T.error, kErrStageOverflow);
+			continue;
+		}
+		for (int e = lane; e < L; e += kWarp) {
+			const int num = seg_number<9>(e, segOff, segStart);
+			S.pos[e] = Q.pos[num];
+			S.tag[e] = P.id[T.newIdx[num]];
+		}
+		__syncwarp();
+		const int st = T.newStart[c];
+		for (int g = 0; g < cnt; g += kWarp) {
+			const int jj = g + lane;
+			const bool active = jj < cnt;
+			const int j = st + jj;
+			float2 xi = make_float2(0.f, 0.f);
+			int ne = 0, m = 0, kc = 0, freeSlots = 0;
+			if (active) {
+				xi = Q.pos[j];
+				const int o = T.newIdx[j];
+				ne = P.springN[o];
+				if (ne > kSprings) {
+					atomicOr(T.error, kErrIndex);
+					ne = kSprings;
+				}
+				for (int q = 0; q < ne; ++q) {
+					const int pn = T.newLabel[P.springP[o * kSprings + q]];
+					float rest = P.springL[o * kSprings + q];
+					S.ex[lane][q] = pn;
+					const float2 xp = Q.pos[pn];
+					const float rx = xp.x - xi.x, ry = xp.y - xi.y;
+					const float r2 = rx * rx + ry * ry;
+					if (r2 < s.h2) rest = plastic(rest, sqrtf(r2), s);
+					if (rest <= s.h) {
+						Q.springP[j * kSprings + m] = pn;
+						Q.springL[j * kSprings + m] = rest;
+						++m;
+					}
+				}
+				freeSlots = s.springMax - m;
+			}
+			// Candidates: every list member in range without a spring.
+			for (int e = 0; e < L; ++e) {
+				const int num = seg_number<9>(e, segOff, segStart);
+				const float2 xj = S.pos[e];
+				if (!active || freeSlots <= 0 || num == j) continue;
+				const float rx = xj.x - xi.x, ry = xj.y - xi.y;
+				const float r2 = rx * rx + ry * ry;
+				if (!(r2 < s.h2)) continue;
+				bool has = false;
+				for (int q = 0; q < ne; ++q) has = has || S.ex[lane][q] == num;
+				if (has) continue;
+				const int tj = S.tag[e];
+				if (kc == freeSlots && !before(r2, tj, S.kr2[lane][kc - 1], S.ktag[lane][kc - 1])) continue;
+				int at = kc < freeSlots ? kc++ : kc - 1;
+				while (at > 0 && before(r2, tj, S.kr2[lane][at - 1], S.ktag[lane][at - 1])) {
+					S.kr2[lane][at] = S.kr2[lane][at - 1];
+					S.ktag[lane][at] = S.ktag[lane][at - 1];
+					S.kj[lane][at] = S.kj[lane][at - 1];
+					--at;
+				}
+				S.kr2[lane][at] = r2;
+				S.ktag[lane][at] = tj;
+				S.kj[lane][at] = num;
+			}
+			if (active) {
+				T.accN[j] = kc;
+				for (int q = 0; q < kc; ++q) T.accP[j * kSprings + q] = S.kj[lane][q];
+				Q.springN[j] = m;
+			}
+			__syncwarp();
+		}
+		__syncwarp();
+	}
+}
+
+// A spring joins both ends where each chose the other.
+__global__ void k_springs_commit(Totals tt, Particles Q, SimTables T) {
+	const int j = blockIdx.x * blockDim.x + threadIdx.x;
+	int m = 0, sid = -1;
+	if (j < tt.n) {
+		sid = T.sceneOf[j];
+		const StepParams &s = T.scenes[sid].p;
+		if (s.springs) {
+			m = Q.springN[j];
+			const float2 xi = Q.pos[j];
+			const int na = T.accN[j];
+			for (int q = 0; q < na; ++q) {
+				const int p = T.accP[j * kSprings + q];
+				const int np = T.accN[p];
+				bool mutual = false;
+				for (int q2 = 0; q2 < np; ++q2) mutual = mutual || T.accP[p * kSprings + q2] == j;
+				if (!mutual) continue;
+				const float2 xp = Q.pos[p];
+				const float rx = xp.x - xi.x, ry = xp.y - xi.y;
+				const float rest = plastic(s.h, sqrtf(rx * rx + ry * ry), s);
+				if (rest <= s.h) {
+					Q.springP[j * kSprings + m] = p;
+					Q.springL[j * kSprings + m] = rest;
+					++m;
+				}
+			}
+			Q.springN[j] = m;
+		}
+	}
+	// Springs per scene (each counted at both ends): one atomic per group of
+	// lanes of one scene.
+	const unsigned same = __match_any_sync(kFullMask, sid);
+	const unsigned total = __reduce_add_sync(same, (unsigned)m);
+	if (sid >= 0 && total && (threadIdx.x & (kWarp - 1)) == __ffs(same) - 1)
+		atomicAdd(&T.springTotal[sid], (unsigned long long)total);
+}
+
+// Spring displacements from the positions before the phase.
+__global__ void k_springs_apply(Totals tt, Particles Q, SimTables T) {
+	const int j = blockIdx.x * blockDim.x + threadIdx.x;
+	if (j >= tt.n) return;
+	const StepParams &s = T.scenes[T.sceneOf[j]].p;
+	const float2 xi = Q.pos[j];
+	if (!s.springs) {
+		T.springPos[j] = xi;
+		return;
+	}
+	float dx = 0.0f, dy = 0.0f;
+	const int m = Q.springN[j];
+	const float kdt2 = s.dt2 * s.springK;
+	for (int q = 0; q < m; ++q) {
+		const int p = Q.springP[j * kSprings + q];
+		const float rest = Q.springL[j * kSprings + q];
+		const float2 xp = Q.pos[p];
+		const float rx = xp.x - xi.x, ry = xp.y - xi.y;
+		const float r = sqrtf(rx * rx + ry * ry);
+		const float len = r == 0.0f ? 1.0f : r;
+		const float inv = 1.0f / len;
+		const float nx = rx * inv, ny = ry * inv;
+		const float f = (kdt2 * (1.0f - rest * s.invH)) * (rest - r);
+		dx = dx - (f * nx) * 0.5f;
+		dy = dy - (f * ny) * 0.5f;
+	}
+	T.springPos[j] = make_float2(dx + xi.x, dy + xi.y);
+}
+
+}  // namespace sphgb

@@ -87,6 +87,16 @@ class StateView(ctypes.Structure):
     ]
 
 
+class SpringParams(ctypes.Structure):
+    """``sph_spring_params``: viscoelastic springs (Clavet et al. 2005)."""
+
+    _fields_ = [("enabled", _c.c_int), ("yield_ratio", _c.c_float), ("plasticity", _c.c_float),
+                ("stiffness", _c.c_float), ("max_per_particle", _c.c_int)]
+
+
+SPRING_SLOTS = 16
+
+
 class BodyDesc(ctypes.Structure):
     """``sph_body_desc``: one collision body of a batched scene."""
 
@@ -179,6 +189,10 @@ def load_library(build_if_missing: bool = True):
         "sph_synchronize": [vp],
         "sph_kernel_launches": [vp, P(_c.c_uint64)],
         "sph_use_graphs": [vp, _c.c_int],
+        "sph_set_springs": [vp, P(SpringParams)],
+        "sph_get_spring_count": [vp, P(_c.c_uint64)],
+        "sph_dump_springs": [vp, _c.c_size_t, vp, vp, vp],
+        "sph_load_springs": [vp, _c.c_size_t, vp, vp, vp],
         "sph_batch_create": [vp, _c.c_size_t, _c.c_int, P(vp)],
         "sph_batch_scene_count": [vp, P(_c.c_size_t)],
         "sph_batch_read_particles": [vp, _c.c_size_t, _c.c_size_t, vp, vp, vp, vp],
@@ -209,7 +223,8 @@ C_SYMBOLS = (
     "sph_set_multithreading", "sph_is_multithreading_supported", "sph_is_multithreading",
     "sph_get_worker_thread_count", "sph_read_particles", "sph_state_info", "sph_dump_state", "sph_load_state",
     "sph_get_stream", "sph_device_arrays", "sph_synchronize", "sph_kernel_launches",
-    "sph_use_graphs", "sph_batch_create", "sph_batch_scene_count", "sph_batch_read_particles", "sph_batch_get_stats",
+    "sph_use_graphs", "sph_set_springs", "sph_get_spring_count", "sph_dump_springs", "sph_load_springs",
+    "sph_batch_create", "sph_batch_scene_count", "sph_batch_read_particles", "sph_batch_get_stats",
     "sph_batch_state_info", "sph_batch_dump_state",
 )
 
@@ -431,6 +446,34 @@ class Simulation:
     def use_graphs(self, enable: bool = True):
         """Replay repeated updates from a per-step CUDA graph (default on)."""
         self._call("sph_use_graphs", 1 if enable else 0)
+
+    # --- viscoelastic springs (no reference counterpart) ----------------------
+    def set_springs(self, enabled: bool = True, yield_ratio: float = 0.1, plasticity: float = 0.3,
+                    stiffness: float = 0.3, max_per_particle: int = SPRING_SLOTS):
+        p = SpringParams(1 if enabled else 0, float(yield_ratio), float(plasticity), float(stiffness),
+                         int(max_per_particle))
+        self._call("sph_set_springs", _c.byref(p))
+
+    def spring_count(self) -> int:
+        out = _c.c_uint64()
+        self._call("sph_get_spring_count", _c.byref(out))
+        return out.value
+
+    def dump_springs(self):
+        """(count (n,), partner (n, 16) internal numbers or -1, rest (n, 16))."""
+        n = self.get_particle_count()
+        count = np.zeros(n, np.int32)
+        partner = np.zeros((n, SPRING_SLOTS), np.int32)
+        rest = np.zeros((n, SPRING_SLOTS), np.float32)
+        self._call("sph_dump_springs", n, count.ctypes.data, partner.ctypes.data, rest.ctypes.data)
+        return count, partner, rest
+
+    def load_springs(self, count, partner, rest):
+        n = len(count)
+        count = np.ascontiguousarray(count, np.int32)
+        partner = np.ascontiguousarray(partner, np.int32).reshape(n, SPRING_SLOTS)
+        rest = np.ascontiguousarray(rest, np.float32).reshape(n, SPRING_SLOTS)
+        self._call("sph_load_springs", n, count.ctypes.data, partner.ctypes.data, rest.ctypes.data)
 
 
 def _scene_desc(scene, keep: list) -> SceneDesc:

@@ -334,8 +334,7 @@ class OracleSim(_CpuSim):
     def _raw_lib(cls):
         if not hasattr(cls, "_raw"):
             path = os.path.join(REF_DIR, "liboracle.so")
-            if not os.path.exists(path):
-                build(reference=False)
+            build(reference=False)  # make: rebuilds only when a source changed
             cls._raw = ctypes.CDLL(path)
         return cls._raw
 
@@ -376,4 +375,50 @@ class OracleSim(_CpuSim):
     @classmethod
     def hardware_threads(cls) -> int:
         return int(cls._raw_lib().sph_oracle_hardware_threads())
+
+    # --- viscoelastic springs (restated from Clavet et al. 2005) -------------
+    SPRING_SLOTS = 16
+
+    def set_springs(self, enabled: bool, yield_ratio: float = 0.1, plasticity: float = 0.3,
+                    stiffness: float = 0.3, max_per_particle: int = 16):
+        fn = self._lib.sph_oracle_set_springs
+        fn.argtypes = [_vp, _i, _f, _f, _f, _i]
+        fn.restype = None
+        fn(self._h, 1 if enabled else 0, float(yield_ratio), float(plasticity), float(stiffness),
+           int(max_per_particle))
+
+    def set_spring_state(self, count, partner, rest, tag=None):
+        """Springs per particle: count (n,), partner (n, 16) particle
+        indices, rest (n, 16) lengths; tag (n,) the AddParticle indices used
+        to order candidates with equal distances."""
+        n = len(count)
+        count = np.ascontiguousarray(count, np.int32)
+        partner = np.ascontiguousarray(partner, np.int32).reshape(n, self.SPRING_SLOTS)
+        rest = np.ascontiguousarray(rest, np.float32).reshape(n, self.SPRING_SLOTS)
+        tg = np.ascontiguousarray(tag, np.int64) if tag is not None else None
+        fn = self._lib.sph_oracle_set_spring_state
+        fn.argtypes = [_vp, _u64, _c.POINTER(_c.c_int32), _c.POINTER(_c.c_int32), _c.POINTER(_c.c_float),
+                       _c.POINTER(_c.c_int64)]
+        fn.restype = _i
+        rc = fn(self._h, n, _ptr(count, _c.c_int32), _ptr(partner, _c.c_int32), _ptr(rest, _c.c_float),
+                _ptr(tg, _c.c_int64))
+        if rc != 0:
+            raise ValueError("oracle set_spring_state: invalid spring state")
+
+    def get_spring_state(self):
+        n = self.particle_count()
+        count = np.zeros(n, np.int32)
+        partner = np.zeros((n, self.SPRING_SLOTS), np.int32)
+        rest = np.zeros((n, self.SPRING_SLOTS), np.float32)
+        fn = self._lib.sph_oracle_get_spring_state
+        fn.argtypes = [_vp, _c.POINTER(_c.c_int32), _c.POINTER(_c.c_int32), _c.POINTER(_c.c_float)]
+        fn.restype = None
+        fn(self._h, _ptr(count, _c.c_int32), _ptr(partner, _c.c_int32), _ptr(rest, _c.c_float))
+        return count, partner, rest
+
+    def spring_total(self) -> int:
+        fn = self._lib.sph_oracle_spring_total
+        fn.argtypes = [_vp]
+        fn.restype = _u64
+        return int(fn(self._h))
 

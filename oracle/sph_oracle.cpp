@@ -175,6 +175,11 @@ struct SimBase {
 	virtual void GetStats(uint64_t *counts, float *times) = 0;
 	virtual size_t Workers() = 0;
 	virtual void SetWorkers(size_t w) = 0;
+	virtual void SetSprings(int enabled, float yield, float plasticity, float stiffness, int maxPer) = 0;
+	virtual int SetSpringState(size_t n, const int32_t *count, const int32_t *partner, const float *rest,
+	                           const int64_t *tag) = 0;
+	virtual void GetSpringState(int32_t *count, int32_t *partner, float *rest) = 0;
+	virtual uint64_t SpringTotal() = 0;
 };
 
 template <typename T>
@@ -209,6 +214,19 @@ struct Sim : SimBase {
 	size_t workers = 1;
 	ChunkPool *pool = nullptr;
 
+	// Viscoelastic springs (not in the reference; Clavet et al. 2005,
+	// "Particle-based viscoelastic fluid simulation", Algorithms 3 and 4):
+	// up to kSprings per particle, stored at both ends, partner = particle
+	// index, rest length per spring; tag = AddParticle index (tie-break).
+	static constexpr int kSprings = 16;
+	int springsOn = 0, springMax = kSprings;
+	T springYield = 0, springPlastic = 0, springK = 0;
+	std::vector<int32_t> sN, sP, accN, accP;
+	std::vector<T> sL;
+	std::vector<int64_t> tag;
+	std::vector<V2<T>> springPos;
+	uint64_t springTotal = 0;
+
 	explicit Sim(const sph_oracle_domain &d) : dom(d) {
 		halfW = T(d.width * 0.5f);
 		halfH = T(d.height * 0.5f);
@@ -226,6 +244,7 @@ struct Sim : SimBase {
 		nb.resize(capN * capNb);
 		cellIdx.resize((size_t)gx * gy * capCell);
 		cellCnt.assign((size_t)gx * gy, 0);
+		tag.resize(capN);
 		float defaults[9];
 		sph_oracle_default_params(defaults);
 		SetParams(defaults);
@@ -335,6 +354,8 @@ struct Sim : SimBase {
 		q.density = q.nearDensity = q.pressure = q.nearPressure = 0;
 		nbCount[i] = 0;
 		inCell[i] = 0;
+		tag[i] = (int64_t)i;
+		if (springsOn) sN[i] = 0;
 		Insert(i);
 		return (int64_t)i;
 	}
@@ -641,6 +662,138 @@ struct Sim : SimBase {
 		return (float)std::chrono::duration_cast<std::chrono::nanoseconds>(d).count() * (1.0f / 1000000);
 	}
 
+	// Plasticity of one spring of rest length L at length r < h (Clavet
+	// 2005, Algorithm 4): outside the tolerable deformation d = yield * L the
+	// rest length moves towards r at rate alpha.
+	T Plastic(T L, T r, T dtAlpha) const {
+		const T d = springYield * L;
+		if (r > L + d) L = L + dtAlpha * ((r - L) - d);
+		else if (r < L - d) L = L - dtAlpha * ((L - d) - r);
+		return L;
+	}
+
+	// Springs, after the neighbour search and before density (Clavet 2005:
+	// adjust springs, then apply spring displacements).  Restated for a
+	// deterministic parallel form:
+	//  1. per particle: existing springs within h are adjusted, springs
+	//     whose rest length exceeds h are removed; the free slots go to the
+	//     nearest candidates (in-range list members without a spring),
+	//     ordered by (r^2, AddParticle index);
+	//  2. a spring is added where both ends chose each other; its rest
+	//     length starts at h and is adjusted like the others;
+	//  3. every particle moves by -D/2 of each of its springs, from the
+	//     positions before this phase (Jacobi), summed in slot order, with
+	//     D = dt^2 k_spring (1 - L/h) (L - r) r_hat.
+	void Springs(T dt) {
+		const T h2 = h * h;
+		const T dtAlpha = dt * springPlastic;
+		const T dt2 = dt * dt;
+		const int K = kSprings;
+		std::vector<int32_t> nN(n);
+		std::vector<int32_t> nP(n * K);
+		std::vector<T> nL(n * K);
+		// Chunks are inclusive ranges [s, e], as the reference's ThreadPool's.
+		ForEachChunk(n, [&](size_t s, size_t e) {
+			for (size_t i = s; i <= e; ++i) {
+				const V2<T> xi = parts[i].cur;
+				int m = 0;
+				for (int q = 0; q < sN[i]; ++q) {
+					const int p = sP[i * K + q];
+					T L = sL[i * K + q];
+					const V2<T> rij = sub(parts[p].cur, xi);
+					const T r2 = dot(rij, rij);
+					if (r2 < h2) L = Plastic(L, sqrt_t(r2), dtAlpha);
+					if (L <= h) {
+						nP[i * K + m] = p;
+						nL[i * K + m] = L;
+						++m;
+					}
+				}
+				nN[i] = m;
+				const int freeSlots = springMax - m;
+				T kr2[kSprings];
+				int64_t ktag[kSprings];
+				int kj[kSprings];
+				int cnt = 0;
+				for (size_t t = 0; t < nbCount[i] && freeSlots > 0; ++t) {
+					const size_t j = nb[i * capNb + t];
+					if (j == i) continue;
+					const V2<T> rij = sub(parts[j].cur, xi);
+					const T r2 = dot(rij, rij);
+					if (!(r2 < h2)) continue;
+					bool has = false;
+					for (int q = 0; q < sN[i]; ++q) has = has || (size_t)sP[i * K + q] == j;
+					if (has) continue;
+					const int64_t tj = tag[j];
+					if (cnt == freeSlots && !(r2 < kr2[cnt - 1] || (r2 == kr2[cnt - 1] && tj < ktag[cnt - 1])))
+						continue;
+					int at = cnt < freeSlots ? cnt++ : cnt - 1;
+					while (at > 0 && (r2 < kr2[at - 1] || (r2 == kr2[at - 1] && tj < ktag[at - 1]))) {
+						kr2[at] = kr2[at - 1];
+						ktag[at] = ktag[at - 1];
+						kj[at] = kj[at - 1];
+						--at;
+					}
+					kr2[at] = r2;
+					ktag[at] = tj;
+					kj[at] = (int)j;
+				}
+				accN[i] = cnt;
+				for (int q = 0; q < cnt; ++q) accP[i * K + q] = kj[q];
+			}
+		});
+		ForEachChunk(n, [&](size_t s, size_t e) {
+			for (size_t i = s; i <= e; ++i) {
+				const V2<T> xi = parts[i].cur;
+				int m = nN[i];
+				for (int q = 0; q < accN[i]; ++q) {
+					const int p = accP[i * K + q];
+					bool mutual = false;
+					for (int q2 = 0; q2 < accN[p]; ++q2) mutual = mutual || (size_t)accP[p * K + q2] == i;
+					if (!mutual) continue;
+					const V2<T> rij = sub(parts[p].cur, xi);
+					const T L = Plastic(h, sqrt_t(dot(rij, rij)), dtAlpha);
+					if (L <= h) {
+						nP[i * K + m] = p;
+						nL[i * K + m] = L;
+						++m;
+					}
+				}
+				nN[i] = m;
+			}
+		});
+		ForEachChunk(n, [&](size_t s, size_t e) {
+			for (size_t i = s; i <= e; ++i) {
+				const V2<T> xi = parts[i].cur;
+				V2<T> dx;
+				for (int q = 0; q < nN[i]; ++q) {
+					const int p = nP[i * K + q];
+					const T L = nL[i * K + q];
+					const V2<T> rij = sub(parts[p].cur, xi);
+					const T r = sqrt_t(dot(rij, rij));
+					const T len = r == T(0) ? T(1) : r;
+					const T inv = T(1) / len;
+					const T nx = rij.x * inv, ny = rij.y * inv;
+					const T f = ((dt2 * springK) * (T(1) - L * invH)) * (L - r);
+					dx.x = dx.x - (f * nx) * T(0.5f);
+					dx.y = dx.y - (f * ny) * T(0.5f);
+				}
+				springPos[i] = add(dx, xi);
+			}
+		});
+		uint64_t total = 0;
+		for (size_t i = 0; i < n; ++i) {
+			parts[i].cur = springPos[i];
+			sN[i] = nN[i];
+			for (int q = 0; q < nN[i]; ++q) {
+				sP[i * K + q] = nP[i * K + q];
+				sL[i * K + q] = nL[i * K + q];
+			}
+			total += (uint64_t)nN[i];
+		}
+		springTotal = total;
+	}
+
 	// demo4.cpp:286-451
 	int Update(float dtf) override {
 		error = 0;
@@ -692,6 +845,7 @@ struct Sim : SimBase {
 			statMinNb = std::min<uint64_t>(nbCount[i], statMinNb);
 			statMaxNb = std::max<uint64_t>(nbCount[i], statMaxNb);
 		}
+		if (springsOn) Springs(dt);
 		times[5] = Ms(t0);
 
 		t0 = clk::now();
@@ -818,6 +972,48 @@ struct Sim : SimBase {
 		counts[3] = statMaxCell;
 		for (int k = 0; k < 9; ++k) t[k] = times[k];
 	}
+	void SetSprings(int enabled, float yield, float plasticity, float stiffness, int maxPer) override {
+		springYield = yield;
+		springPlastic = plasticity;
+		springK = stiffness;
+		springMax = std::min(std::max(maxPer, 0), (int)kSprings);
+		if (enabled && !springsOn) {
+			sN.assign(capN, 0);
+			sP.assign(capN * kSprings, 0);
+			sL.assign(capN * kSprings, T(0));
+			accN.assign(capN, 0);
+			accP.assign(capN * kSprings, 0);
+			springPos.assign(capN, V2<T>());
+		}
+		springsOn = enabled ? 1 : 0;
+	}
+	int SetSpringState(size_t cnt, const int32_t *count, const int32_t *partner, const float *rest,
+	                   const int64_t *tags) override {
+		if (!springsOn || cnt != n) return SPH_ORACLE_ERR_CAPACITY;
+		for (size_t i = 0; i < cnt; ++i) {
+			if (count[i] < 0 || count[i] > kSprings) return SPH_ORACLE_ERR_CAPACITY;
+			sN[i] = count[i];
+			for (int q = 0; q < count[i]; ++q) {
+				const int32_t p = partner[i * kSprings + q];
+				if (p < 0 || (size_t)p >= cnt) return SPH_ORACLE_ERR_CAPACITY;
+				sP[i * kSprings + q] = p;
+				sL[i * kSprings + q] = (T)rest[i * kSprings + q];
+			}
+			if (tags) tag[i] = tags[i];
+		}
+		return 0;
+	}
+	void GetSpringState(int32_t *count, int32_t *partner, float *rest) override {
+		for (size_t i = 0; i < n; ++i) {
+			const int c = springsOn ? sN[i] : 0;
+			if (count) count[i] = c;
+			for (int q = 0; q < kSprings; ++q) {
+				if (partner) partner[i * kSprings + q] = q < c ? sP[i * kSprings + q] : -1;
+				if (rest) rest[i * kSprings + q] = q < c ? (float)sL[i * kSprings + q] : 0.0f;
+			}
+		}
+	}
+	uint64_t SpringTotal() override { return springTotal; }
 	size_t Workers() override { return workers; }
 	void SetWorkers(size_t w) override {
 		w = std::max<size_t>(1, w);
@@ -910,6 +1106,17 @@ int sph_oracle_set_state(void *p, uint64_t n, const double *pos, const double *p
 void sph_oracle_get_stats(void *p, uint64_t *counts, float *times) { B(p)->GetStats(counts, times); }
 void sph_oracle_set_workers(void *p, uint64_t w) { B(p)->SetWorkers(w); }
 uint64_t sph_oracle_workers(void *p) { return B(p)->Workers(); }
+void sph_oracle_set_springs(void *p, int enabled, float yield, float plasticity, float stiffness, int max_per) {
+	B(p)->SetSprings(enabled, yield, plasticity, stiffness, max_per);
+}
+int sph_oracle_set_spring_state(void *p, uint64_t n, const int32_t *count, const int32_t *partner, const float *rest,
+                                const int64_t *tag) {
+	return B(p)->SetSpringState(n, count, partner, rest, tag);
+}
+void sph_oracle_get_spring_state(void *p, int32_t *count, int32_t *partner, float *rest) {
+	B(p)->GetSpringState(count, partner, rest);
+}
+uint64_t sph_oracle_spring_total(void *p) { return B(p)->SpringTotal(); }
 uint64_t sph_oracle_hardware_threads(void) {
 	unsigned t = std::thread::hardware_concurrency();
 	return t ? t : 1;
