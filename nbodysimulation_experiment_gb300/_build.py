@@ -18,9 +18,18 @@ LIB_NAME = "libsph_gb300.so"
 LIB_PATH = os.path.join(PKG_DIR, LIB_NAME)
 BUILD_DIR = os.path.join(PKG_DIR, "_build")
 
-SOURCES = ["sph_kernels.cu", "sph_springs.cu", "sph_api.cu", "sph_noalloc.cu"]
+SOURCES = ["sph_kernels.cu", "sph_springs.cu", "sph_api.cu", "sph_noalloc.cu", "mpnn_gemm.cu", "mpnn.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off"]
+# The learned frame's kernels are checked against an FP64 reference within a
+# tolerance, not bit for bit: fused multiply-adds are allowed there.
+FMA_SOURCES = {"mpnn_gemm.cu", "mpnn.cu", "mpnn_kernels.cu"}
+
+
+def _flags(src: str) -> List[str]:
+    if src in FMA_SOURCES:
+        return [f for f in NVCC_FLAGS if f != "--fmad=false"]
+    return NVCC_FLAGS
 
 
 def nvcc() -> str:
@@ -35,7 +44,8 @@ def _deps() -> List[str]:
     for name in os.listdir(CSRC):
         if name.endswith((".cu", ".cuh", ".h")):
             out.append(os.path.join(CSRC, name))
-    out.append(os.path.join(os.path.dirname(PKG_DIR), "include", "sph_gb300.h"))
+    for h in ("sph_gb300.h", "sph_mpnn.h"):
+        out.append(os.path.join(os.path.dirname(PKG_DIR), "include", h))
     return out
 
 
@@ -57,7 +67,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     for src in SOURCES:
         obj = os.path.join(BUILD_DIR, src.replace(".cu", ".o"))
         objs.append(obj)
-        cmd = [cc] + ARCH + NVCC_FLAGS + ["-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [cc] + ARCH + _flags(src) + ["-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:
             print(" ".join(cmd), file=sys.stderr)
         procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))

@@ -1,0 +1,244 @@
+// BF16 tensor-core GEMM for the message-passing network (5th-generation
+// tensor cores: tcgen05.mma with the accumulator in tensor memory).
+//
+//   C[M x N] (+)= A[M x K] * B[N x K]^T      A, B bf16 row-major (K-major),
+//                                            FP32 accumulation in TMEM.
+//
+// One CTA of four warps computes a 128-row tile of C for all N <= 256
+// columns: operands are staged in shared memory in the canonical no-swizzle
+// K-major layout (8-row x 16-byte core matrices), thread 0 issues
+// tcgen05.mma (M=128, N, K=16) per 16-wide K step and commits to an
+// mbarrier; two stages let the next K chunk load while the tensor core works
+// on the current one.  The epilogue reads the accumulator with tcgen05.ld
+// (warp w owns TMEM lanes 32w..32w+31, one row per thread) and applies the
+// requested bias, row-scaled bias and ReLU before storing FP32 and/or BF16
+// (row-major or transposed).  Split-K over gridDim.y accumulates FP32 with
+// atomics.  Every mbarrier wait is bounded; a timeout sets an error flag and
+// the CTA still frees its tensor memory.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "mpnn_internal.cuh"
+
+namespace sphgb {
+
+namespace {
+
+constexpr int kGemmThreads = 128;
+constexpr int kTileM = 128;
+constexpr int kChunkK = 64;                  // K per stage
+constexpr int kCoreBytes = 128;              // 8 rows x 16 bytes
+constexpr int kLbo = kCoreBytes;             // K-adjacent core matrices
+constexpr int kSbo = kCoreBytes * (kChunkK / 8);  // 8-row groups: 1 KiB
+constexpr int kStageABytes = kTileM * kChunkK * 2;
+constexpr int kMaxN = 256;
+constexpr int kStageBBytes = kMaxN * kChunkK * 2;
+constexpr uint32_t kWaitPolls = 1u << 26;
+
+struct __align__(1024) GemmSmem {
+	unsigned char a[2][kStageABytes];
+	unsigned char b[2][kStageBBytes];
+	unsigned long long bar[2];  // MMA-done barrier per stage
+	unsigned long long done;    // all MMAs done
+	uint32_t tmem;
+	int fail;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+	return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Shared-memory matrix descriptor: start address, leading (K) and stride
+// (M/N) byte offsets of core matrices, descriptor version 1, no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+	uint64_t d = 0;
+	d |= (uint64_t)((addr >> 4) & 0x3fff);
+	d |= (uint64_t)((kLbo >> 4) & 0x3fff) << 16;
+	d |= (uint64_t)((kSbo >> 4) & 0x3fff) << 32;
+	d |= (uint64_t)1 << 46;
+	return d;
+}
+
+// Instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N and M.
+__device__ __forceinline__ uint32_t instr_desc(int n) {
+	return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kTileM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, uint32_t count) {
+	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+// Bounded wait for the phase with the given parity to complete.
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, uint32_t parity) {
+	const uint32_t addr = smem_u32(bar);
+	for (uint32_t i = 0; i < kWaitPolls; ++i) {
+		uint32_t ok;
+		asm volatile(
+		    "{\n\t.reg .pred p;\n\t"
+		    "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+		    "selp.u32 %0, 1, 0, p;\n\t}"
+		    : "=r"(ok)
+		    : "r"(addr), "r"(parity)
+		    : "memory");
+		if (ok) return true;
+	}
+	return false;
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc, bool acc) {
+	asm volatile(
+	    "{\n\t.reg .pred p;\n\t"
+	    "setp.ne.u32 p, %4, 0;\n\t"
+	    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+	    "l"(a), "l"(b), "r"(idesc), "r"((uint32_t)acc)
+	    : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(unsigned long long *bar) {
+	asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+	             : "memory");
+}
+
+// Stage rows [row0, row0+rows) x K [k0, k0+kc) of a row-major bf16 matrix
+// (leading dimension ld) into the core-matrix layout; rows past `valid` and
+// K past kc are zero.
+__device__ __forceinline__ void stage_tile(unsigned char *dst, const __nv_bfloat16 *src, int ld, int row0, int rows,
+                                           int valid, int k0, int kc) {
+	const int chunks = rows * (kChunkK / 8);
+	for (int q = threadIdx.x; q < chunks; q += kGemmThreads) {
+		const int r = q / (kChunkK / 8), c8 = q % (kChunkK / 8);
+		uint4 v = make_uint4(0, 0, 0, 0);
+		if (row0 + r < valid && c8 * 8 < kc)
+			v = *reinterpret_cast<const uint4 *>(src + (size_t)(row0 + r) * ld + k0 + c8 * 8);
+		*reinterpret_cast<uint4 *>(dst + (r / 8) * kSbo + c8 * kLbo + (r % 8) * 16) = v;
+	}
+}
+
+}  // namespace
+
+size_t gemm_smem_bytes() { return sizeof(GemmSmem) + 1024; }
+
+__global__ void __launch_bounds__(kGemmThreads, 1) k_gemm_bf16(GemmArgs g) {
+	extern __shared__ unsigned char smem_raw[];
+	GemmSmem &S = *reinterpret_cast<GemmSmem *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+	const int tid = threadIdx.x, warp = tid / 32, lane = tid & 31;
+	const int row0 = blockIdx.x * kTileM;
+	// K range of this split.
+	const int kPer = ((g.K + gridDim.y - 1) / gridDim.y + kChunkK - 1) / kChunkK * kChunkK;
+	const int kBegin = blockIdx.y * kPer;
+	const int kEnd = min(g.K, kBegin + kPer);
+	const int ncols = g.N <= 32 ? 32 : (g.N <= 64 ? 64 : (g.N <= 128 ? 128 : 256));
+
+	if (tid == 0) {
+		mbar_init(&S.bar[0], 1);
+		mbar_init(&S.bar[1], 1);
+		mbar_init(&S.done, 1);
+		S.fail = 0;
+		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+	}
+	if (warp == 0) {
+		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&S.tmem)),
+		             "r"(ncols)
+		             : "memory");
+		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+	__syncthreads();
+	asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+	const uint32_t tmem = S.tmem;
+	const uint32_t idesc = instr_desc(g.N);
+
+	const int nChunks = kEnd > kBegin ? (kEnd - kBegin + kChunkK - 1) / kChunkK : 0;
+	uint32_t phase[2] = {0, 0};
+	bool ok = true;
+	for (int c = 0; c < nChunks; ++c) {
+		const int st = c & 1;
+		if (c >= 2) {
+			// The MMAs that read this stage two chunks ago must be done.
+			ok = ok && mbar_wait(&S.bar[st], phase[st]);
+			phase[st] ^= 1;
+		}
+		const int k0 = kBegin + c * kChunkK;
+		const int kc = min(kChunkK, kEnd - k0);
+		stage_tile(S.a[st], g.A, g.lda, row0, kTileM, g.M, k0, kc);
+		stage_tile(S.b[st], g.B, g.ldb, 0, (g.N + 7) / 8 * 8, g.N, k0, kc);
+		asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+		__syncthreads();
+		if (tid == 0) {
+			asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+			const uint32_t a0 = smem_u32(S.a[st]), b0 = smem_u32(S.b[st]);
+			for (int s = 0; s < kc / 16; ++s) {
+				mma_bf16(tmem, smem_desc(a0 + s * 2 * kLbo), smem_desc(b0 + s * 2 * kLbo), idesc, c > 0 || s > 0);
+			}
+			mma_commit(&S.bar[st]);
+		}
+	}
+	if (tid == 0) mma_commit(&S.done);  // arrives when every MMA issued above is complete
+	ok = ok && mbar_wait(&S.done, 0);
+	if (!ok) atomicOr(&S.fail, 1);
+	asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+	__syncthreads();
+	const bool good = S.fail == 0;
+	if (!good && tid == 0) atomicOr(g.error, 1u);
+
+	// Epilogue: thread = row; 16 columns per tensor-memory load.
+	const int row = row0 + warp * 32 + lane;
+	for (int c0 = 0; c0 < g.N && good && nChunks > 0; c0 += 16) {
+		uint32_t v[16];
+		const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+		asm volatile(
+		    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+		    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+		      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+		    : "r"(taddr)
+		    : "memory");
+		asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+		if (row >= g.M) continue;
+#pragma unroll
+		for (int u = 0; u < 16; ++u) {
+			const int col = c0 + u;
+			if (col >= g.N) break;
+			float x = __uint_as_float(v[u]);
+			if (g.bias) x += g.bias[col];
+			if (g.rowScale) x += g.rowScale[row] * g.bias2[col];
+			if (g.relu) x = fmaxf(x, 0.0f);
+			if (g.C) {
+				float *dst = g.C + (size_t)row * g.ldc + col;
+				if (g.accumulate) atomicAdd(dst, x);
+				else *dst = x;
+			}
+			if (g.Cb) g.Cb[(size_t)row * g.ldcb + col] = __float2bfloat16_rn(x);
+			if (g.CbT) g.CbT[(size_t)col * g.ldcbT + row] = __float2bfloat16_rn(x);
+		}
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+	__syncthreads();
+	if (warp == 0) {
+		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
+	}
+}
+
+int gemm_check(const GemmArgs &g, int splits) {
+	if (g.M <= 0 || g.N <= 0 || g.K <= 0 || g.N > kMaxN || g.N % 16 != 0 || g.K % 16 != 0) return -1;
+	if (g.lda % 8 != 0 || g.ldb % 8 != 0 || splits < 1) return -1;
+	if ((reinterpret_cast<uintptr_t>(g.A) | reinterpret_cast<uintptr_t>(g.B)) & 15) return -1;
+	if (splits > 1 && !(g.C && g.accumulate)) return -1;
+	return 0;
+}
+
+cudaError_t gemm_launch(const GemmArgs &g, int splits, cudaStream_t stream) {
+	static bool attr = false;
+	if (!attr) {
+		cudaError_t e = cudaFuncSetAttribute(k_gemm_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                                     (int)gemm_smem_bytes());
+		if (e != cudaSuccess) return e;
+		attr = true;
+	}
+	dim3 grid((g.M + kTileM - 1) / kTileM, splits);
+	k_gemm_bf16<<<grid, kGemmThreads, gemm_smem_bytes(), stream>>>(g);
+	return cudaGetLastError();
+}
+
+}  // namespace sphgb
