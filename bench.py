@@ -262,6 +262,76 @@ def bench_block_1m(torch, pkg, scenes, device: int, steps: int, warmup: int, spr
     return out
 
 
+def bench_learned(torch, pkg, scenes, device: int, args):
+    """The learned frame on the 262,144-particle dam break with obstacles:
+    the network is trained on the GPU on plain frames of seeded 65,536-particle
+    obstacle scenes, then learned frames (one plain update over the frame plus
+    the network's correction, judged by the density deviation with a bound of
+    0.01 rest density) are timed against plain frames (four updates of dt/4,
+    the reference's kSPHSubsteps) on the same scene."""
+    from nbodysimulation_experiment_gb300 import learned
+    frame, sub = float(scenes.DT), learned.SUBSTEPS
+    scene = scenes.dam_break_262144()
+    model = pkg.Mpnn(scene.n, device=device, seed=7)
+    t0 = time.perf_counter()
+    ntrain = learned.collect(model, lambda k: scenes.obstacles_65536(seed=1000 + k), range(args.learned_scenes),
+                             args.learned_frames)
+    learned.collect(model, lambda k: scenes.obstacles_65536(seed=5000 + k), range(2), 4)
+    t_collect = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    losses = learned.train(model, args.learned_steps, indices=range(ntrain))
+    t_train = time.perf_counter() - t0
+    ev = learned.evaluate(model, range(ntrain, model.sample_count))
+    model.clear_samples()
+
+    def run(use_network: bool):
+        sim = pkg.Simulation(scene.domain(), device=device)
+        scene.apply(sim)
+        for _ in range(3):
+            sim.update(frame / sub)
+        stream = torch.cuda.ExternalStream(sim.stream())
+        ms, used, errs = [], 0, []
+        for f in range(args.learned_warmup + args.learned_eval_frames):
+            with torch.cuda.stream(stream):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            if use_network:
+                u, err = sim.learned_frame(model, frame, sub, bound=0.01)
+            else:
+                for _ in range(sub):
+                    sim.update(frame / sub)
+                u, err = False, 0.0
+            with torch.cuda.stream(stream):
+                e1.record(stream)
+            e1.synchronize()
+            if f >= args.learned_warmup:
+                ms.append(e0.elapsed_time(e1))
+                used += int(u)
+                errs.append(err)
+        if not use_network:  # density deviation of the plain result, as the judge measures it
+            errs = [sim.learned_frame(model, frame, sub, bound=-1.0)[1]]
+        sim.close()
+        return statistics.mean(ms), used, float(np.mean(errs))
+
+    ms_l, used, err_l = run(True)
+    ms_p, _, err_p = run(False)
+    n, nf = scene.n, args.learned_eval_frames
+    model.close()
+    return {"value": n / (ms_l / 1e3), "unit": "particle-frames/s",
+            "frame": "1/60 s = %d reference substeps" % sub,
+            "particle_steps_per_s": n * sub / (ms_l / 1e3),
+            "ms_per_frame": ms_l, "plain_ms_per_frame": ms_p, "speedup_vs_plain_frame": ms_p / ms_l,
+            "frames": nf, "accepted_frames": used, "density_error": err_l,
+            "density_error_plain_frame": err_p, "judge_bound": 0.01, "particles": n,
+            "workload": "dam_break_262144: 512x512 jittered block, 102.4 x 57.6 box, 4 walls + 8 circles + "
+                        "4 segments; 2-round MPNN (edge 6-128-128, node 130-128-2, BF16 tcgen05 GEMMs)",
+            "train": {"samples": ntrain, "scenes": args.learned_scenes, "frames_per_scene": args.learned_frames,
+                      "scene": "obstacles_65536 seeds 1000..", "steps": args.learned_steps,
+                      "collect_s": t_collect, "train_s": t_train, "final_loss": float(np.mean(losses[-50:])),
+                      "held_out_loss": ev["learned"], "held_out_loss_without_network": ev["without_network"]}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -274,6 +344,12 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--block-steps", type=int, default=10, help="timed updates of the 1M-particle block")
     ap.add_argument("--no-block", action="store_true")
+    ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--learned-scenes", type=int, default=100, help="seeded 65,536-particle training scenes")
+    ap.add_argument("--learned-frames", type=int, default=20, help="training frames captured per scene")
+    ap.add_argument("--learned-steps", type=int, default=1500, help="Adam steps")
+    ap.add_argument("--learned-eval-frames", type=int, default=20)
+    ap.add_argument("--learned-warmup", type=int, default=3)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
@@ -376,6 +452,10 @@ def main():
         block = {"plain": bench_block_1m(torch, pkg, scenes, local, args.block_steps, 3, False),
                  "springs": bench_block_1m(torch, pkg, scenes, local, args.block_steps, 3, True)}
 
+    learned_line = None
+    if not args.no_learned:
+        learned_line = bench_learned(torch, pkg, scenes, local, args)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         from oracle.oracle import OracleSim, build as build_oracle
@@ -403,6 +483,7 @@ def main():
             "cpu_baseline": cpu,
             "batched": batched,
             "block_1m": block,
+            "learned": learned_line,
             "clocks": clocks,
         }
         print(json.dumps(line), flush=True)

@@ -11,6 +11,7 @@ from ._build import build, LIB_PATH
 from .simulation import (
     BatchSimulation,
     Domain,
+    Mpnn,
     Params,
     SphError,
     Simulation,
@@ -22,6 +23,6 @@ from .simulation import (
 from . import scenes
 
 __all__ = [
-    "BatchSimulation", "Domain", "Params", "SphError", "Simulation", "Stats", "build", "default_params", "load_library",
+    "BatchSimulation", "Domain", "Mpnn", "Params", "SphError", "Simulation", "Stats", "build", "default_params", "load_library",
     "reference_domain", "scenes", "LIB_PATH",
 ]

@@ -18,7 +18,10 @@ LIB_NAME = "libsph_gb300.so"
 LIB_PATH = os.path.join(PKG_DIR, LIB_NAME)
 BUILD_DIR = os.path.join(PKG_DIR, "_build")
 
-SOURCES = ["sph_kernels.cu", "sph_springs.cu", "sph_api.cu", "sph_noalloc.cu", "mpnn_gemm.cu", "mpnn.cu"]
+SOURCES = [
+    "sph_kernels.cu", "sph_springs.cu", "sph_learned.cu", "sph_api.cu", "sph_noalloc.cu", "mpnn_gemm.cu",
+    "mpnn_kernels.cu", "mpnn.cu",
+]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off"]
 # The learned frame's kernels are checked against an FP64 reference within a

@@ -1,0 +1,460 @@
+// CUDA-core kernels of the message-passing network: the edge layer (built
+// on the fly from the cell grid, summed per particle), elementwise node
+// work, reductions, layout transposes and the optimizer.  The dense layers
+// are the tcgen05 GEMM (mpnn_gemm.cu).  Arithmetic follows the FP64
+// restatement in the oracle up to FP32/BF16 rounding.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "mpnn_internal.cuh"
+#include "sph_internal.cuh"
+
+namespace sphgb {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+struct EdgeWarp {
+	float2 pos[kMpnnStage];
+	float2 z[kMpnnStage];
+};
+
+// The 3x3 block of cells around cell c (y-major), as segments of the
+// cell-ordered particle numbering.
+struct Block {
+	int start[9], off[9];
+	int L, own;
+};
+
+__device__ __forceinline__ Block make_block(const MpnnGraph &G, int c) {
+	Block b;
+	const int cx = c % G.gx, cy = c / G.gx;
+	b.L = 0;
+	b.own = 0;
+#pragma unroll
+	for (int q = 0; q < 9; ++q) {
+		const int x = cx + q % 3 - 1, y = cy + q / 3 - 1;
+		int st = 0, nn = 0;
+		if (x >= 0 && x < G.gx && y >= 0 && y < G.gy) {
+			const int c2 = y * G.gx + x;
+			st = G.cellStart[c2];
+			nn = G.cellCount[c2];
+		}
+		b.start[q] = st;
+		b.off[q] = b.L;
+		if (q == 4) b.own = b.L;
+		b.L += nn;
+	}
+	return b;
+}
+
+__device__ __forceinline__ int block_number(const Block &b, int e) {
+	int src = b.start[0] + e;
+#pragma unroll
+	for (int q = 1; q < 9; ++q) src = (e >= b.off[q]) ? b.start[q] + (e - b.off[q]) : src;
+	return src;
+}
+
+__device__ __forceinline__ void stage_block(EdgeWarp &S, const Block &b, const MpnnGraph &G, const float2 *z,
+                                            int lane) {
+	for (int e = lane; e < b.L; e += kWarp) {
+		const int num = block_number(b, e);
+		S.pos[e] = G.pos[num];
+		S.z[e] = z[num];
+	}
+	__syncwarp();
+}
+
+// Edge features e_ij (see mpnn_internal.cuh).
+struct Feat {
+	float f[kEdgeIn];
+};
+
+__device__ __forceinline__ Feat features(float dx, float dy, float r, float2 zi, float2 zj, float invH) {
+	Feat e;
+	const float q = r * invH;
+	e.f[0] = dx * invH;
+	e.f[1] = dy * invH;
+	e.f[2] = q;
+	e.f[3] = zj.x - zi.x;
+	e.f[4] = zj.y - zi.y;
+	e.f[5] = (1.0f - q) * (1.0f - q);
+	return e;
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+	return v;
+}
+
+}  // namespace
+
+// Edge layer 1, summed per particle: one warp per cell stages the cell's 3x3
+// block; lane l owns hidden features l, l+32, l+64, l+96.
+__global__ void __launch_bounds__(kEdgeWarps * kWarp) k_mpnn_edge_fwd(MpnnGraph G, const float *W1, const float *b1,
+                                                                     const float2 *z, __nv_bfloat16 *Hb, float *degS,
+                                                                     int np, uint32_t *error) {
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	EdgeWarp &S = reinterpret_cast<EdgeWarp *>(smem_raw)[threadIdx.x / kWarp];
+	const int lane = threadIdx.x & (kWarp - 1);
+	float w[4][kEdgeIn], bias[4];
+#pragma unroll
+	for (int q = 0; q < 4; ++q) {
+		const int f = lane + 32 * q;
+#pragma unroll
+		for (int k = 0; k < kEdgeIn; ++k) w[q][k] = W1[f * kEdgeIn + k];
+		bias[q] = b1[f];
+	}
+	const float h2 = __fmul_rn(G.h, G.h);
+	const int ncell = G.gx * G.gy;
+	const int warpsTotal = gridDim.x * kEdgeWarps;
+	for (int c = blockIdx.x * kEdgeWarps + threadIdx.x / kWarp; c < ncell; c += warpsTotal) {
+		const int cnt = G.cellCount[c];
+		if (cnt == 0) continue;
+		const Block b = make_block(G, c);
+		const int st = G.cellStart[c];
+		if (b.L > kMpnnStage) {
+			if (lane == 0) atomicOr(error, 2u);
+			for (int jj = 0; jj < cnt; ++jj) {
+#pragma unroll
+				for (int q = 0; q < 4; ++q) Hb[(size_t)(st + jj) * kHidden + lane + 32 * q] = __float2bfloat16_rn(0.f);
+				if (lane == 0) degS[st + jj] = 0.f;
+			}
+			continue;
+		}
+		stage_block(S, b, G, z, lane);
+		for (int jj = 0; jj < cnt; ++jj) {
+			const int self = b.own + jj;
+			const float2 xi = S.pos[self], zi = S.z[self];
+			float acc[4] = {0.f, 0.f, 0.f, 0.f};
+			int deg = 0;
+			for (int e = 0; e < b.L; ++e) {
+				const float2 xj = S.pos[e];
+				const float dx = xj.x - xi.x, dy = xj.y - xi.y;
+				// Unfused, as the neighbour sets of the plain step are computed.
+				const float r2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+				if (!(r2 < h2) || e == self) continue;
+				const Feat fe = features(dx, dy, sqrtf(r2), zi, S.z[e], G.invH);
+#pragma unroll
+				for (int q = 0; q < 4; ++q) {
+					float a = bias[q];
+#pragma unroll
+					for (int k = 0; k < kEdgeIn; ++k) a += w[q][k] * fe.f[k];
+					acc[q] += fmaxf(a, 0.f);
+				}
+				++deg;
+			}
+			const int i = st + jj;
+#pragma unroll
+			for (int q = 0; q < 4; ++q) Hb[(size_t)i * kHidden + lane + 32 * q] = __float2bfloat16_rn(acc[q] * kAggScale);
+			if (lane == 0) degS[i] = (float)deg * kAggScale;
+		}
+		__syncwarp();
+	}
+	// Padding rows [n, np) are zero.
+	const int tail = (np - G.n) * kHidden;
+	for (int t = (blockIdx.x * blockDim.x + threadIdx.x); t < tail; t += gridDim.x * blockDim.x) {
+		Hb[(size_t)G.n * kHidden + t] = __float2bfloat16_rn(0.f);
+		if (t % kHidden == 0) degS[G.n + t / kHidden] = 0.f;
+	}
+}
+
+// Backward of the edge layer: dW1, db1 from every edge (i aggregates j),
+// and, if needDz, the node-state gradient through the z_j - z_i features
+// (scattered to j with atomics).
+__global__ void __launch_bounds__(kEdgeWarps * kWarp) k_mpnn_edge_bwd(MpnnGraph G, const float *W1, const float *b1,
+                                                                     const float2 *z, const float *dH, float2 *dzEdge,
+                                                                     float *gW1, float *gb1, int needDz,
+                                                                     uint32_t *error) {
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	EdgeWarp &S = reinterpret_cast<EdgeWarp *>(smem_raw)[threadIdx.x / kWarp];
+	const int lane = threadIdx.x & (kWarp - 1);
+	float w[4][kEdgeIn], bias[4];
+	float gw[4][kEdgeIn], gb[4];
+#pragma unroll
+	for (int q = 0; q < 4; ++q) {
+		const int f = lane + 32 * q;
+#pragma unroll
+		for (int k = 0; k < kEdgeIn; ++k) {
+			w[q][k] = W1[f * kEdgeIn + k];
+			gw[q][k] = 0.f;
+		}
+		bias[q] = b1[f];
+		gb[q] = 0.f;
+	}
+	const float h2 = __fmul_rn(G.h, G.h);
+	const int ncell = G.gx * G.gy;
+	const int warpsTotal = gridDim.x * kEdgeWarps;
+	for (int c = blockIdx.x * kEdgeWarps + threadIdx.x / kWarp; c < ncell; c += warpsTotal) {
+		const int cnt = G.cellCount[c];
+		if (cnt == 0) continue;
+		const Block b = make_block(G, c);
+		if (b.L > kMpnnStage) {
+			if (lane == 0) atomicOr(error, 2u);
+			continue;
+		}
+		stage_block(S, b, G, z, lane);
+		const int st = G.cellStart[c];
+		for (int jj = 0; jj < cnt; ++jj) {
+			const int self = b.own + jj;
+			const int i = st + jj;
+			const float2 xi = S.pos[self], zi = S.z[self];
+			float g[4];
+#pragma unroll
+			for (int q = 0; q < 4; ++q) g[q] = dH[(size_t)i * kHidden + lane + 32 * q] * kAggScale;
+			float dzx = 0.f, dzy = 0.f;
+			for (int e = 0; e < b.L; ++e) {
+				const float2 xj = S.pos[e];
+				const float dx = xj.x - xi.x, dy = xj.y - xi.y;
+				// Unfused, as the neighbour sets of the plain step are computed.
+				const float r2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+				if (!(r2 < h2) || e == self) continue;
+				const Feat fe = features(dx, dy, sqrtf(r2), zi, S.z[e], G.invH);
+				float d3 = 0.f, d4 = 0.f;
+#pragma unroll
+				for (int q = 0; q < 4; ++q) {
+					float a = bias[q];
+#pragma unroll
+					for (int k = 0; k < kEdgeIn; ++k) a += w[q][k] * fe.f[k];
+					const float da = a > 0.f ? g[q] : 0.f;
+#pragma unroll
+					for (int k = 0; k < kEdgeIn; ++k) gw[q][k] += da * fe.f[k];
+					gb[q] += da;
+					d3 += w[q][3] * da;
+					d4 += w[q][4] * da;
+				}
+				if (needDz) {
+					d3 = warp_sum(d3);
+					d4 = warp_sum(d4);
+					if (lane == 0) {
+						const int j = block_number(b, e);
+						atomicAdd(&dzEdge[j].x, d3);
+						atomicAdd(&dzEdge[j].y, d4);
+						dzx -= d3;
+						dzy -= d4;
+					}
+				}
+			}
+			if (needDz && lane == 0) {
+				atomicAdd(&dzEdge[i].x, dzx);
+				atomicAdd(&dzEdge[i].y, dzy);
+			}
+		}
+		__syncwarp();
+	}
+#pragma unroll
+	for (int q = 0; q < 4; ++q) {
+		const int f = lane + 32 * q;
+#pragma unroll
+		for (int k = 0; k < kEdgeIn; ++k)
+			if (gw[q][k] != 0.f) atomicAdd(&gW1[f * kEdgeIn + k], gw[q][k]);
+		if (gb[q] != 0.f) atomicAdd(&gb1[f], gb[q]);
+	}
+}
+
+// Node-MLP input columns 128..143: z, then zeros (row-major and, if given,
+// feature-major).
+__global__ void k_mpnn_x3_tail(const float2 *z, __nv_bfloat16 *X3b, __nv_bfloat16 *X3f, int np, int ldf) {
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= np) return;
+	const float2 zi = z[i];
+	for (int k = kHidden; k < kNodeInPad; ++k) {
+		const float v = k == kHidden ? zi.x : (k == kHidden + 1 ? zi.y : 0.f);
+		const __nv_bfloat16 b = __float2bfloat16_rn(v);
+		X3b[(size_t)i * kNodeInPad + k] = b;
+		if (X3f) X3f[(size_t)k * ldf + i] = b;
+	}
+}
+
+// z_out = z_in + W4 c + b4.
+__global__ void k_mpnn_node_out(const __nv_bfloat16 *cb, const float *W4, const float *b4, const float2 *zin,
+                                float2 *zout, int np) {
+	__shared__ float w[2 * kHidden];
+	for (int t = threadIdx.x; t < 2 * kHidden; t += blockDim.x) w[t] = W4[t];
+	__syncthreads();
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= np) return;
+	const uint4 *row = reinterpret_cast<const uint4 *>(cb + (size_t)i * kHidden);
+	float s0 = b4[0], s1 = b4[1];
+	for (int v = 0; v < kHidden / 8; ++v) {
+		const uint4 pk = row[v];
+		const __nv_bfloat16 *e = reinterpret_cast<const __nv_bfloat16 *>(&pk);
+#pragma unroll
+		for (int u = 0; u < 8; ++u) {
+			const float c = __bfloat162float(e[u]);
+			s0 += w[v * 8 + u] * c;
+			s1 += w[kHidden + v * 8 + u] * c;
+		}
+	}
+	const float2 z = zin[i];
+	zout[i] = make_float2(z.x + s0, z.y + s1);
+}
+
+// Loss sum_i |u_i - t_i|^2 (accumulated; the mean is taken on the host) and
+// its gradient 2 (u - t) / n on [0, n), zero on the padding.
+__global__ void k_mpnn_loss(const float2 *z2, const float2 *z0, const float2 *target, float2 *dz, int n, int np,
+                            float *loss) {
+	__shared__ float part[256];
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	float l = 0.f;
+	if (i < n) {
+		const float ux = z2[i].x - z0[i].x, uy = z2[i].y - z0[i].y;
+		const float ex = ux - target[i].x, ey = uy - target[i].y;
+		dz[i] = make_float2(2.f * ex / (float)n, 2.f * ey / (float)n);
+		l = ex * ex + ey * ey;
+	} else if (i < np) {
+		dz[i] = make_float2(0.f, 0.f);
+	}
+	part[threadIdx.x] = l;
+	__syncthreads();
+	for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+		if (threadIdx.x < o) part[threadIdx.x] += part[threadIdx.x + o];
+		__syncthreads();
+	}
+	if (threadIdx.x == 0 && part[0] != 0.f) atomicAdd(loss, part[0]);
+}
+
+// da3 = (W4^T dz) * [c > 0], one warp per particle.
+__global__ void k_mpnn_node_bwd(const float2 *dz, const float *W4, const __nv_bfloat16 *cb, __nv_bfloat16 *da3b,
+                                int np) {
+	const int i = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+	const int lane = threadIdx.x & (kWarp - 1);
+	if (i >= np) return;
+	const float2 g = dz[i];
+#pragma unroll
+	for (int q = 0; q < 4; ++q) {
+		const int f = lane + 32 * q;
+		const float dc = W4[f] * g.x + W4[kHidden + f] * g.y;
+		const float c = __bfloat162float(cb[(size_t)i * kHidden + f]);
+		da3b[(size_t)i * kHidden + f] = __float2bfloat16_rn(c > 0.f ? dc : 0.f);
+	}
+}
+
+// gW4[o][f] += sum_i dz_i[o] c_i[f]; block f (one per hidden feature); block
+// 0 also adds gb4 += sum_i dz_i.
+__global__ void k_mpnn_dw4(const float2 *dz, const __nv_bfloat16 *cf, int ldf, int n, float *gW4, float *gb4) {
+	__shared__ float p0[256], p1[256], q0[256], q1[256];
+	const int f = blockIdx.x;
+	float a0 = 0.f, a1 = 0.f, s0 = 0.f, s1 = 0.f;
+	for (int i = threadIdx.x; i < n; i += blockDim.x) {
+		const float2 g = dz[i];
+		const float c = __bfloat162float(cf[(size_t)f * ldf + i]);
+		a0 += g.x * c;
+		a1 += g.y * c;
+		s0 += g.x;
+		s1 += g.y;
+	}
+	p0[threadIdx.x] = a0;
+	p1[threadIdx.x] = a1;
+	q0[threadIdx.x] = s0;
+	q1[threadIdx.x] = s1;
+	__syncthreads();
+	for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+		if (threadIdx.x < o) {
+			p0[threadIdx.x] += p0[threadIdx.x + o];
+			p1[threadIdx.x] += p1[threadIdx.x + o];
+			q0[threadIdx.x] += q0[threadIdx.x + o];
+			q1[threadIdx.x] += q1[threadIdx.x + o];
+		}
+		__syncthreads();
+	}
+	if (threadIdx.x == 0) {
+		gW4[f] += p0[0];
+		gW4[kHidden + f] += p1[0];
+		if (f == 0) {
+			gb4[0] += q0[0];
+			gb4[1] += q1[0];
+		}
+	}
+}
+
+// out[r] += sum_{i<n} X[r][i] (* w[i]); one block per row.
+__global__ void k_mpnn_rowsum(const __nv_bfloat16 *X, int ld, int n, const float *w, float *out) {
+	__shared__ float part[256];
+	const int r = blockIdx.x;
+	float s = 0.f;
+	for (int i = threadIdx.x; i < n; i += blockDim.x) {
+		const float x = __bfloat162float(X[(size_t)r * ld + i]);
+		s += w ? x * w[i] : x;
+	}
+	part[threadIdx.x] = s;
+	__syncthreads();
+	for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+		if (threadIdx.x < o) part[threadIdx.x] += part[threadIdx.x + o];
+		__syncthreads();
+	}
+	if (threadIdx.x == 0) out[r] += part[0];
+}
+
+// dz_r = dz_{r+1} + (dX3 columns of z) + edge term, zero on the padding.
+__global__ void k_mpnn_combine(const float2 *dzNext, const float *dX, const float2 *dzEdge, float2 *dz, int n,
+                               int np) {
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= np) return;
+	if (i >= n) {
+		dz[i] = make_float2(0.f, 0.f);
+		return;
+	}
+	const float2 a = dzNext[i], e = dzEdge[i];
+	const float *row = dX + (size_t)i * kNodeInPad;
+	dz[i] = make_float2(a.x + row[kHidden] + e.x, a.y + row[kHidden + 1] + e.y);
+}
+
+// dst[c][r] = src[r][c] for a rows x cols bf16 matrix (32x32 tiles).
+__global__ void k_mpnn_transpose(const __nv_bfloat16 *src, int rows, int cols, int lds, __nv_bfloat16 *dst, int ldd) {
+	__shared__ __nv_bfloat16 tile[32][33];
+	const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+	for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+		const int r = r0 + y, c = c0 + threadIdx.x;
+		if (r < rows && c < cols) tile[y][threadIdx.x] = src[(size_t)r * lds + c];
+	}
+	__syncthreads();
+	for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+		const int c = c0 + y, r = r0 + threadIdx.x;
+		if (r < rows && c < cols) dst[(size_t)c * ldd + r] = tile[threadIdx.x][y];
+	}
+}
+
+// Adam (Kingma & Ba 2015) with optional gradient clipping by value.
+__global__ void k_mpnn_adam(float *p, const float *g, float *m, float *v, int count, float lr, float beta1,
+                            float beta2, float eps, float bc1, float bc2, float clip) {
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= count) return;
+	float gi = g[i];
+	if (clip > 0.f) gi = fminf(fmaxf(gi, -clip), clip);
+	const float mi = beta1 * m[i] + (1.f - beta1) * gi;
+	const float vi = beta2 * v[i] + (1.f - beta2) * gi * gi;
+	m[i] = mi;
+	v[i] = vi;
+	p[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+}
+
+// BF16 copies of the GEMM weights of round blockIdx.y: W2, W2^T, W3, W3^T.
+__global__ void k_mpnn_refresh(const float *p, __nv_bfloat16 *W2b, __nv_bfloat16 *W2Tb, __nv_bfloat16 *W3b,
+                               __nv_bfloat16 *W3Tb) {
+	const int r = blockIdx.y;
+	const float *P = p + (size_t)r * kRoundParams;
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t < kHidden * kHidden) {
+		const int a = t / kHidden, b = t % kHidden;
+		const __nv_bfloat16 x = __float2bfloat16_rn(P[kOffW2 + t]);
+		W2b[(size_t)r * kHidden * kHidden + t] = x;
+		W2Tb[(size_t)r * kHidden * kHidden + b * kHidden + a] = x;
+	}
+	if (t < kHidden * kNodeInPad) {
+		const int a = t / kNodeInPad, b = t % kNodeInPad;
+		const __nv_bfloat16 x = __float2bfloat16_rn(P[kOffW3 + t]);
+		W3b[(size_t)r * kHidden * kNodeInPad + t] = x;
+		W3Tb[(size_t)r * kHidden * kNodeInPad + b * kHidden + a] = x;
+	}
+}
+
+__global__ void k_mpnn_u(const float2 *z2, const float2 *z0, float2 *u, int n) {
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	u[i] = make_float2(z2[i].x - z0[i].x, z2[i].y - z0[i].y);
+}
+
+}  // namespace sphgb

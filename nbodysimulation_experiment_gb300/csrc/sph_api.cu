@@ -21,6 +21,8 @@
 #include <vector>
 
 #include "../../include/sph_gb300.h"
+#include "../../include/sph_mpnn.h"
+#include "mpnn_internal.cuh"
 #include "sph_internal.cuh"
 #include "sph_kernels.cuh"
 
@@ -123,6 +125,14 @@ struct sph_sim {
 	uint64_t graphKernels[2] = {0, 0};
 	int steadySteps = 0;  // updates since the scene table last changed
 	bool useGraphs = true;
+
+	// Learned frames: a snapshot of the canonical state (for the fallback and
+	// for sample capture), the network's input/output and judge scratch.
+	BufferSet snap;
+	int *snapCellStart = nullptr, *snapCellCount = nullptr;
+	float2 *lz0 = nullptr, *lu = nullptr, *lbyId = nullptr, *ldens = nullptr;
+	float *lerr = nullptr;
+	uint32_t *lstats = nullptr;
 
 	cudaEvent_t ev[kEvCount] = {};
 	bool timed = false;
@@ -857,7 +867,203 @@ int dump_scene(sph_sim *s, size_t scene, const sph_state_view *v) {
 	return SPH_OK;
 }
 
+// ---- Learned frames -------------------------------------------------------
+
+int ensure_learned(sph_sim *s) {
+	if (s->lz0) return SPH_OK;
+	const size_t N = (size_t)round_up128((int)s->capTotal), C = (size_t)s->ncellTotal;
+	int rc;
+	BufferSet &B = s->snap;
+	if ((rc = dalloc(&B.pos, N)) || (rc = dalloc(&B.prev, N)) || (rc = dalloc(&B.vel, N)) ||
+	    (rc = dalloc(&B.acc, N)) || (rc = dalloc(&B.dens, N)) || (rc = dalloc(&B.press, N)) ||
+	    (rc = dalloc(&B.id, N)) || (rc = dalloc(&B.cellOf, N)) || (rc = dalloc(&s->snapCellStart, C)) ||
+	    (rc = dalloc(&s->snapCellCount, C)) || (rc = dalloc(&s->lz0, N)) || (rc = dalloc(&s->lu, N)) ||
+	    (rc = dalloc(&s->lbyId, N)) || (rc = dalloc(&s->ldens, N)) || (rc = dalloc(&s->lerr, 1)) ||
+	    (rc = dalloc(&s->lstats, 4)))
+		return rc;
+	return SPH_OK;
+}
+
+// Copy the canonical state (particle arrays and cell ranges) to or from the
+// snapshot.
+int copy_state(sph_sim *s, bool save) {
+	BufferSet &A = s->buf[s->cur];
+	BufferSet &Z = s->snap;
+	const size_t n = s->totalParticles(), C = (size_t)s->ncellTotal;
+	cudaStream_t st = s->stream;
+	auto cp = [&](void *live, void *snap, size_t bytes) {
+		return cudaMemcpyAsync(save ? snap : live, save ? live : snap, bytes, cudaMemcpyDeviceToDevice, st);
+	};
+	const size_t f2 = n * sizeof(float2), i4 = n * sizeof(int);
+	if (n) {
+		SPH_CUDA(cp(A.pos, Z.pos, f2));
+		SPH_CUDA(cp(A.prev, Z.prev, f2));
+		SPH_CUDA(cp(A.vel, Z.vel, f2));
+		SPH_CUDA(cp(A.acc, Z.acc, f2));
+		SPH_CUDA(cp(A.dens, Z.dens, f2));
+		SPH_CUDA(cp(A.press, Z.press, f2));
+		SPH_CUDA(cp(A.id, Z.id, i4));
+		SPH_CUDA(cp(A.cellOf, Z.cellOf, i4));
+	}
+	SPH_CUDA(cp(s->cellStartA, s->snapCellStart, C * sizeof(int)));
+	SPH_CUDA(cp(s->cellCountA, s->snapCellCount, C * sizeof(int)));
+	return SPH_OK;
+}
+
+// Mean |rho - rho0| / rho0 of the canonical state's final positions (density
+// from the cell ranges, as the step computes it), on scratch arrays.
+int density_error(sph_sim *s, float *out) {
+	const Scene &sc = s->scenes[0];
+	int rc = upload_scenes(s, s->tableDt > 0.0f ? s->tableDt : 1.0f);
+	if (rc) return rc;
+	const Totals tt = totals(s);
+	SimTables T = tables(s);
+	T.newStart = s->cellStartA;
+	T.newCount = s->cellCountA;
+	T.stats = s->lstats;
+	Particles Q = s->buf[s->cur].view();
+	Q.dens = s->ldens;
+	Q.press = s->lbyId;
+	k_density<<<s->densBlocks, kDensWarps * kWarp, dens_smem_bytes(), s->stream>>>(tt, Q, T);
+	SPH_LAUNCHED(s);
+	SPH_CUDA(cudaMemsetAsync(s->lerr, 0, sizeof(float), s->stream));
+	k_density_error<<<blocks_for(tt.n, 256), 256, 0, s->stream>>>(tt.n, s->ldens, sc.params.rest_density, s->lerr);
+	SPH_LAUNCHED(s);
+	float sum = 0.0f;
+	SPH_CUDA(cudaMemcpyAsync(&sum, s->lerr, sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+	rc = check_device_errors(s);
+	if (rc) return rc;
+	*out = tt.n > 0 ? sum / ((float)tt.n * sc.params.rest_density) : 0.0f;
+	return SPH_OK;
+}
+
+int learned_checks(sph_sim *s, sph_mpnn *m, float dt, int substeps) {
+	Scene *sc = single(s);
+	if (!sc) return not_single(s);
+	if (!m || !(dt > 0.0f) || substeps < 1) return SPH_ERR_INVALID_ARGUMENT;
+	if (sc->springs.enabled) return SPH_ERR_NOT_SUPPORTED;
+	if (mpnn_device(m) != s->device) return SPH_ERR_INVALID_ARGUMENT;
+	SPH_CUDA(cudaSetDevice(s->device));
+	int rc = flush_adds(s);
+	if (rc) return rc;
+	if ((size_t)round_up128((int)sc->n) > mpnn_capacity(m)) return SPH_ERR_CAPACITY;
+	return ensure_learned(s);
+}
+
+int plain_frame(sph_sim *s, float dt, int substeps) {
+	for (int k = 0; k < substeps; ++k) {
+		int rc = run_step(s, dt / (float)substeps);
+		if (rc) return rc;
+	}
+	return SPH_OK;
+}
+
+// The network's graph on the canonical state after an update: positions,
+// z0 = v dt / h (written to s->lz0 by the caller) and the cell ranges.
+MpnnGraph learned_graph(sph_sim *s, const Scene &sc) {
+	MpnnGraph g;
+	g.pos = s->buf[s->cur].pos;
+	g.z0 = s->lz0;
+	g.cellStart = s->cellStartA;
+	g.cellCount = s->cellCountA;
+	g.n = (int)sc.n;
+	g.gx = sc.gx;
+	g.gy = sc.gy;
+	g.h = sc.params.kernel_height;
+	g.invH = sc.params.inv_kernel_height;
+	return g;
+}
+
+int learned_z0(sph_sim *s, const Scene &sc) {
+	const int n = (int)sc.n, np = round_up128(n);
+	const BufferSet &A = s->buf[s->cur];
+	k_learned_z0<<<blocks_for(np, kElemThreads), kElemThreads, 0, s->stream>>>(n, np, A.pos, A.prev,
+	                                                                            sc.params.inv_kernel_height, s->lz0);
+	SPH_LAUNCHED(s);
+	return SPH_OK;
+}
+
 }  // namespace
+
+extern "C" {
+
+int sph_learned_frame(sph_sim *s, sph_mpnn *m, float dt, int substeps, float bound, int *used_learned,
+                      float *density_err) {
+	int rc = learned_checks(s, m, dt, substeps);
+	if (rc) return rc;
+	Scene &sc = s->scenes[0];
+	int used = 0;
+	float err = 0.0f;
+	if (sc.n == 0) {
+		rc = SPH_OK;
+	} else if (sc.n0 != sc.nDev) {
+		// Particles added since the last update: the frame runs plainly.
+		rc = plain_frame(s, dt, substeps);
+		if (!rc) rc = density_error(s, &err);
+	} else {
+		// One plain update over the whole frame, corrected by the network
+		// towards the `substeps` updates it stands in for.
+		rc = copy_state(s, true);
+		if (!rc) rc = run_step(s, dt);
+		float err1 = 0.0f;
+		if (!rc) rc = density_error(s, &err1);
+		if (!rc) rc = learned_z0(s, sc);
+		if (!rc) rc = mpnn_forward_dev(m, learned_graph(s, sc), s->lu, s->stream);
+		if (rc) return rc;
+		const Totals tt = totals(s);
+		k_learned_finish<<<blocks_for(tt.n, kCollideThreads), kCollideThreads, 0, s->stream>>>(
+		    tt, s->buf[s->cur].view(), s->lu, tables(s));
+		SPH_LAUNCHED(s);
+		rc = density_error(s, &err);
+		if (rc) return rc;
+		// The judge: the correction stands if it leaves the mean density
+		// deviation of the plain update it corrects at most `bound` (a
+		// fraction of the rest density) higher.
+		if (std::isfinite(err) && err <= err1 + bound) {
+			used = 1;
+		} else {
+			rc = copy_state(s, false);
+			if (!rc) rc = plain_frame(s, dt, substeps);
+			if (!rc) rc = density_error(s, &err);
+			if (rc) return rc;
+		}
+	}
+	if (used_learned) *used_learned = used;
+	if (density_err) *density_err = err;
+	return rc ? rc : check_device_errors(s);
+}
+
+int sph_mpnn_capture(sph_sim *s, sph_mpnn *m, float dt, int substeps) {
+	int rc = learned_checks(s, m, dt, substeps);
+	if (rc) return rc;
+	Scene &sc = s->scenes[0];
+	if (sc.n == 0 || sc.n0 != sc.nDev) return SPH_ERR_NOT_SUPPORTED;  // needs a canonical state: update first
+	const int n = (int)sc.n;
+	// Inputs: the state after one plain update over the whole frame.
+	rc = copy_state(s, true);
+	if (!rc) rc = run_step(s, dt);
+	if (!rc) rc = learned_z0(s, sc);
+	if (rc) return rc;
+	float2 *x1 = nullptr, *target = nullptr;
+	int *ids = nullptr;
+	rc = mpnn_add_sample(m, learned_graph(s, sc), s->stream, &x1, &target, &ids);
+	if (rc) return rc;
+	SPH_CUDA(cudaMemcpyAsync(ids, s->buf[s->cur].id, sizeof(int) * n, cudaMemcpyDeviceToDevice, s->stream));
+	// Target: where `substeps` plain updates of dt / substeps take each
+	// particle, relative to x1, in units of h.
+	rc = copy_state(s, false);
+	if (!rc) rc = plain_frame(s, dt, substeps);
+	if (rc) return rc;
+	const BufferSet &F = s->buf[s->cur];
+	k_scatter_by_id<<<blocks_for(n, kElemThreads), kElemThreads, 0, s->stream>>>(n, F.pos, F.id, s->lbyId);
+	SPH_LAUNCHED(s);
+	k_learned_target<<<blocks_for(n, kElemThreads), kElemThreads, 0, s->stream>>>(
+	    n, s->lbyId, ids, x1, sc.params.inv_kernel_height, target);
+	SPH_LAUNCHED(s);
+	return check_device_errors(s);
+}
+
+}  // extern "C"
 
 extern "C" {
 
@@ -994,7 +1200,10 @@ int sph_destroy(sph_sim *s) {
 	                T.enterCount,  T.leaveCount,  T.enterOffset, T.enterCursor, T.enterList,   T.moverCount,
 	                T.bbox,        T.newIdx,      T.newLabel,    T.taskCounter, T.stats,       T.error,
 	                T.abort,       T.bodies,      s->doneV,      s->doneD,      s->stagePos,   s->stageForce,
-	                s->prof,       T.accN,        T.accP,        T.springPos,   T.springTotal};
+	                s->prof,       T.accN,        T.accP,        T.springPos,   T.springTotal,
+	                s->snap.pos,   s->snap.prev,  s->snap.vel,   s->snap.acc,   s->snap.dens,  s->snap.press,
+	                s->snap.id,    s->snap.cellOf, s->snapCellStart, s->snapCellCount, s->lz0, s->lu,
+	                s->lbyId,      s->ldens,      s->lerr,       s->lstats};
 	for (void *p : ptrs)
 		if (p) cudaFree(p);
 	if (s->hostPos) cudaFreeHost(s->hostPos);

@@ -1239,6 +1239,33 @@ __global__ void __launch_bounds__(kCollideThreads) k_collide(Totals tt, Particle
 }
 
 // ---------------------------------------------------------------------------
+// Learned correction of a finished update: x += h u, bodies as in the
+// collision stage, velocity from the previous position (canonical numbering).
+__global__ void __launch_bounds__(kCollideThreads) k_learned_finish(Totals tt, Particles P, const float2 *u,
+                                                                   SimTables T) {
+	const int j = blockIdx.x * blockDim.x + threadIdx.x;
+	if (j >= tt.n) return;
+	const SceneDev &sc = T.scenes[T.sceneOf[j]];
+	const StepParams &s = sc.p;
+	const float2 d = u[j];
+	float2 x = P.pos[j];
+	x = make_float2(x.x + s.h * d.x, x.y + s.h * d.y);
+	for (int b = 0; b < s.nbodies; ++b) {
+		const Body &bd = T.bodies[sc.bodyBase + b];
+		switch (bd.type) {
+			case kBodyPlane: solve_plane(x, bd, s); break;
+			case kBodyCircle: solve_circle(x, bd, s); break;
+			case kBodySegment: solve_segment(x, bd, s); break;
+			case kBodyPolygon: solve_polygon(x, bd, s); break;
+			default: break;
+		}
+	}
+	const float2 pv = P.prev[j];
+	P.pos[j] = x;
+	P.vel[j] = make_float2((x.x - pv.x) * s.invDt, (x.y - pv.y) * s.invDt);
+}
+
+// ---------------------------------------------------------------------------
 // AddParticle (demo4.cpp:142-153) for a batch of numbers [first, first+count)
 // of scene `scene`: the new particles join the appendix of their cell.
 __global__ void k_add(int first, int count, int scene, int firstId, const float2 *pos, const float2 *force,

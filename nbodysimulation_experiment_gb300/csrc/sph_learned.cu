@@ -1,0 +1,55 @@
+// Kernels of the learned frame and of training-sample capture: the
+// network's node state, the density-error judge and the plain-method
+// targets.
+#include <cuda_runtime.h>
+
+#include "sph_internal.cuh"
+#include "sph_kernels.cuh"
+
+namespace sphgb {
+
+// z0 = (x - x_prev) / h = v dt / h of the state after an update; zero on the
+// padding [n, np).
+__global__ void k_learned_z0(int n, int np, const float2 *pos, const float2 *prev, float invH, float2 *z0) {
+	const int j = blockIdx.x * blockDim.x + threadIdx.x;
+	if (j >= np) return;
+	if (j >= n) {
+		z0[j] = make_float2(0.f, 0.f);
+		return;
+	}
+	const float2 x = pos[j], p = prev[j];
+	z0[j] = make_float2((x.x - p.x) * invH, (x.y - p.y) * invH);
+}
+
+// sum_i |rho_i - rho0| (the host divides by n rho0).
+__global__ void k_density_error(int n, const float2 *dens, float rho0, float *out) {
+	__shared__ float part[256];
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	part[threadIdx.x] = i < n ? fabsf(dens[i].x - rho0) : 0.f;
+	__syncthreads();
+	for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+		if (threadIdx.x < o) part[threadIdx.x] += part[threadIdx.x + o];
+		__syncthreads();
+	}
+	if (threadIdx.x == 0) atomicAdd(out, part[0]);
+}
+
+// byId[id[k]] = pos[k].
+__global__ void k_scatter_by_id(int n, const float2 *pos, const int *id, float2 *byId) {
+	const int k = blockIdx.x * blockDim.x + threadIdx.x;
+	if (k >= n) return;
+	const int i = id[k];
+	if (i >= 0 && i < n) byId[i] = pos[k];
+}
+
+// target[j] = (x_final(id_j) - x*_j) / h.
+__global__ void k_learned_target(int n, const float2 *byId, const int *ids, const float2 *xstar, float invH,
+                                 float2 *target) {
+	const int j = blockIdx.x * blockDim.x + threadIdx.x;
+	if (j >= n) return;
+	const int i = ids[j];
+	const float2 xf = (i >= 0 && i < n) ? byId[i] : xstar[j];
+	target[j] = make_float2((xf.x - xstar[j].x) * invH, (xf.y - xstar[j].y) * invH);
+}
+
+}  // namespace sphgb

@@ -16,6 +16,8 @@ Scenes:
   four walls, 8 seeded circles with radii in [2h, 6h] and 4 seeded line
   segments, all outside the block.
 * ``block_1m``         -- 1024x1024 jittered block in a 204.8 x 115.2 box.
+* ``dam_break_262144`` -- 512x512 block in a 102.4 x 57.6 box with 8 circles
+  and 4 segments (the learned frame's workload).
 * ``batch_scenes``     -- 512 independent boxes with log-uniform particle
   counts in [1,024, 65,536], each a jittered block plus 0-4 circles.
 """
@@ -186,6 +188,12 @@ def obstacles_65536(seed: int = 1234) -> Scene:
     return _block_scene("obstacles_65536", 256, 51.2, 28.8, 8, 4, seed)
 
 
+def dam_break_262144(seed: int = 1234) -> Scene:
+    """512x512 jittered block (262,144 particles) at the lower left of a
+    102.4 x 57.6 box with four walls, 8 seeded circles and 4 segments."""
+    return _block_scene("dam_break_262144", 512, 102.4, 57.6, 8, 4, seed)
+
+
 def block_1m(seed: int = 1234) -> Scene:
     return _block_scene("block_1m", 1024, 204.8, 115.2, 0, 0, seed)
 
@@ -224,4 +232,5 @@ SCENES = {
     "dam_break_4096": dam_break_4096,
     "obstacles_65536": obstacles_65536,
     "block_1m": block_1m,
+    "dam_break_262144": dam_break_262144,
 }

@@ -193,6 +193,20 @@ def load_library(build_if_missing: bool = True):
         "sph_get_spring_count": [vp, P(_c.c_uint64)],
         "sph_dump_springs": [vp, _c.c_size_t, vp, vp, vp],
         "sph_load_springs": [vp, _c.c_size_t, vp, vp, vp],
+        "sph_mpnn_create": [_c.c_int, _c.c_size_t, _c.c_uint64, P(vp)],
+        "sph_mpnn_destroy": [vp],
+        "sph_mpnn_param_count": [P(_c.c_size_t)],
+        "sph_mpnn_get_params": [vp, vp],
+        "sph_mpnn_set_params": [vp, vp],
+        "sph_mpnn_capture": [vp, vp, _c.c_float, _c.c_int],
+        "sph_mpnn_sample_count": [vp, P(_c.c_size_t)],
+        "sph_mpnn_clear_samples": [vp],
+        "sph_mpnn_sample_info": [vp, _c.c_size_t, P(_c.c_size_t), P(_c.c_int), P(_c.c_int), P(_c.c_float)],
+        "sph_mpnn_read_sample": [vp, _c.c_size_t, vp, vp, vp, vp, vp],
+        "sph_mpnn_eval": [vp, _c.c_size_t, P(_c.c_float), vp],
+        "sph_mpnn_gradient": [vp, _c.c_size_t, P(_c.c_float), vp],
+        "sph_mpnn_train_step": [vp, _c.c_size_t, _c.c_float, P(_c.c_float)],
+        "sph_learned_frame": [vp, vp, _c.c_float, _c.c_int, _c.c_float, P(_c.c_int), P(_c.c_float)],
         "sph_batch_create": [vp, _c.c_size_t, _c.c_int, P(vp)],
         "sph_batch_scene_count": [vp, P(_c.c_size_t)],
         "sph_batch_read_particles": [vp, _c.c_size_t, _c.c_size_t, vp, vp, vp, vp],
@@ -224,6 +238,9 @@ C_SYMBOLS = (
     "sph_get_worker_thread_count", "sph_read_particles", "sph_state_info", "sph_dump_state", "sph_load_state",
     "sph_get_stream", "sph_device_arrays", "sph_synchronize", "sph_kernel_launches",
     "sph_use_graphs", "sph_set_springs", "sph_get_spring_count", "sph_dump_springs", "sph_load_springs",
+    "sph_mpnn_create", "sph_mpnn_destroy", "sph_mpnn_param_count", "sph_mpnn_get_params", "sph_mpnn_set_params",
+    "sph_mpnn_capture", "sph_mpnn_sample_count", "sph_mpnn_clear_samples", "sph_mpnn_sample_info",
+    "sph_mpnn_read_sample", "sph_mpnn_eval", "sph_mpnn_gradient", "sph_mpnn_train_step", "sph_learned_frame",
     "sph_batch_create", "sph_batch_scene_count", "sph_batch_read_particles", "sph_batch_get_stats",
     "sph_batch_state_info", "sph_batch_dump_state",
 )
@@ -468,6 +485,15 @@ class Simulation:
         self._call("sph_dump_springs", n, count.ctypes.data, partner.ctypes.data, rest.ctypes.data)
         return count, partner, rest
 
+    def learned_frame(self, model: "Mpnn", frame_dt: float, substeps: int = 4, bound: float = 0.01):
+        """One frame by the network, judged by the plain method (see
+        ``sph_learned_frame``); returns (learned frame used, density error)."""
+        used = _c.c_int()
+        err = _c.c_float()
+        self._call("sph_learned_frame", model._h, float(np.float32(frame_dt)), int(substeps), float(bound),
+                   _c.byref(used), _c.byref(err))
+        return bool(used.value), float(err.value)
+
     def load_springs(self, count, partner, rest):
         n = len(count)
         count = np.ascontiguousarray(count, np.int32)
@@ -604,3 +630,98 @@ class BatchSimulation:
     def use_graphs(self, enable: bool = True):
         """Replay repeated updates from a per-step CUDA graph (default on)."""
         self._call("sph_use_graphs", 1 if enable else 0)
+
+
+class Mpnn:
+    """The learned frame's message-passing network (``include/sph_mpnn.h``):
+    parameters, training samples captured from plain frames, and training on
+    the GPU by the library's own forward and backward kernels."""
+
+    def __init__(self, max_particles: int, device: int = 0, seed: int = 1):
+        self._lib = load_library()
+        h = _c.c_void_p()
+        _check(self._lib.sph_mpnn_create(int(device), int(max_particles), int(seed), _c.byref(h)), "sph_mpnn_create")
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.sph_mpnn_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _call(self, name: str, *args) -> None:
+        _check(getattr(self._lib, name)(self._h, *args), name)
+
+    @staticmethod
+    def param_count() -> int:
+        out = _c.c_size_t()
+        _check(load_library().sph_mpnn_param_count(_c.byref(out)), "sph_mpnn_param_count")
+        return out.value
+
+    def get_params(self) -> np.ndarray:
+        p = np.zeros(self.param_count(), np.float32)
+        self._call("sph_mpnn_get_params", p.ctypes.data)
+        return p
+
+    def set_params(self, p) -> None:
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == self.param_count()
+        self._call("sph_mpnn_set_params", p.ctypes.data)
+
+    def capture(self, sim: Simulation, frame_dt: float, substeps: int = 4) -> None:
+        _check(self._lib.sph_mpnn_capture(sim._h, self._h, float(np.float32(frame_dt)), int(substeps)),
+               "sph_mpnn_capture")
+
+    @property
+    def sample_count(self) -> int:
+        out = _c.c_size_t()
+        self._call("sph_mpnn_sample_count", _c.byref(out))
+        return out.value
+
+    def clear_samples(self) -> None:
+        self._call("sph_mpnn_clear_samples")
+
+    def sample(self, index: int) -> Dict[str, np.ndarray]:
+        n, gx, gy, h = _c.c_size_t(), _c.c_int(), _c.c_int(), _c.c_float()
+        self._call("sph_mpnn_sample_info", int(index), _c.byref(n), _c.byref(gx), _c.byref(gy), _c.byref(h))
+        n = n.value
+        out = {k: np.zeros((n, 2), np.float32) for k in ("pos", "z0", "target")}
+        out["cell_start"] = np.zeros(gx.value * gy.value, np.int32)
+        out["cell_count"] = np.zeros(gx.value * gy.value, np.int32)
+        self._call("sph_mpnn_read_sample", int(index), out["pos"].ctypes.data, out["z0"].ctypes.data,
+                   out["target"].ctypes.data, out["cell_start"].ctypes.data, out["cell_count"].ctypes.data)
+        out["grid"] = (gx.value, gy.value)
+        out["h"] = h.value
+        return out
+
+    def eval(self, index: int, want_u: bool = False):
+        loss = _c.c_float()
+        u = None
+        if want_u:
+            n = _c.c_size_t()
+            self._call("sph_mpnn_sample_info", int(index), _c.byref(n), None, None, None)
+            u = np.zeros((n.value, 2), np.float32)
+        self._call("sph_mpnn_eval", int(index), _c.byref(loss), u.ctypes.data if u is not None else None)
+        return (loss.value, u) if want_u else loss.value
+
+    def gradient(self, index: int):
+        loss = _c.c_float()
+        g = np.zeros(self.param_count(), np.float32)
+        self._call("sph_mpnn_gradient", int(index), _c.byref(loss), g.ctypes.data)
+        return loss.value, g
+
+    def train_step(self, index: int, lr: float) -> float:
+        loss = _c.c_float()
+        self._call("sph_mpnn_train_step", int(index), float(lr), _c.byref(loss))
+        return loss.value

@@ -1,0 +1,127 @@
+"""The learned frame on the GPU: its network against the FP64 oracle
+(forward and every parameter gradient), training on samples of plain
+frames, the judge and fallback, and what a trained network gains.
+
+Samples come from the plain method: from a canonical state, one plain
+update over the whole frame (dt = 1/60) gives the inputs x1 and
+z0 = (x1 - x_prev) / h, and the target is (x4 - x1) / h with x4 the
+positions after the reference's four substeps of dt/4.  The method without
+the network is that single update (u = 0).
+"""
+import numpy as np
+import pytest
+
+import nbodysimulation_experiment_gb300 as pkg
+from nbodysimulation_experiment_gb300 import learned, scenes
+from oracle import mpnn_ref
+
+pytestmark = pytest.mark.gpu
+
+FRAME = float(scenes.DT)
+SUBSTEPS = 4
+GRAD_TOL = 2e-2   # relative norm per parameter block (BF16 activations and weights)
+FWD_TOL = 1e-2
+
+
+def _sim(scene, warm=3):
+    sim = pkg.Simulation(scene.domain())
+    scene.apply(sim)
+    for _ in range(warm):
+        sim.update(FRAME / SUBSTEPS)
+    return sim
+
+
+def _oracle_case(sample):
+    gx, gy = sample["grid"]
+    start, count = sample["cell_start"], sample["cell_count"]
+    n = len(sample["pos"])
+    cell_of = np.zeros(n, np.int64)
+    for c in np.nonzero(count)[0]:
+        cell_of[start[c]:start[c] + count[c]] = c
+    I, J = mpnn_ref.edges(sample["pos"], start, count, gx, gy, sample["h"], cell_of)
+    return I, J
+
+
+def test_forward_and_gradients_match_oracle():
+    scene = scenes.scaled_block(20, seed=3)
+    sim = _sim(scene)
+    model = pkg.Mpnn(4096, seed=11)
+    p = model.get_params()
+    # Nonzero biases so that every parameter block is exercised.
+    p = p + np.random.default_rng(0).normal(0, 0.02, p.shape).astype(np.float32)
+    model.set_params(p)
+    model.capture(sim, FRAME, SUBSTEPS)
+    s = model.sample(0)
+    I, J = _oracle_case(s)
+    flat = model.get_params().astype(np.float64)
+    u_ref, cache = mpnn_ref.forward(flat, s["pos"], s["z0"], I, J, s["h"], emulate_bf16=True)
+    g_ref = mpnn_ref.backward(flat, cache, u_ref, s["target"].astype(np.float64), emulate_bf16=True)
+    loss_gpu, u_gpu = model.eval(0, want_u=True)
+    err_u = np.linalg.norm(u_gpu - u_ref) / np.linalg.norm(u_ref)
+    assert err_u < FWD_TOL, err_u
+    assert abs(loss_gpu - mpnn_ref.loss(u_ref, s["target"])) <= 1e-2 * loss_gpu
+    loss2, g_gpu = model.gradient(0)
+    assert abs(loss2 - loss_gpu) <= 1e-6 * max(loss_gpu, 1e-12)
+    for rd, (gg, gr) in enumerate(zip(mpnn_ref.unpack(g_gpu.astype(np.float64)), mpnn_ref.unpack(g_ref))):
+        for name in gr:
+            num = np.linalg.norm(gg[name] - gr[name])
+            den = np.linalg.norm(gr[name])
+            assert den > 0, (rd, name)
+            assert num / den < GRAD_TOL, (rd, name, num / den)
+    model.close()
+    sim.close()
+
+
+def _samples(model, scene, frames, warm=3):
+    sim = _sim(scene, warm)
+    for _ in range(frames):
+        model.capture(sim, FRAME, SUBSTEPS)
+    sim.close()
+
+
+def test_training_reduces_the_loss():
+    model = pkg.Mpnn(8192, seed=2)
+    _samples(model, scenes.dam_break_4096(seed=1), 6)
+    before = np.mean([model.eval(k) for k in range(model.sample_count)])
+    for it in range(240):
+        model.train_step(it % model.sample_count, 1e-3)
+    after = np.mean([model.eval(k) for k in range(model.sample_count)])
+    assert after < 0.5 * before, (before, after)
+    model.close()
+
+
+def test_judge_falls_back_to_the_plain_frame():
+    scene = scenes.scaled_block(24, seed=5)
+    model = pkg.Mpnn(4096, seed=3)
+    a, b = _sim(scene), _sim(scene)
+    for _ in range(3):
+        used, err = a.learned_frame(model, FRAME, SUBSTEPS, bound=-1.0)  # nothing passes
+        assert not used and np.isfinite(err)
+        for _ in range(SUBSTEPS):
+            b.update(FRAME / SUBSTEPS)
+    sa, sb = a.dump_state(), b.dump_state()
+    for k in ("pos", "prev", "vel", "dens", "press", "id", "cell_start", "cell_count"):
+        assert np.array_equal(sa[k], sb[k]), k
+    used, err = a.learned_frame(model, FRAME, SUBSTEPS, bound=1e9)  # everything passes
+    assert used and np.isfinite(err)
+    st = a.dump_state()
+    assert np.all(np.isfinite(st["pos"])) and np.array_equal(np.sort(st["id"]), np.arange(scene.n))
+    a.close()
+    b.close()
+
+
+def test_trained_network_gains_over_the_method_without_it():
+    """Held-out frames: the trained network's correction beats the single
+    plain update without it (u = 0) by a wide margin, and the judge takes
+    learned frames."""
+    model = pkg.Mpnn(8192, seed=4)
+    train = learned.collect(model, lambda s: scenes.dam_break_4096(seed=s), (1, 2), 8)
+    learned.collect(model, lambda s: scenes.dam_break_4096(seed=s), (3,), 4)
+    learned.train(model, 600, indices=range(train))
+    ev = learned.evaluate(model, range(train, model.sample_count))
+    assert ev["learned"] < 0.5 * ev["without_network"], ev
+    sim = _sim(scenes.dam_break_4096(seed=3), warm=3)
+    used = [sim.learned_frame(model, FRAME, SUBSTEPS, bound=0.01)[0] for _ in range(10)]
+    assert sum(used) >= 6, used
+    sim.close()
+    model.close()
