@@ -1,0 +1,73 @@
+"""Small, self-contained workloads for profiling single kernels with a
+profiler such as Nsight Compute (each runs a few launches of its kernels on
+inputs larger than L2 but a few hundred MB on the device at most).
+
+    python -m nbodysimulation_experiment_gb300.profile_cases springs
+    python -m nbodysimulation_experiment_gb300.profile_cases mpnn
+    python -m nbodysimulation_experiment_gb300.profile_cases batched
+    python -m nbodysimulation_experiment_gb300.profile_cases learned_frame
+"""
+from __future__ import annotations
+
+import sys
+
+import numpy as np
+
+from . import learned, scenes
+from .simulation import BatchSimulation, Mpnn, Simulation
+
+
+def springs(updates: int = 3) -> None:
+    """262,144-particle block with springs (gamma 0.1, alpha 0.3, k 0.3)."""
+    scene = scenes.scaled_block(512, seed=3, obstacles=False)
+    sim = Simulation(scene.domain())
+    scene.apply(sim)
+    sim.set_springs(True, yield_ratio=0.1, plasticity=0.3, stiffness=0.3, max_per_particle=16)
+    for _ in range(updates):
+        sim.update(float(scenes.DT))
+    sim.synchronize()
+    print("springs", sim.spring_count())
+    sim.close()
+
+
+def mpnn(steps: int = 3) -> None:
+    """Three training steps of the network on one 65,536-particle frame."""
+    model = Mpnn(70000, seed=1)
+    learned.collect(model, lambda s: scenes.obstacles_65536(seed=s), (1,), 1)
+    for _ in range(steps):
+        loss = model.train_step(0, 1e-3)
+    print("loss", loss)
+    model.close()
+
+
+def batched(updates: int = 3) -> None:
+    """64 scenes of the batched workload's distribution."""
+    mix = scenes.batch_scenes(count=64, seed=11)
+    batch = BatchSimulation(mix)
+    for _ in range(updates):
+        batch.update(float(scenes.DT))
+    batch.synchronize()
+    print("particles", batch.get_particle_count())
+    batch.close()
+
+
+def learned_frame(frames: int = 3) -> None:
+    """Learned frames (untrained network, judge off) on the 65,536-particle
+    obstacle scene."""
+    scene = scenes.obstacles_65536()
+    sim = Simulation(scene.domain())
+    scene.apply(sim)
+    sim.update(float(scenes.DT) / 4)
+    model = Mpnn(70000, seed=2)
+    for _ in range(frames):
+        sim.learned_frame(model, float(scenes.DT), 4, bound=1e9)
+    sim.synchronize()
+    print("frames", frames)
+    model.close()
+    sim.close()
+
+
+CASES = {"springs": springs, "mpnn": mpnn, "batched": batched, "learned_frame": learned_frame}
+
+if __name__ == "__main__":
+    CASES[sys.argv[1]]()
