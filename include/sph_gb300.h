@@ -212,6 +212,12 @@ int sph_kernel_launches(sph_sim *sim, uint64_t *out);
  * are replayed from a CUDA graph captured per step; enable = 0 launches every
  * kernel one by one instead.  Results are identical either way.  Default 1. */
 int sph_use_graphs(sph_sim *sim, int enable);
+/* No counterpart in the reference.  Launch-shape autotuner: times the next
+ * update (step dt) from the current state with 1, 2, ... resident blocks per
+ * SM for each of the two ordered sweeps, keeps the fastest counts and
+ * restores the state (results do not depend on the counts).  Needs a state
+ * after an update.  Reports the chosen block counts. */
+int sph_autotune(sph_sim *sim, float dt, int *visc_blocks, int *delta_blocks);
 
 /* ---- Viscoelastic springs (no reference counterpart) ----------------------
  * Springs with plasticity after Clavet et al. 2005 ("Particle-based

@@ -118,7 +118,6 @@ int refresh(sph_mpnn *m, cudaStream_t st) {
 	return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 
-size_t edge_smem() { return sizeof(float2) * 2 * kMpnnStage * kEdgeWarps; }
 
 int edge_blocks(const MpnnGraph &g) { return blocks((size_t)g.gx * g.gy, kEdgeWarps); }
 
@@ -130,7 +129,7 @@ int forward(sph_mpnn *m, const MpnnGraph &G, bool training, cudaStream_t st) {
 	const float2 *zin = G.z0;
 	for (int r = 0; r < kRounds; ++r) {
 		const float *P = m->params + (size_t)r * kRoundParams;
-		k_mpnn_edge_fwd<<<edge_blocks(G), kEdgeWarps * kWarp, edge_smem(), st>>>(G, P + kOffW1, P + kOffB1, zin,
+		k_mpnn_edge_fwd<<<edge_blocks(G), kEdgeWarps * kWarp, mpnn_edge_smem(false), st>>>(G, P + kOffW1, P + kOffB1, zin,
 		                                                                          m->Hb[r], m->degS, np, m->error);
 		MPNN_CUDA(cudaGetLastError());
 		if (training) {
@@ -230,7 +229,7 @@ int backward(sph_mpnn *m, const MpnnGraph &G, const float2 *target, cudaStream_t
 		MpnnGraph Gr = G;
 		const int needDz = r > 0;
 		if (needDz) MPNN_CUDA(cudaMemsetAsync(m->dzEdge, 0, sizeof(float2) * np, st));
-		k_mpnn_edge_bwd<<<edge_blocks(G), kEdgeWarps * kWarp, edge_smem(), st>>>(
+		k_mpnn_edge_bwd<<<edge_blocks(G), kEdgeWarps * kWarp, mpnn_edge_smem(true), st>>>(
 		    Gr, P + kOffW1, P + kOffB1, zr, m->dH, m->dzEdge, Gp + kOffW1, Gp + kOffB1, needDz, m->error);
 		MPNN_CUDA(cudaGetLastError());
 		if (needDz) {
@@ -355,10 +354,10 @@ int sph_mpnn_create(int device, size_t max_particles, uint64_t seed, sph_mpnn **
 		return code;
 	};
 	if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(SPH_ERR_CUDA);
-	if (cudaFuncSetAttribute(k_mpnn_edge_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)edge_smem()) !=
-	        cudaSuccess ||
-	    cudaFuncSetAttribute(k_mpnn_edge_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)edge_smem()) !=
-	        cudaSuccess)
+	if (cudaFuncSetAttribute(k_mpnn_edge_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize,
+	                         (int)mpnn_edge_smem(false)) != cudaSuccess ||
+	    cudaFuncSetAttribute(k_mpnn_edge_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize,
+	                         (int)mpnn_edge_smem(true)) != cudaSuccess)
 		return fail(SPH_ERR_CUDA);
 	if ((rc = zalloc(&m->params, kParams)) || (rc = zalloc(&m->grads, kParams)) || (rc = zalloc(&m->adamM, kParams)) ||
 	    (rc = zalloc(&m->adamV, kParams)) || (rc = zalloc(&m->W2b, kRounds * kHidden * kHidden)) ||

@@ -103,16 +103,28 @@ __device__ __forceinline__ void mma_commit(unsigned long long *bar) {
 
 // Stage rows [row0, row0+rows) x K [k0, k0+kc) of a row-major bf16 matrix
 // (leading dimension ld) into the core-matrix layout; rows past `valid` and
-// K past kc are zero.
-__device__ __forceinline__ void stage_tile(unsigned char *dst, const __nv_bfloat16 *src, int ld, int row0, int rows,
-                                           int valid, int k0, int kc) {
+// K past kc are zero.  Four 16-byte loads per thread are issued before their
+// shared-memory stores, so several loads are in flight per thread.
+__device__ __forceinline__ void stage_tile(unsigned char *dst, const __nv_bfloat16 *__restrict__ src, int ld, int row0,
+                                           int rows, int valid, int k0, int kc) {
 	const int chunks = rows * (kChunkK / 8);
-	for (int q = threadIdx.x; q < chunks; q += kGemmThreads) {
-		const int r = q / (kChunkK / 8), c8 = q % (kChunkK / 8);
-		uint4 v = make_uint4(0, 0, 0, 0);
-		if (row0 + r < valid && c8 * 8 < kc)
-			v = *reinterpret_cast<const uint4 *>(src + (size_t)(row0 + r) * ld + k0 + c8 * 8);
-		*reinterpret_cast<uint4 *>(dst + (r / 8) * kSbo + c8 * kLbo + (r % 8) * 16) = v;
+	for (int q0 = threadIdx.x; q0 < chunks; q0 += 4 * kGemmThreads) {
+		uint4 v[4];
+#pragma unroll
+		for (int u = 0; u < 4; ++u) {
+			const int q = q0 + u * kGemmThreads;
+			const int r = q / (kChunkK / 8), c8 = q % (kChunkK / 8);
+			v[u] = make_uint4(0, 0, 0, 0);
+			if (q < chunks && row0 + r < valid && c8 * 8 < kc)
+				v[u] = __ldg(reinterpret_cast<const uint4 *>(src + (size_t)(row0 + r) * ld + k0 + c8 * 8));
+		}
+#pragma unroll
+		for (int u = 0; u < 4; ++u) {
+			const int q = q0 + u * kGemmThreads;
+			if (q >= chunks) break;
+			const int r = q / (kChunkK / 8), c8 = q % (kChunkK / 8);
+			*reinterpret_cast<uint4 *>(dst + (r / 8) * kSbo + c8 * kLbo + (r % 8) * 16) = v[u];
+		}
 	}
 }
 
@@ -156,9 +168,14 @@ __global__ void __launch_bounds__(kGemmThreads, 1) k_gemm_bf16(GemmArgs g) {
 	for (int c = 0; c < nChunks; ++c) {
 		const int st = c & 1;
 		if (c >= 2) {
-			// The MMAs that read this stage two chunks ago must be done.
-			ok = ok && mbar_wait(&S.bar[st], phase[st]);
+			// The MMAs that read this stage two chunks ago must be done; if
+			// the bounded wait runs out, no further MMA is issued.
+			const bool w = mbar_wait(&S.bar[st], phase[st]);
 			phase[st] ^= 1;
+			if (__syncthreads_or(!w)) {
+				ok = false;
+				break;
+			}
 		}
 		const int k0 = kBegin + c * kChunkK;
 		const int kc = min(kChunkK, kEnd - k0);
@@ -176,8 +193,10 @@ __global__ void __launch_bounds__(kGemmThreads, 1) k_gemm_bf16(GemmArgs g) {
 		}
 	}
 	if (tid == 0) mma_commit(&S.done);  // arrives when every MMA issued above is complete
-	ok = ok && mbar_wait(&S.done, 0);
-	if (!ok) atomicOr(&S.fail, 1);
+	// Always wait (bounded) for the issued MMAs before reading or freeing
+	// tensor memory.
+	const bool d = mbar_wait(&S.done, 0);
+	if (!ok || !d) atomicOr(&S.fail, 1);
 	asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 	__syncthreads();
 	const bool good = S.fail == 0;

@@ -79,6 +79,7 @@ struct MpnnGraph {
 };
 
 constexpr int kEdgeWarps = 4;
+size_t mpnn_edge_smem(bool backward);
 
 __global__ void k_mpnn_edge_fwd(MpnnGraph G, const float *W1, const float *b1, const float2 *z, __nv_bfloat16 *Hb,
                                 float *degS, int np, uint32_t *error);

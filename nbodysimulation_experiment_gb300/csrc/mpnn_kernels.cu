@@ -18,6 +18,13 @@ constexpr unsigned kFull = 0xffffffffu;
 struct EdgeWarp {
 	float2 pos[kMpnnStage];
 	float2 z[kMpnnStage];
+	float feat[kWarp][8];  // features of the in-range edges of one group of 32 candidates
+	int nbr[kWarp];        // their neighbour numbers
+};
+
+struct EdgeWarpBwd {
+	EdgeWarp core;
+	float part[2][kWarp][kWarp + 1];  // per-edge partial sums, one per lane
 };
 
 // The 3x3 block of cells around cell c (y-major), as segments of the
@@ -66,21 +73,53 @@ __device__ __forceinline__ void stage_block(EdgeWarp &S, const Block &b, const M
 	__syncwarp();
 }
 
-// Edge features e_ij (see mpnn_internal.cuh).
-struct Feat {
-	float f[kEdgeIn];
-};
+__device__ __forceinline__ unsigned lanemask_lt() {
+	unsigned m;
+	asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+	return m;
+}
 
-__device__ __forceinline__ Feat features(float dx, float dy, float r, float2 zi, float2 zj, float invH) {
-	Feat e;
-	const float q = r * invH;
-	e.f[0] = dx * invH;
-	e.f[1] = dy * invH;
-	e.f[2] = q;
-	e.f[3] = zj.x - zi.x;
-	e.f[4] = zj.y - zi.y;
-	e.f[5] = (1.0f - q) * (1.0f - q);
-	return e;
+// The in-range edges among staged candidates [base, base+32) of the particle
+// at staged slot `self`: each lane tests one candidate and writes its edge
+// features (e_ij, see mpnn_internal.cuh) and neighbour number into the
+// group's compacted list; returns the list length.
+__device__ __forceinline__ int edge_group(EdgeWarp &S, const Block &b, int base, int self, float2 xi, float2 zi,
+                                          float h2, float invH, int lane) {
+	const int e = base + lane;
+	bool in = false;
+	float dx = 0.f, dy = 0.f, r2 = 0.f;
+	if (e < b.L && e != self) {
+		const float2 xj = S.pos[e];
+		dx = xj.x - xi.x;
+		dy = xj.y - xi.y;
+		// Unfused, as the neighbour sets of the plain step are computed.
+		r2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+		in = r2 < h2;
+	}
+	const unsigned mask = __ballot_sync(kFull, in);
+	if (in) {
+		const int slot = __popc(mask & lanemask_lt());
+		const float r = sqrtf(r2);
+		const float q = r * invH;
+		const float2 zj = S.z[e];
+		float *f = S.feat[slot];
+		*reinterpret_cast<float4 *>(f) = make_float4(dx * invH, dy * invH, q, zj.x - zi.x);
+		*reinterpret_cast<float2 *>(f + 4) = make_float2(zj.y - zi.y, (1.0f - q) * (1.0f - q));
+		S.nbr[slot] = block_number(b, e);
+	}
+	__syncwarp();
+	return __popc(mask);
+}
+
+__device__ __forceinline__ void load_feat(const EdgeWarp &S, int q, float (&f)[kEdgeIn]) {
+	const float4 a = *reinterpret_cast<const float4 *>(S.feat[q]);
+	const float2 c = *reinterpret_cast<const float2 *>(S.feat[q] + 4);
+	f[0] = a.x;
+	f[1] = a.y;
+	f[2] = a.z;
+	f[3] = a.w;
+	f[4] = c.x;
+	f[5] = c.y;
 }
 
 __device__ __forceinline__ float warp_sum(float v) {
@@ -92,7 +131,9 @@ __device__ __forceinline__ float warp_sum(float v) {
 }  // namespace
 
 // Edge layer 1, summed per particle: one warp per cell stages the cell's 3x3
-// block; lane l owns hidden features l, l+32, l+64, l+96.
+// block; per group of 32 candidates the lanes compute the in-range edges'
+// features once, then every lane applies its hidden features l, l+32, l+64,
+// l+96 to each edge.
 __global__ void __launch_bounds__(kEdgeWarps * kWarp) k_mpnn_edge_fwd(MpnnGraph G, const float *W1, const float *b1,
                                                                      const float2 *z, __nv_bfloat16 *Hb, float *degS,
                                                                      int np, uint32_t *error) {
@@ -130,21 +171,21 @@ __global__ void __launch_bounds__(kEdgeWarps * kWarp) k_mpnn_edge_fwd(MpnnGraph 
 			const float2 xi = S.pos[self], zi = S.z[self];
 			float acc[4] = {0.f, 0.f, 0.f, 0.f};
 			int deg = 0;
-			for (int e = 0; e < b.L; ++e) {
-				const float2 xj = S.pos[e];
-				const float dx = xj.x - xi.x, dy = xj.y - xi.y;
-				// Unfused, as the neighbour sets of the plain step are computed.
-				const float r2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
-				if (!(r2 < h2) || e == self) continue;
-				const Feat fe = features(dx, dy, sqrtf(r2), zi, S.z[e], G.invH);
+			for (int base = 0; base < b.L; base += kWarp) {
+				const int m = edge_group(S, b, base, self, xi, zi, h2, G.invH, lane);
+				for (int q = 0; q < m; ++q) {
+					float fe[kEdgeIn];
+					load_feat(S, q, fe);
 #pragma unroll
-				for (int q = 0; q < 4; ++q) {
-					float a = bias[q];
+					for (int u = 0; u < 4; ++u) {
+						float a = bias[u];
 #pragma unroll
-					for (int k = 0; k < kEdgeIn; ++k) a += w[q][k] * fe.f[k];
-					acc[q] += fmaxf(a, 0.f);
+						for (int k = 0; k < kEdgeIn; ++k) a += w[u][k] * fe[k];
+						acc[u] += fmaxf(a, 0.f);
+					}
 				}
-				++deg;
+				deg += m;
+				__syncwarp();
 			}
 			const int i = st + jj;
 #pragma unroll
@@ -162,14 +203,17 @@ __global__ void __launch_bounds__(kEdgeWarps * kWarp) k_mpnn_edge_fwd(MpnnGraph 
 }
 
 // Backward of the edge layer: dW1, db1 from every edge (i aggregates j),
-// and, if needDz, the node-state gradient through the z_j - z_i features
-// (scattered to j with atomics).
+// and, if needDz, the node-state gradient through the z_j - z_i features.
+// Per group of edges, each lane's share of the two node-state components is
+// summed across lanes through shared memory (lane q then owns edge q and
+// scatters its +share to the neighbour with atomics).
 __global__ void __launch_bounds__(kEdgeWarps * kWarp) k_mpnn_edge_bwd(MpnnGraph G, const float *W1, const float *b1,
                                                                      const float2 *z, const float *dH, float2 *dzEdge,
                                                                      float *gW1, float *gb1, int needDz,
                                                                      uint32_t *error) {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
-	EdgeWarp &S = reinterpret_cast<EdgeWarp *>(smem_raw)[threadIdx.x / kWarp];
+	EdgeWarpBwd &SB = reinterpret_cast<EdgeWarpBwd *>(smem_raw)[threadIdx.x / kWarp];
+	EdgeWarp &S = SB.core;
 	const int lane = threadIdx.x & (kWarp - 1);
 	float w[4][kEdgeIn], bias[4];
 	float gw[4][kEdgeIn], gb[4];
@@ -204,42 +248,54 @@ __global__ void __launch_bounds__(kEdgeWarps * kWarp) k_mpnn_edge_bwd(MpnnGraph 
 			float g[4];
 #pragma unroll
 			for (int q = 0; q < 4; ++q) g[q] = dH[(size_t)i * kHidden + lane + 32 * q] * kAggScale;
-			float dzx = 0.f, dzy = 0.f;
-			for (int e = 0; e < b.L; ++e) {
-				const float2 xj = S.pos[e];
-				const float dx = xj.x - xi.x, dy = xj.y - xi.y;
-				// Unfused, as the neighbour sets of the plain step are computed.
-				const float r2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
-				if (!(r2 < h2) || e == self) continue;
-				const Feat fe = features(dx, dy, sqrtf(r2), zi, S.z[e], G.invH);
-				float d3 = 0.f, d4 = 0.f;
+			float dzx = 0.f, dzy = 0.f;  // lane q: minus the shares of the edges it owned
+			for (int base = 0; base < b.L; base += kWarp) {
+				const int m = edge_group(S, b, base, self, xi, zi, h2, G.invH, lane);
+				for (int q = 0; q < m; ++q) {
+					float fe[kEdgeIn];
+					load_feat(S, q, fe);
+					float d3 = 0.f, d4 = 0.f;
 #pragma unroll
-				for (int q = 0; q < 4; ++q) {
-					float a = bias[q];
+					for (int u = 0; u < 4; ++u) {
+						float a = bias[u];
 #pragma unroll
-					for (int k = 0; k < kEdgeIn; ++k) a += w[q][k] * fe.f[k];
-					const float da = a > 0.f ? g[q] : 0.f;
+						for (int k = 0; k < kEdgeIn; ++k) a += w[u][k] * fe[k];
+						const float da = a > 0.f ? g[u] : 0.f;
 #pragma unroll
-					for (int k = 0; k < kEdgeIn; ++k) gw[q][k] += da * fe.f[k];
-					gb[q] += da;
-					d3 += w[q][3] * da;
-					d4 += w[q][4] * da;
-				}
-				if (needDz) {
-					d3 = warp_sum(d3);
-					d4 = warp_sum(d4);
-					if (lane == 0) {
-						const int j = block_number(b, e);
-						atomicAdd(&dzEdge[j].x, d3);
-						atomicAdd(&dzEdge[j].y, d4);
-						dzx -= d3;
-						dzy -= d4;
+						for (int k = 0; k < kEdgeIn; ++k) gw[u][k] += da * fe[k];
+						gb[u] += da;
+						d3 += w[u][3] * da;
+						d4 += w[u][4] * da;
+					}
+					if (needDz) {
+						SB.part[0][q][lane] = d3;
+						SB.part[1][q][lane] = d4;
 					}
 				}
+				if (needDz) {
+					__syncwarp();
+					if (lane < m) {
+						float s3 = 0.f, s4 = 0.f;
+						for (int t = 0; t < kWarp; ++t) {
+							s3 += SB.part[0][lane][t];
+							s4 += SB.part[1][lane][t];
+						}
+						const int j = S.nbr[lane];
+						atomicAdd(&dzEdge[j].x, s3);
+						atomicAdd(&dzEdge[j].y, s4);
+						dzx -= s3;
+						dzy -= s4;
+					}
+				}
+				__syncwarp();
 			}
-			if (needDz && lane == 0) {
-				atomicAdd(&dzEdge[i].x, dzx);
-				atomicAdd(&dzEdge[i].y, dzy);
+			if (needDz) {
+				dzx = warp_sum(dzx);
+				dzy = warp_sum(dzy);
+				if (lane == 0) {
+					atomicAdd(&dzEdge[i].x, dzx);
+					atomicAdd(&dzEdge[i].y, dzy);
+				}
 			}
 		}
 		__syncwarp();
@@ -455,6 +511,10 @@ __global__ void k_mpnn_u(const float2 *z2, const float2 *z0, float2 *u, int n) {
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= n) return;
 	u[i] = make_float2(z2[i].x - z0[i].x, z2[i].y - z0[i].y);
+}
+
+size_t mpnn_edge_smem(bool backward) {
+	return (backward ? sizeof(EdgeWarpBwd) : sizeof(EdgeWarp)) * kEdgeWarps;
 }
 
 }  // namespace sphgb

@@ -480,8 +480,15 @@ int enqueue_step(sph_sim *s, bool capturing) {
 	SPH_LAUNCHED(s);
 	SPH_CUDA(mark(kEvPredict));
 
-	k_scan<<<1, kScanThreads, 0, st>>>(tt, T);
-	SPH_LAUNCHED(s);
+	{
+		const int ntiles = (tt.ncell + kScanTile - 1) / kScanTile;
+		k_scan_reduce<<<ntiles, kScanThreads, 0, st>>>(tt, T);
+		SPH_LAUNCHED(s);
+		k_scan_tiles<<<1, kScanThreads, 0, st>>>(tt, T, ntiles);
+		SPH_LAUNCHED(s);
+		k_scan_apply<<<ntiles, kScanThreads, 0, st>>>(tt, T);
+		SPH_LAUNCHED(s);
+	}
 	k_scatter<<<blocks_for(tt.n, kElemThreads), kElemThreads, 0, st>>>(tt, A.view(), T);
 	SPH_LAUNCHED(s);
 	k_grid_update<<<s->gridBlocks, kGridWarps * kWarp, 0, st>>>(tt, A.view(), B.view(), T);
@@ -640,6 +647,7 @@ int allocate(sph_sim *s) {
 	    (rc = dalloc(&T.enterCursor, C)) || (rc = dalloc(&T.enterList, N)) || (rc = dalloc(&T.moverCount, 2)) ||
 	    (rc = dalloc(&T.bbox, 4 * C)) || (rc = dalloc(&T.newIdx, N)) || (rc = dalloc(&T.newLabel, N)) ||
 	    (rc = dalloc(&T.taskCounter, 2)) || (rc = dalloc(&T.stats, 4 * S)) || (rc = dalloc(&T.error, 1)) ||
+	    (rc = dalloc(&T.scanTiles, 3 * ((C + kScanTile - 1) / kScanTile))) ||
 	    (rc = dalloc(&T.abort, 1)) || (rc = dalloc(&T.bodies, s->bodyCap)) || (rc = dalloc(&s->doneV, C)))
 		return rc;
 	// Appendix runs: at most one partial run per scene beyond N / kAppendixRun.
@@ -1199,6 +1207,7 @@ int sph_destroy(sph_sim *s) {
 	                T.appPrev,     T.appCount,    T.appStart,    T.appIdx,      T.appCursor,   T.newCell,
 	                T.enterCount,  T.leaveCount,  T.enterOffset, T.enterCursor, T.enterList,   T.moverCount,
 	                T.bbox,        T.newIdx,      T.newLabel,    T.taskCounter, T.stats,       T.error,
+	                T.scanTiles,
 	                T.abort,       T.bodies,      s->doneV,      s->doneD,      s->stagePos,   s->stageForce,
 	                s->prof,       T.accN,        T.accP,        T.springPos,   T.springTotal,
 	                s->snap.pos,   s->snap.prev,  s->snap.vel,   s->snap.acc,   s->snap.dens,  s->snap.press,
@@ -1685,6 +1694,67 @@ int sph_load_springs(sph_sim *s, size_t count, const int32_t *spring_count, cons
 		SPH_CUDA(cudaMemcpyAsync(A.springL, rest, count * kSprings * 4, cudaMemcpyHostToDevice, s->stream));
 	}
 	SPH_CUDA(cudaStreamSynchronize(s->stream));
+	return SPH_OK;
+}
+
+// Launch-shape autotuner: the ordered sweeps are persistent kernels whose
+// resident block count trades parallel tasks against polling traffic; every
+// count gives the same results (the task order fixes them), so each candidate
+// is timed on the same update from a snapshot, and the fastest kept.
+int sph_autotune(sph_sim *s, float dt, int *visc_blocks, int *delta_blocks) {
+	if (!s || !(dt > 0.0f)) return SPH_ERR_INVALID_ARGUMENT;
+	SPH_CUDA(cudaSetDevice(s->device));
+	int rc = flush_adds(s);
+	if (rc) return rc;
+	for (const Scene &sc : s->scenes)
+		if (sc.n0 != sc.nDev) return SPH_ERR_NOT_SUPPORTED;  // needs a canonical state: update first
+	if (s->totalParticles() == 0) return SPH_ERR_NOT_SUPPORTED;
+	rc = ensure_learned(s);
+	if (rc) return rc;
+	int occV = 0, occD = 0;
+	SPH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occV, k_viscosity, kViscTaskWarps * kWarp,
+	                                                         visc_smem_bytes()));
+	SPH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occD, k_delta, kDeltaTaskWarps * kWarp,
+	                                                         delta_smem_bytes()));
+	const bool graphs = s->useGraphs;
+	s->useGraphs = false;
+	rc = copy_state(s, true);
+	if (rc) return rc;
+	float bestV = 1e30f, bestD = 1e30f;
+	int pickV = s->viscBlocks, pickD = s->deltaBlocks;
+	const int maxPer = std::max(occV, occD);
+	for (int per = 1; per <= maxPer && !rc; ++per) {
+		for (int rep = 0; rep < 2 && !rc; ++rep) {  // the first run of a shape warms it up
+			const int vb = std::min(per, occV) * s->numSMs, db = std::min(per, occD) * s->numSMs;
+			s->viscBlocks = vb;
+			s->deltaBlocks = db;
+			rc = copy_state(s, false);
+			if (!rc) rc = run_step(s, dt);
+			if (!rc) rc = check_device_errors(s);
+			if (rc || rep == 0) continue;
+			float tv = 0.f, td = 0.f;
+			SPH_CUDA(cudaEventElapsedTime(&tv, s->ev[kEvIntegrate], s->ev[kEvVisc]));
+			SPH_CUDA(cudaEventElapsedTime(&td, s->ev[kEvDensity], s->ev[kEvDelta]));
+			if (tv < bestV) {
+				bestV = tv;
+				pickV = vb;
+			}
+			if (td < bestD) {
+				bestD = td;
+				pickD = db;
+			}
+		}
+	}
+	if (!rc) rc = copy_state(s, false);
+	s->viscBlocks = pickV;
+	s->deltaBlocks = pickD;
+	s->useGraphs = graphs;
+	drop_graphs(s);
+	s->timed = false;
+	if (rc) return rc;
+	SPH_CUDA(cudaStreamSynchronize(s->stream));
+	if (visc_blocks) *visc_blocks = pickV;
+	if (delta_blocks) *delta_blocks = pickD;
 	return SPH_OK;
 }
 

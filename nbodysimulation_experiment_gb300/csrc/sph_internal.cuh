@@ -130,6 +130,7 @@ struct SimTables {
 	int *moverList, *moverCount;       // moverCount[0]: movers; [1]: max cell move
 	int *bbox;                         // per cell: x0, y0, x1, y1 of new cells
 	int *newCount, *newStart;
+	int *scanTiles;                    // 3 x tiles: per-tile sums, then tile offsets
 	int *newIdx;    // new number -> old number (the new cell arrays, concatenated)
 	int *newLabel;  // old number -> new number
 	uint32_t *done;                    // per sweep task

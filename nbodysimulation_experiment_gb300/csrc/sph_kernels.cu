@@ -411,47 +411,132 @@ __global__ void k_predict(Totals tt, Particles P, SimTables T) {
 }
 
 // ---------------------------------------------------------------------------
-// Exclusive scans over cells (single block).  Each thread owns a contiguous
-// run of cells (in `order` if given), sums it, the block scans the run
-// totals, and each thread writes its run's prefixes.
-__device__ void block_exscan_runs(int ncell, const int *in, const int *order, int *out) {
-	__shared__ int sums[kScanThreads];
-	const int tid = threadIdx.x;
-	const int per = (ncell + kScanThreads - 1) / kScanThreads;
-	const int b = tid * per, e = min(ncell, b + per);
-	int acc = 0;
-	for (int r = b; r < e; ++r) acc += in[order ? order[r] : r];
-	sums[tid] = acc;
-	__syncthreads();
-	for (int off = 1; off < kScanThreads; off <<= 1) {
-		int v = tid >= off ? sums[tid - off] : 0;
-		__syncthreads();
-		sums[tid] += v;
-		__syncthreads();
-	}
-	int run = tid > 0 ? sums[tid - 1] : 0;
-	for (int r = b; r < e; ++r) {
-		const int c = order ? order[r] : r;
-		out[c] = run;
-		run += in[c];
-	}
-	__syncthreads();
+// Exclusive scans over cells, in three passes over tiles of kScanTile
+// positions: per-tile sums, a scan of the tile sums, per-tile scans.  Three
+// scans run together: the appendix counts and the entering counts in cell
+// order, and the new cell counts (cellCount + appCount - leaveCount +
+// enterCount) in numbering order (scenes in order, cells in colour rank).
+
+namespace {
+
+__device__ __forceinline__ int new_count(const SimTables &T, int c) {
+	return T.cellCount[c] + T.appCount[c] - T.leaveCount[c] + T.enterCount[c];
 }
 
-__global__ void __launch_bounds__(kScanThreads) k_scan(Totals tt, SimTables T) {
-	for (int c = threadIdx.x; c < tt.ncell; c += blockDim.x) {
-		T.newCount[c] = T.cellCount[c] + T.appCount[c] - T.leaveCount[c] + T.enterCount[c];
+// Block-wide exclusive scan of one value per thread (kScanThreads threads);
+// returns the exclusive prefix and writes the block total to *total.
+__device__ __forceinline__ int block_exscan(int v, int *warpSums, int *total) {
+	const int lane = threadIdx.x & (kWarp - 1), warp = threadIdx.x / kWarp;
+	int incl = v;
+#pragma unroll
+	for (int o = 1; o < kWarp; o <<= 1) {
+		const int t = __shfl_up_sync(kFull, incl, o);
+		if (lane >= o) incl += t;
+	}
+	if (lane == kWarp - 1) warpSums[warp] = incl;
+	__syncthreads();
+	if (warp == 0) {
+		int w = lane < kScanThreads / kWarp ? warpSums[lane] : 0;
+		int wi = w;
+#pragma unroll
+		for (int o = 1; o < kWarp; o <<= 1) {
+			const int t = __shfl_up_sync(kFull, wi, o);
+			if (lane >= o) wi += t;
+		}
+		if (lane < kScanThreads / kWarp) warpSums[lane] = wi - w;
+		if (lane == kWarp - 1) *total = wi;
 	}
 	__syncthreads();
-	block_exscan_runs(tt.ncell, T.appCount, nullptr, T.appStart);
-	block_exscan_runs(tt.ncell, T.enterCount, nullptr, T.enterOffset);
-	// The new numbering: scenes in order, cells in colour rank order.
-	block_exscan_runs(tt.ncell, T.newCount, T.numberOrder, T.newStart);
+	const int r = warpSums[warp] + incl - v;
+	__syncthreads();
+	return r;
+}
+
+}  // namespace
+
+// Pass 1: the three sums of every tile.
+__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(Totals tt, SimTables T) {
+	__shared__ int part[3][kScanThreads / kWarp];
+	const int t = blockIdx.x;
+	int a = 0, e = 0, nw = 0;
+	for (int k = 0; k < kScanTile / kScanThreads; ++k) {
+		const int r = t * kScanTile + k * kScanThreads + threadIdx.x;
+		if (r < tt.ncell) {
+			a += T.appCount[r];
+			e += T.enterCount[r];
+			nw += new_count(T, T.numberOrder[r]);
+		}
+	}
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) {
+		a += __shfl_xor_sync(kFull, a, o);
+		e += __shfl_xor_sync(kFull, e, o);
+		nw += __shfl_xor_sync(kFull, nw, o);
+	}
+	const int lane = threadIdx.x & (kWarp - 1), warp = threadIdx.x / kWarp;
+	if (lane == 0) {
+		part[0][warp] = a;
+		part[1][warp] = e;
+		part[2][warp] = nw;
+	}
+	__syncthreads();
+	if (threadIdx.x < 3) {
+		int sum = 0;
+		for (int w = 0; w < kScanThreads / kWarp; ++w) sum += part[threadIdx.x][w];
+		T.scanTiles[threadIdx.x * gridDim.x + t] = sum;
+	}
+}
+
+// Pass 2 (one block): exclusive scans of the tile sums; also restarts the
+// per-scene neighbour-count statistics (demo4.cpp:369-370).
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(Totals tt, SimTables T, int ntiles) {
+	__shared__ int warpSums[kScanThreads / kWarp];
+	__shared__ int total;
+	for (int s3 = 0; s3 < 3; ++s3) {
+		int *v = T.scanTiles + s3 * ntiles;
+		int carry = 0;
+		for (int base = 0; base < ntiles; base += kScanThreads) {
+			const int i = base + threadIdx.x;
+			const int x = i < ntiles ? v[i] : 0;
+			const int ex = block_exscan(x, warpSums, &total);
+			if (i < ntiles) v[i] = carry + ex;
+			carry += total;
+			__syncthreads();
+		}
+	}
 	for (int sc = threadIdx.x; sc < tt.nscenes; sc += blockDim.x) {
-		// Neighbour-count statistics restart every search (demo4.cpp:369-370).
 		T.stats[4 * sc + 0] = T.scenes[sc].nbSeed;
 		T.stats[4 * sc + 1] = 0;
 		if (T.springTotal) T.springTotal[sc] = 0;
+	}
+}
+
+// Pass 3: per-tile scans plus the tile offsets; writes appStart, enterOffset,
+// newCount and newStart.
+__global__ void __launch_bounds__(kScanThreads) k_scan_apply(Totals tt, SimTables T) {
+	__shared__ int warpSums[kScanThreads / kWarp];
+	__shared__ int total;
+	const int t = blockIdx.x, nt = gridDim.x;
+	int ca = T.scanTiles[t], ce = T.scanTiles[nt + t], cn = T.scanTiles[2 * nt + t];
+	for (int k = 0; k < kScanTile / kScanThreads; ++k) {
+		const int r = t * kScanTile + k * kScanThreads + threadIdx.x;
+		const bool in = r < tt.ncell;
+		const int a = in ? T.appCount[r] : 0;
+		const int e = in ? T.enterCount[r] : 0;
+		const int c = in ? T.numberOrder[r] : 0;
+		const int nw = in ? new_count(T, c) : 0;
+		int ex = block_exscan(a, warpSums, &total);
+		if (in) T.appStart[r] = ca + ex;
+		ca += total;
+		ex = block_exscan(e, warpSums, &total);
+		if (in) T.enterOffset[r] = ce + ex;
+		ce += total;
+		ex = block_exscan(nw, warpSums, &total);
+		if (in) {
+			T.newCount[c] = nw;
+			T.newStart[c] = cn + ex;
+		}
+		cn += total;
 	}
 }
 

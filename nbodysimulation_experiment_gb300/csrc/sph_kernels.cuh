@@ -10,6 +10,7 @@ constexpr int kDeltaTaskWarps = 4;  // warps cooperating on one delta task (one 
 constexpr int kDensWarps = 8;
 constexpr int kGridWarps = 4;
 constexpr int kScanThreads = 1024;
+constexpr int kScanTile = 4 * kScanThreads;  // scan positions per block
 constexpr int kElemThreads = 256;  // elementwise kernels
 constexpr int kCollideThreads = 256;
 constexpr int kSpringWarps = 4;
@@ -26,7 +27,9 @@ size_t springs_smem_bytes();
 __global__ void k_integrate(Totals tt, Particles P, SimTables T);
 __global__ void k_viscosity(Totals tt, Particles P, SimTables T);
 __global__ void k_predict(Totals tt, Particles P, SimTables T);
-__global__ void k_scan(Totals tt, SimTables T);
+__global__ void k_scan_reduce(Totals tt, SimTables T);
+__global__ void k_scan_tiles(Totals tt, SimTables T, int ntiles);
+__global__ void k_scan_apply(Totals tt, SimTables T);
 __global__ void k_scatter(Totals tt, Particles P, SimTables T);
 __global__ void k_grid_update(Totals tt, Particles P, Particles Q, SimTables T);
 __global__ void k_density(Totals tt, Particles Q, SimTables T);

@@ -59,10 +59,12 @@ __device__ __forceinline__ int seg_number(int e, const int (&off)[NSEG], const i
 struct SpringWarp {
 	float2 pos[kStageCap];
 	int tag[kStageCap];
-	int ex[kWarp][kSprings];     // existing partners (new numbers) per lane
-	float kr2[kWarp][kSprings];  // chosen candidates per lane, sorted
-	int ktag[kWarp][kSprings];
-	int kj[kWarp][kSprings];
+	// Per-lane lists, slot-major ([slot][lane]) so that the lanes' accesses
+	// fall on distinct banks.
+	int ex[kSprings][kWarp];     // existing partners (new numbers)
+	float kr2[kSprings][kWarp];  // chosen candidates, sorted
+	int ktag[kSprings][kWarp];
+	int kj[kSprings][kWarp];
 };
 
 size_t springs_smem_bytes() { return sizeof(SpringWarp) * kSpringWarps; }
@@ -124,7 +126,7 @@ __global__ void __launch_bounds__(kSpringWarps * kWarp) k_springs_select(Totals 
 				for (int q = 0; q < ne; ++q) {
 					const int pn = T.newLabel[P.springP[o * kSprings + q]];
 					float rest = P.springL[o * kSprings + q];
-					S.ex[lane][q] = pn;
+					S.ex[q][lane] = pn;
 					const float2 xp = Q.pos[pn];
 					const float rx = xp.x - xi.x, ry = xp.y - xi.y;
 					const float r2 = rx * rx + ry * ry;
@@ -146,24 +148,24 @@ __global__ void __launch_bounds__(kSpringWarps * kWarp) k_springs_select(Totals 
 				const float r2 = rx * rx + ry * ry;
 				if (!(r2 < s.h2)) continue;
 				bool has = false;
-				for (int q = 0; q < ne; ++q) has = has || S.ex[lane][q] == num;
+				for (int q = 0; q < ne; ++q) has = has || S.ex[q][lane] == num;
 				if (has) continue;
 				const int tj = S.tag[e];
-				if (kc == freeSlots && !before(r2, tj, S.kr2[lane][kc - 1], S.ktag[lane][kc - 1])) continue;
+				if (kc == freeSlots && !before(r2, tj, S.kr2[kc - 1][lane], S.ktag[kc - 1][lane])) continue;
 				int at = kc < freeSlots ? kc++ : kc - 1;
-				while (at > 0 && before(r2, tj, S.kr2[lane][at - 1], S.ktag[lane][at - 1])) {
-					S.kr2[lane][at] = S.kr2[lane][at - 1];
-					S.ktag[lane][at] = S.ktag[lane][at - 1];
-					S.kj[lane][at] = S.kj[lane][at - 1];
+				while (at > 0 && before(r2, tj, S.kr2[at - 1][lane], S.ktag[at - 1][lane])) {
+					S.kr2[at][lane] = S.kr2[at - 1][lane];
+					S.ktag[at][lane] = S.ktag[at - 1][lane];
+					S.kj[at][lane] = S.kj[at - 1][lane];
 					--at;
 				}
-				S.kr2[lane][at] = r2;
-				S.ktag[lane][at] = tj;
-				S.kj[lane][at] = num;
+				S.kr2[at][lane] = r2;
+				S.ktag[at][lane] = tj;
+				S.kj[at][lane] = num;
 			}
 			if (active) {
 				T.accN[j] = kc;
-				for (int q = 0; q < kc; ++q) T.accP[j * kSprings + q] = S.kj[lane][q];
+				for (int q = 0; q < kc; ++q) T.accP[j * kSprings + q] = S.kj[q][lane];
 				Q.springN[j] = m;
 			}
 			__syncwarp();

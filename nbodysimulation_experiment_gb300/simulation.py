@@ -189,6 +189,7 @@ def load_library(build_if_missing: bool = True):
         "sph_synchronize": [vp],
         "sph_kernel_launches": [vp, P(_c.c_uint64)],
         "sph_use_graphs": [vp, _c.c_int],
+        "sph_autotune": [vp, _c.c_float, P(_c.c_int), P(_c.c_int)],
         "sph_set_springs": [vp, P(SpringParams)],
         "sph_get_spring_count": [vp, P(_c.c_uint64)],
         "sph_dump_springs": [vp, _c.c_size_t, vp, vp, vp],
@@ -237,7 +238,7 @@ C_SYMBOLS = (
     "sph_set_multithreading", "sph_is_multithreading_supported", "sph_is_multithreading",
     "sph_get_worker_thread_count", "sph_read_particles", "sph_state_info", "sph_dump_state", "sph_load_state",
     "sph_get_stream", "sph_device_arrays", "sph_synchronize", "sph_kernel_launches",
-    "sph_use_graphs", "sph_set_springs", "sph_get_spring_count", "sph_dump_springs", "sph_load_springs",
+    "sph_use_graphs", "sph_autotune", "sph_set_springs", "sph_get_spring_count", "sph_dump_springs", "sph_load_springs",
     "sph_mpnn_create", "sph_mpnn_destroy", "sph_mpnn_param_count", "sph_mpnn_get_params", "sph_mpnn_set_params",
     "sph_mpnn_capture", "sph_mpnn_sample_count", "sph_mpnn_clear_samples", "sph_mpnn_sample_info",
     "sph_mpnn_read_sample", "sph_mpnn_eval", "sph_mpnn_gradient", "sph_mpnn_train_step", "sph_learned_frame",
@@ -464,6 +465,12 @@ class Simulation:
         """Replay repeated updates from a per-step CUDA graph (default on)."""
         self._call("sph_use_graphs", 1 if enable else 0)
 
+    def autotune(self, delta_time: float) -> Tuple[int, int]:
+        """Pick the sweeps' resident block counts by timing (state kept)."""
+        v, d = _c.c_int(), _c.c_int()
+        self._call("sph_autotune", float(np.float32(delta_time)), _c.byref(v), _c.byref(d))
+        return v.value, d.value
+
     # --- viscoelastic springs (no reference counterpart) ----------------------
     def set_springs(self, enabled: bool = True, yield_ratio: float = 0.1, plasticity: float = 0.3,
                     stiffness: float = 0.3, max_per_particle: int = SPRING_SLOTS):
@@ -630,6 +637,12 @@ class BatchSimulation:
     def use_graphs(self, enable: bool = True):
         """Replay repeated updates from a per-step CUDA graph (default on)."""
         self._call("sph_use_graphs", 1 if enable else 0)
+
+    def autotune(self, delta_time: float) -> Tuple[int, int]:
+        """Pick the sweeps' resident block counts by timing (state kept)."""
+        v, d = _c.c_int(), _c.c_int()
+        self._call("sph_autotune", float(np.float32(delta_time)), _c.byref(v), _c.byref(d))
+        return v.value, d.value
 
 
 class Mpnn:

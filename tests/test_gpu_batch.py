@@ -126,3 +126,22 @@ def test_full_batch_of_512_scenes():
         want, _ = _single_run(mix[k], steps)
         _assert_same_state(got, want, mix[k].name)
     batch.close()
+
+
+def test_autotune_keeps_results_and_state():
+    """The autotuner times candidate launch shapes from a snapshot and
+    restores it: the trajectory is the same as without tuning."""
+    mix = scenes.batch_scenes(count=4, seed=17, n_min=1024, n_max=4096)
+    runs = []
+    for tune in (False, True):
+        batch = pkg.BatchSimulation(mix)
+        batch.update(float(scenes.DT))
+        if tune:
+            v, d = batch.autotune(float(scenes.DT))
+            assert v > 0 and d > 0
+        for _ in range(10):
+            batch.update(float(scenes.DT))
+        runs.append([batch.dump_state(k) for k in range(len(mix))])
+        batch.close()
+    for a, b in zip(*runs):
+        _assert_same_state(a, b, "autotune")
