@@ -22,9 +22,11 @@ extern "C" {
  * of 8, 16-byte aligned), C FP32 row-major (ldc).  N a multiple of 16 up to
  * 256, K a multiple of 16, any M.  Optional bias [N] and ReLU; accumulate = 1
  * adds into C atomically (required when splits > 1 divides K over CTAs).
- * Enqueued on `stream` (cudaStream_t) and waited for. */
+ * staging = 0 feeds the operands with TMA (cp.async.bulk.tensor, 128-byte
+ * swizzle); 1 with plain loads.  Enqueued on `stream` (cudaStream_t) and
+ * waited for. */
 int sph_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K, int lda, int ldb, int ldc,
-                  const float *bias, int relu, int accumulate, int splits, void *stream);
+                  const float *bias, int relu, int accumulate, int splits, int staging, void *stream);
 
 /* The network.  Two rounds of message passing over the radius-h neighbour
  * graph (the 3x3 cell block of each particle, pairs closer than h), each

@@ -533,7 +533,7 @@ uint32_t *gemm_error_word(int device) {
 }  // namespace
 
 extern "C" int sph_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K, int lda, int ldb, int ldc,
-                             const float *bias, int relu, int accumulate, int splits, void *stream) {
+                             const float *bias, int relu, int accumulate, int splits, int staging, void *stream) {
 	int device = 0;
 	if (cudaGetDevice(&device) != cudaSuccess) return SPH_ERR_NO_DEVICE;
 	GemmArgs g{};
@@ -549,6 +549,7 @@ extern "C" int sph_gemm_bf16(const void *A, const void *B, float *C, int M, int 
 	g.C = C;
 	g.ldc = ldc;
 	g.accumulate = accumulate;
+	g.noTma = staging;
 	g.error = gemm_error_word(device);
 	if (!A || !B || !C || !g.error || ldc < N) return SPH_ERR_INVALID_ARGUMENT;
 	if (gemm_check(g, splits) != 0) return SPH_ERR_INVALID_ARGUMENT;

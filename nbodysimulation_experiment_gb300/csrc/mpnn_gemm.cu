@@ -15,9 +15,13 @@
 // (row-major or transposed).  Split-K over gridDim.y accumulates FP32 with
 // atomics.  Every mbarrier wait is bounded; a timeout sets an error flag and
 // the CTA still frees its tensor memory.
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 #include <stdint.h>
+
+#include <mutex>
 
 #include "mpnn_internal.cuh"
 
@@ -34,7 +38,7 @@ constexpr int kSbo = kCoreBytes * (kChunkK / 8);  // 8-row groups: 1 KiB
 constexpr int kStageABytes = kTileM * kChunkK * 2;
 constexpr int kMaxN = 256;
 constexpr int kStageBBytes = kMaxN * kChunkK * 2;
-constexpr uint32_t kWaitPolls = 1u << 26;
+constexpr uint32_t kWaitPolls = 1u << 22;
 
 struct __align__(1024) GemmSmem {
 	unsigned char a[2][kStageABytes];
@@ -70,19 +74,22 @@ __device__ __forceinline__ void mbar_init(unsigned long long *bar, uint32_t coun
 	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
 
-// Bounded wait for the phase with the given parity to complete.
+// Bounded wait for the phase with the given parity to complete: a
+// non-blocking test with a short sleep between polls, at most 2^22 polls
+// (well under a second) before giving up.
 __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, uint32_t parity) {
 	const uint32_t addr = smem_u32(bar);
 	for (uint32_t i = 0; i < kWaitPolls; ++i) {
 		uint32_t ok;
 		asm volatile(
 		    "{\n\t.reg .pred p;\n\t"
-		    "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+		    "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
 		    "selp.u32 %0, 1, 0, p;\n\t}"
 		    : "=r"(ok)
 		    : "r"(addr), "r"(parity)
 		    : "memory");
 		if (ok) return true;
+		if (i > 64) __nanosleep(64);
 	}
 	return false;
 }
@@ -124,6 +131,41 @@ __device__ __forceinline__ void stage_tile(unsigned char *dst, const __nv_bfloat
 			if (q >= chunks) break;
 			const int r = q / (kChunkK / 8), c8 = q % (kChunkK / 8);
 			*reinterpret_cast<uint4 *>(dst + (r / 8) * kSbo + c8 * kLbo + (r % 8) * 16) = v[u];
+		}
+	}
+}
+
+// Epilogue: thread = row (warp w reads TMEM lanes 32w..32w+31); 16 columns
+// per tensor-memory load; bias, row-scaled bias, ReLU, then the requested
+// stores.
+__device__ __forceinline__ void epilogue(const GemmArgs &g, uint32_t tmem, int row0, int warp, int lane) {
+	const int row = row0 + warp * 32 + lane;
+	for (int c0 = 0; c0 < g.N; c0 += 16) {
+		uint32_t v[16];
+		const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+		asm volatile(
+		    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+		    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+		      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+		    : "r"(taddr)
+		    : "memory");
+		asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+		if (row >= g.M) continue;
+#pragma unroll
+		for (int u = 0; u < 16; ++u) {
+			const int col = c0 + u;
+			if (col >= g.N) break;
+			float x = __uint_as_float(v[u]);
+			if (g.bias) x += g.bias[col];
+			if (g.rowScale) x += g.rowScale[row] * g.bias2[col];
+			if (g.relu) x = fmaxf(x, 0.0f);
+			if (g.C) {
+				float *dst = g.C + (size_t)row * g.ldc + col;
+				if (g.accumulate) atomicAdd(dst, x);
+				else *dst = x;
+			}
+			if (g.Cb) g.Cb[(size_t)row * g.ldcb + col] = __float2bfloat16_rn(x);
+			if (g.CbT) g.CbT[(size_t)col * g.ldcbT + row] = __float2bfloat16_rn(x);
 		}
 	}
 }
@@ -203,41 +245,188 @@ __global__ void __launch_bounds__(kGemmThreads, 1) k_gemm_bf16(GemmArgs g) {
 	if (!good && tid == 0) atomicOr(g.error, 1u);
 
 	// Epilogue: thread = row; 16 columns per tensor-memory load.
-	const int row = row0 + warp * 32 + lane;
-	for (int c0 = 0; c0 < g.N && good && nChunks > 0; c0 += 16) {
-		uint32_t v[16];
-		const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
-		asm volatile(
-		    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-		    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-		      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-		    : "r"(taddr)
-		    : "memory");
-		asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-		if (row >= g.M) continue;
-#pragma unroll
-		for (int u = 0; u < 16; ++u) {
-			const int col = c0 + u;
-			if (col >= g.N) break;
-			float x = __uint_as_float(v[u]);
-			if (g.bias) x += g.bias[col];
-			if (g.rowScale) x += g.rowScale[row] * g.bias2[col];
-			if (g.relu) x = fmaxf(x, 0.0f);
-			if (g.C) {
-				float *dst = g.C + (size_t)row * g.ldc + col;
-				if (g.accumulate) atomicAdd(dst, x);
-				else *dst = x;
-			}
-			if (g.Cb) g.Cb[(size_t)row * g.ldcb + col] = __float2bfloat16_rn(x);
-			if (g.CbT) g.CbT[(size_t)col * g.ldcbT + row] = __float2bfloat16_rn(x);
-		}
-	}
+	if (good && nChunks > 0) epilogue(g, tmem, row0, warp, lane);
 	asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
 	__syncthreads();
 	if (warp == 0) {
 		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
 	}
 }
+
+// ---------------------------------------------------------------------------
+// TMA-fed variant: each operand tile (128 or N rows x 64 K) is one
+// cp.async.bulk.tensor load with 128-byte swizzle into a 1 KiB-aligned stage,
+// completing on the stage's "full" mbarrier; the MMAs read it through
+// SWIZZLE_128B K-major descriptors (8-row groups 1 KiB apart; the 16-wide K
+// steps advance the start address by 32 bytes inside the swizzle atom) and
+// release it through tcgen05.commit on the stage's "empty" mbarrier.  One
+// thread drives the three-stage pipeline; the others wait for the final
+// commit and run the epilogue.  Rows and K beyond the matrices read as zero.
+
+namespace {
+
+constexpr int kTmaStages = 3;
+constexpr int kTmaABytes = kTileM * kChunkK * 2;  // 16 KiB
+
+__host__ __device__ inline size_t tma_stage_bytes(int n) { return (size_t)kTmaABytes + (size_t)n * kChunkK * 2; }
+
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
+	uint64_t d = 0;
+	d |= (uint64_t)((addr >> 4) & 0x3fff);
+	d |= (uint64_t)1 << 16;                  // leading byte offset (unused for swizzled K-major)
+	d |= (uint64_t)(1024 >> 4) << 32;        // 8-row groups 1 KiB apart
+	d |= (uint64_t)1 << 46;                  // descriptor version
+	d |= (uint64_t)2 << 61;                  // SWIZZLE_128B
+	return d;
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, uint32_t bytes) {
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+	             : "memory");
+}
+
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y,
+                                            unsigned long long *bar) {
+	asm volatile(
+	    "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+	    "[%4];" ::"r"(smem_u32(dst)),
+	    "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+	    : "memory");
+}
+
+}  // namespace
+
+size_t gemm_tma_smem_bytes(int n) { return kTmaStages * tma_stage_bytes(n) + 2048; }
+
+__global__ void __launch_bounds__(kGemmThreads, 1) k_gemm_bf16_tma(GemmArgs g, const __grid_constant__ CUtensorMap mapA,
+                                                                   const __grid_constant__ CUtensorMap mapB) {
+	extern __shared__ unsigned char smem_raw[];
+	unsigned char *base =
+	    reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+	const size_t stage = tma_stage_bytes(g.N);
+	unsigned long long *full = reinterpret_cast<unsigned long long *>(base + kTmaStages * stage);
+	unsigned long long *empty = full + kTmaStages;
+	unsigned long long *done = empty + kTmaStages;
+	uint32_t *tmemSlot = reinterpret_cast<uint32_t *>(done + 1);
+	int *fail = reinterpret_cast<int *>(tmemSlot + 1);
+	const int tid = threadIdx.x, warp = tid / 32, lane = tid & 31;
+	const int row0 = blockIdx.x * kTileM;
+	const int kPer = ((g.K + gridDim.y - 1) / gridDim.y + kChunkK - 1) / kChunkK * kChunkK;
+	const int kBegin = blockIdx.y * kPer;
+	const int kEnd = min(g.K, kBegin + kPer);
+	const int ncols = g.N <= 32 ? 32 : (g.N <= 64 ? 64 : (g.N <= 128 ? 128 : 256));
+	const int nChunks = kEnd > kBegin ? (kEnd - kBegin + kChunkK - 1) / kChunkK : 0;
+
+	if (tid == 0) {
+		for (int s = 0; s < kTmaStages; ++s) {
+			mbar_init(&full[s], 1);
+			mbar_init(&empty[s], 1);
+		}
+		mbar_init(done, 1);
+		*fail = 0;
+		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+		asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapA)) : "memory");
+		asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapB)) : "memory");
+	}
+	if (warp == 0) {
+		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmemSlot)),
+		             "r"(ncols)
+		             : "memory");
+		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+	__syncthreads();
+	asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+	const uint32_t tmem = *tmemSlot;
+
+	if (tid == 0) {
+		const uint32_t idesc = instr_desc(g.N);
+		const uint32_t bytes = (uint32_t)stage;
+		bool ok = true;
+		for (int c = 0; c < nChunks && c < kTmaStages; ++c) {
+			unsigned char *st = base + c * stage;
+			mbar_expect_tx(&full[c], bytes);
+			tma_load_2d(st, &mapA, kBegin + c * kChunkK, row0, &full[c]);
+			tma_load_2d(st + kTmaABytes, &mapB, kBegin + c * kChunkK, 0, &full[c]);
+		}
+		for (int c = 0; c < nChunks && ok; ++c) {
+			const int s = c % kTmaStages;
+			const uint32_t parity = (uint32_t)(c / kTmaStages) & 1u;
+			if (!mbar_wait(&full[s], parity)) {
+				ok = false;
+				break;
+			}
+			asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+			const uint32_t a0 = smem_u32(base + s * stage), b0 = a0 + kTmaABytes;
+			const int kc = min(kChunkK, kEnd - (kBegin + c * kChunkK));
+			for (int k = 0; k < kc / 16; ++k)
+				mma_bf16(tmem, sw128_desc(a0 + k * 32), sw128_desc(b0 + k * 32), idesc, c > 0 || k > 0);
+			mma_commit(&empty[s]);
+			const int next = c + kTmaStages;
+			if (next < nChunks) {
+				// The stage is reloaded once the MMAs reading it are done.
+				if (!mbar_wait(&empty[s], parity)) {
+					ok = false;
+					break;
+				}
+				unsigned char *st = base + s * stage;
+				mbar_expect_tx(&full[s], bytes);
+				tma_load_2d(st, &mapA, kBegin + next * kChunkK, row0, &full[s]);
+				tma_load_2d(st + kTmaABytes, &mapB, kBegin + next * kChunkK, 0, &full[s]);
+			}
+		}
+		mma_commit(done);
+		if (!ok) *fail = 1;
+	}
+	__syncwarp();
+	// Always wait (bounded) for the issued MMAs before reading or freeing
+	// tensor memory.  A load still in flight after a failed wait completes
+	// into this CTA's own shared memory.
+	const bool d = mbar_wait(done, 0);
+	if (!d) atomicOr(fail, 1);
+	asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+	__syncthreads();
+	const bool good = *fail == 0;
+	if (!good && tid == 0) atomicOr(g.error, 1u);
+	if (good && nChunks > 0) epilogue(g, tmem, row0, warp, lane);
+	asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+	__syncthreads();
+	if (warp == 0) {
+		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
+	}
+}
+
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+	static std::once_flag once;
+	static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+	std::call_once(once, [] {
+		void *p = nullptr;
+		cudaDriverEntryPointQueryResult q;
+		if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+		        cudaSuccess &&
+		    q == cudaDriverEntryPointSuccess)
+			fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+	});
+	return fn;
+}
+
+// Row-major bf16 matrix [rows][K] (leading dimension ld) as 64 x boxRows
+// tiles with 128-byte swizzle.
+bool encode(CUtensorMap *map, const __nv_bfloat16 *ptr, int rows, int K, int ld, int boxRows) {
+	PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
+	if (!fn) return false;
+	const cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+	const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+	const cuuint32_t box[2] = {(cuuint32_t)kChunkK, (cuuint32_t)boxRows};
+	const cuuint32_t estr[2] = {1, 1};
+	return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16 *>(ptr), dims, strides, box, estr,
+	          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+	          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace
 
 int gemm_check(const GemmArgs &g, int splits) {
 	if (g.M <= 0 || g.N <= 0 || g.K <= 0 || g.N > kMaxN || g.N % 16 != 0 || g.K % 16 != 0) return -1;
@@ -248,15 +437,23 @@ int gemm_check(const GemmArgs &g, int splits) {
 }
 
 cudaError_t gemm_launch(const GemmArgs &g, int splits, cudaStream_t stream) {
-	static bool attr = false;
-	if (!attr) {
-		cudaError_t e = cudaFuncSetAttribute(k_gemm_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize,
-		                                     (int)gemm_smem_bytes());
-		if (e != cudaSuccess) return e;
-		attr = true;
-	}
+	static std::once_flag once;
+	static cudaError_t attrErr = cudaSuccess;
+	std::call_once(once, [] {
+		attrErr = cudaFuncSetAttribute(k_gemm_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                               (int)gemm_smem_bytes());
+		if (attrErr == cudaSuccess)
+			attrErr = cudaFuncSetAttribute(k_gemm_bf16_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			                               (int)gemm_tma_smem_bytes(kMaxN));
+	});
+	if (attrErr != cudaSuccess) return attrErr;
 	dim3 grid((g.M + kTileM - 1) / kTileM, splits);
-	k_gemm_bf16<<<grid, kGemmThreads, gemm_smem_bytes(), stream>>>(g);
+	CUtensorMap mapA, mapB;
+	if (!g.noTma && encode(&mapA, g.A, g.M, g.K, g.lda, kTileM) && encode(&mapB, g.B, g.N, g.K, g.ldb, g.N)) {
+		k_gemm_bf16_tma<<<grid, kGemmThreads, gemm_tma_smem_bytes(g.N), stream>>>(g, mapA, mapB);
+	} else {
+		k_gemm_bf16<<<grid, kGemmThreads, gemm_smem_bytes(), stream>>>(g);
+	}
 	return cudaGetLastError();
 }
 

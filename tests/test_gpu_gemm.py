@@ -14,20 +14,21 @@ pytestmark = pytest.mark.gpu
 REL_TOL = 1e-5
 
 
-def _gemm(lib, a, b, c, bias=None, relu=False, accumulate=False, splits=1):
+def _gemm(lib, a, b, c, bias=None, relu=False, accumulate=False, splits=1, staging=0):
     fn = lib.sph_gemm_bf16
     fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_int] * 6 + [
-        ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+        ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
     fn.restype = ctypes.c_int
     m, k = a.shape
     n = b.shape[0]
     return fn(a.data_ptr(), b.data_ptr(), c.data_ptr(), m, n, k, a.stride(0), b.stride(0), c.stride(0),
-              bias.data_ptr() if bias is not None else None, int(relu), int(accumulate), splits, None)
+              bias.data_ptr() if bias is not None else None, int(relu), int(accumulate), splits, staging, None)
 
 
+@pytest.mark.parametrize("staging", [0, 1])
 @pytest.mark.parametrize("m,n,k", [(128, 128, 128), (256, 144, 144), (300, 16, 128), (128, 256, 64),
                                    (1000, 128, 48)])
-def test_gemm_matches_fp32_reference(m, n, k):
+def test_gemm_matches_fp32_reference(m, n, k, staging):
     torch = pytest.importorskip("torch")
     lib = pkg.load_library()
     g = torch.Generator(device="cuda").manual_seed(m * 7 + n + k)
@@ -35,11 +36,27 @@ def test_gemm_matches_fp32_reference(m, n, k):
     b = torch.randn(n, k, device="cuda", generator=g).to(torch.bfloat16)
     bias = torch.randn(n, device="cuda", generator=g)
     c = torch.full((m, n), float("nan"), device="cuda")
-    assert _gemm(lib, a, b, c, bias=bias, relu=True) == simulation.SPH_OK
+    assert _gemm(lib, a, b, c, bias=bias, relu=True, staging=staging) == simulation.SPH_OK
     torch.cuda.synchronize()
     want = torch.relu(a.float() @ b.float().T + bias)
     err = (c - want).norm() / want.norm()
     assert err < REL_TOL, float(err)
+
+
+def test_gemm_with_leading_dimensions():
+    """Operands that are column slices of wider arrays (leading dimension >
+    K), as the network's backward pass uses them."""
+    torch = pytest.importorskip("torch")
+    lib = pkg.load_library()
+    g = torch.Generator(device="cuda").manual_seed(9)
+    wide_a = torch.randn(384, 144, device="cuda", generator=g).to(torch.bfloat16)
+    wide_b = torch.randn(128, 200, device="cuda", generator=g).to(torch.bfloat16)
+    a, b = wide_a[:, :128], wide_b[:, :128]
+    c = torch.zeros(384, 128, device="cuda")
+    assert _gemm(lib, a, b, c) == simulation.SPH_OK
+    torch.cuda.synchronize()
+    want = a.float() @ b.float().T
+    assert float((c - want).norm() / want.norm()) < REL_TOL
 
 
 def test_gemm_split_k_accumulates():
