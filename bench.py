@@ -222,7 +222,8 @@ def bench_batched(torch, pkg, scenes, device: int, steps: int, warmup: int):
     return {"value": total * steps / (sum(ms) / 1e3), "unit": UNIT, "ms_per_step": statistics.mean(ms),
             "steps": steps, "warmup": warmup, "scenes": len(mix), "particles": int(total),
             "gpu_launches": int(launches), "graphs": True,
-            "autotuned_blocks": {"viscosity": tuned[0], "delta": tuned[1]},
+            "autotuned_shape": {"viscosity_warps": tuned[0], "viscosity_blocks": tuned[1],
+                                "delta_warps": tuned[2], "delta_blocks": tuned[3]},
             "density_error": float(np.mean(errs)),
             "workload": "512 independent box scenes, particle counts log-uniform in [1024, 65536] (seeded), "
                         "each a jittered block + 0-4 circles, 4 walls, plain step, FP32; inputs > L2"}

@@ -212,12 +212,17 @@ int sph_kernel_launches(sph_sim *sim, uint64_t *out);
  * are replayed from a CUDA graph captured per step; enable = 0 launches every
  * kernel one by one instead.  Results are identical either way.  Default 1. */
 int sph_use_graphs(sph_sim *sim, int enable);
-/* No counterpart in the reference.  Launch-shape autotuner: times the next
- * update (step dt) from the current state with 1, 2, ... resident blocks per
- * SM for each of the two ordered sweeps, keeps the fastest counts and
- * restores the state (results do not depend on the counts).  Needs a state
- * after an update.  Reports the chosen block counts. */
-int sph_autotune(sph_sim *sim, float dt, int *visc_blocks, int *delta_blocks);
+/* No counterpart in the reference.  Launch shapes of the two ordered sweeps
+ * (viscosity, delta): shape[4] = {viscosity warps per task (4 or 2),
+ * viscosity blocks, delta warps per task (4 or 2), delta blocks}.  Four
+ * warps shorten one scene's critical path; two fit more tasks on an SM for
+ * many scenes.  Results do not depend on the shape.  sph_autotune times the
+ * next update (step dt) from the current state for every shape and resident
+ * block count per SM, keeps the fastest for each sweep, restores the state
+ * and reports the choice; it needs a state after an update. */
+int sph_autotune(sph_sim *sim, float dt, int *shape);
+int sph_get_sweep_shape(sph_sim *sim, int *shape);
+int sph_set_sweep_shape(sph_sim *sim, const int *shape);
 
 /* ---- Viscoelastic springs (no reference counterpart) ----------------------
  * Springs with plasticity after Clavet et al. 2005 ("Particle-based

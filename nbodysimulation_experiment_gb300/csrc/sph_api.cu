@@ -96,6 +96,7 @@ struct sph_sim {
 	cudaStream_t stream = nullptr;
 	int numSMs = 0;
 	int viscBlocks = 0, deltaBlocks = 0, densBlocks = 0, gridBlocks = 0;
+	int viscLean = 0, deltaLean = 0;  // sweep shapes: 0 = wide (4 warps), 1 = lean (2 warps)
 	bool batch = false;
 	int multithreading = 0;
 
@@ -471,7 +472,7 @@ int enqueue_step(sph_sim *s, bool capturing) {
 		SPH_CUDA(cudaMemsetAsync(T.taskCounter, 0, sizeof(int), st));
 		SimTables v = T;
 		v.done = s->doneV;
-		k_viscosity<<<s->viscBlocks, kViscTaskWarps * kWarp, visc_smem_bytes(), st>>>(tt, A.view(), v);
+		launch_viscosity(s->viscLean, s->viscBlocks, st, tt, A.view(), v);
 		SPH_LAUNCHED(s);
 	}
 	SPH_CUDA(mark(kEvVisc));
@@ -518,7 +519,7 @@ int enqueue_step(sph_sim *s, bool capturing) {
 	{
 		SimTables d = T;
 		d.done = s->doneD;
-		k_delta<<<s->deltaBlocks, kDeltaTaskWarps * kWarp, delta_smem_bytes(), st>>>(tt, B.view(), d);
+		launch_delta(s->deltaLean, s->deltaBlocks, st, tt, B.view(), d);
 		SPH_LAUNCHED(s);
 	}
 	SPH_CUDA(mark(kEvDelta));
@@ -708,26 +709,16 @@ int allocate(sph_sim *s) {
 	cudaDeviceProp prop;
 	if (cudaGetDeviceProperties(&prop, s->device) != cudaSuccess) return SPH_ERR_CUDA;
 	s->numSMs = prop.multiProcessorCount;
-	if (cudaFuncSetAttribute(k_viscosity, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)visc_smem_bytes()) !=
-	        cudaSuccess ||
-	    cudaFuncSetAttribute(k_delta, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)delta_smem_bytes()) !=
-	        cudaSuccess ||
+	if (sweep_attributes() != cudaSuccess ||
 	    cudaFuncSetAttribute(k_density, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dens_smem_bytes()) !=
 	        cudaSuccess ||
 	    cudaFuncSetAttribute(k_springs_select, cudaFuncAttributeMaxDynamicSharedMemorySize,
 	                         (int)springs_smem_bytes()) != cudaSuccess)
 		return SPH_ERR_CUDA;
-	int occ = 0;
-	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_viscosity, kViscTaskWarps * kWarp, visc_smem_bytes()) !=
-	        cudaSuccess ||
-	    occ < 1)
-		return SPH_ERR_CUDA;
-	s->viscBlocks = occ * s->numSMs;
-	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_delta, kDeltaTaskWarps * kWarp, delta_smem_bytes()) !=
-	        cudaSuccess ||
-	    occ < 1)
-		return SPH_ERR_CUDA;
-	s->deltaBlocks = occ * s->numSMs;
+	int occV = 0, occD = 0;
+	if (sweep_occupancy(false, false, &occV, &occD) != cudaSuccess || occV < 1 || occD < 1) return SPH_ERR_CUDA;
+	s->viscBlocks = occV * s->numSMs;
+	s->deltaBlocks = occD * s->numSMs;
 	s->densBlocks = std::max(1, std::min(blocks_for(C, kDensWarps), 64 * s->numSMs));
 	s->springBlocks = std::max(1, std::min(blocks_for(C, kSpringWarps), 64 * s->numSMs));
 	s->gridBlocks = std::max(1, std::min(blocks_for(C, kGridWarps), 64 * s->numSMs));
@@ -1697,11 +1688,13 @@ int sph_load_springs(sph_sim *s, size_t count, const int32_t *spring_count, cons
 	return SPH_OK;
 }
 
-// Launch-shape autotuner: the ordered sweeps are persistent kernels whose
-// resident block count trades parallel tasks against polling traffic; every
-// count gives the same results (the task order fixes them), so each candidate
-// is timed on the same update from a snapshot, and the fastest kept.
-int sph_autotune(sph_sim *s, float dt, int *visc_blocks, int *delta_blocks) {
+// Launch-shape autotuner: the ordered sweeps are persistent kernels; each
+// has two shapes (wide: four warps per task; lean: two warps, more tasks per
+// SM) and a resident block count that trades parallel tasks against polling
+// traffic.  Every shape gives the same results (the task order fixes them),
+// so each candidate is timed on the same update from a snapshot and the
+// fastest kept for each sweep.
+int sph_autotune(sph_sim *s, float dt, int *shape) {
 	if (!s || !(dt > 0.0f)) return SPH_ERR_INVALID_ARGUMENT;
 	SPH_CUDA(cudaSetDevice(s->device));
 	int rc = flush_adds(s);
@@ -1711,50 +1704,97 @@ int sph_autotune(sph_sim *s, float dt, int *visc_blocks, int *delta_blocks) {
 	if (s->totalParticles() == 0) return SPH_ERR_NOT_SUPPORTED;
 	rc = ensure_learned(s);
 	if (rc) return rc;
-	int occV = 0, occD = 0;
-	SPH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occV, k_viscosity, kViscTaskWarps * kWarp,
-	                                                         visc_smem_bytes()));
-	SPH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occD, k_delta, kDeltaTaskWarps * kWarp,
-	                                                         delta_smem_bytes()));
 	const bool graphs = s->useGraphs;
 	s->useGraphs = false;
 	rc = copy_state(s, true);
 	if (rc) return rc;
-	float bestV = 1e30f, bestD = 1e30f;
-	int pickV = s->viscBlocks, pickD = s->deltaBlocks;
-	const int maxPer = std::max(occV, occD);
-	for (int per = 1; per <= maxPer && !rc; ++per) {
-		for (int rep = 0; rep < 2 && !rc; ++rep) {  // the first run of a shape warms it up
+	// Median of three timed updates per shape (after one warm-up update); the
+	// current shape is kept unless another is faster by more than 2%.
+	auto measure = [&](int vLean, int vBlocks, int dLean, int dBlocks, float *tv, float *td) -> int {
+		s->viscLean = vLean;
+		s->viscBlocks = vBlocks;
+		s->deltaLean = dLean;
+		s->deltaBlocks = dBlocks;
+		float v[3], d[3];
+		for (int rep = 0; rep < 4; ++rep) {
+			int r = copy_state(s, false);
+			if (!r) r = run_step(s, dt);
+			if (!r) r = check_device_errors(s);
+			if (r) return r;
+			if (rep == 0) continue;
+			SPH_CUDA(cudaEventElapsedTime(&v[rep - 1], s->ev[kEvIntegrate], s->ev[kEvVisc]));
+			SPH_CUDA(cudaEventElapsedTime(&d[rep - 1], s->ev[kEvDensity], s->ev[kEvDelta]));
+		}
+		std::sort(v, v + 3);
+		std::sort(d, d + 3);
+		*tv = v[1];
+		*td = d[1];
+		return SPH_OK;
+	};
+	int pick[4] = {s->viscLean, s->viscBlocks, s->deltaLean, s->deltaBlocks};
+	float bestV = 0.f, bestD = 0.f;
+	rc = measure(pick[0], pick[1], pick[2], pick[3], &bestV, &bestD);
+	for (int lean = 0; lean < 2 && !rc; ++lean) {
+		int occV = 0, occD = 0;
+		rc = cuda_status(sweep_occupancy(lean != 0, lean != 0, &occV, &occD));
+		const int maxPer = std::max(occV, occD);
+		for (int per = 1; per <= maxPer && !rc; ++per) {
 			const int vb = std::min(per, occV) * s->numSMs, db = std::min(per, occD) * s->numSMs;
-			s->viscBlocks = vb;
-			s->deltaBlocks = db;
-			rc = copy_state(s, false);
-			if (!rc) rc = run_step(s, dt);
-			if (!rc) rc = check_device_errors(s);
-			if (rc || rep == 0) continue;
 			float tv = 0.f, td = 0.f;
-			SPH_CUDA(cudaEventElapsedTime(&tv, s->ev[kEvIntegrate], s->ev[kEvVisc]));
-			SPH_CUDA(cudaEventElapsedTime(&td, s->ev[kEvDensity], s->ev[kEvDelta]));
-			if (tv < bestV) {
+			rc = measure(lean, vb, lean, db, &tv, &td);
+			if (rc) break;
+			if (tv < 0.98f * bestV) {
 				bestV = tv;
-				pickV = vb;
+				pick[0] = lean;
+				pick[1] = vb;
 			}
-			if (td < bestD) {
+			if (td < 0.98f * bestD) {
 				bestD = td;
-				pickD = db;
+				pick[2] = lean;
+				pick[3] = db;
 			}
 		}
 	}
 	if (!rc) rc = copy_state(s, false);
-	s->viscBlocks = pickV;
-	s->deltaBlocks = pickD;
+	s->viscLean = pick[0];
+	s->viscBlocks = pick[1];
+	s->deltaLean = pick[2];
+	s->deltaBlocks = pick[3];
 	s->useGraphs = graphs;
 	drop_graphs(s);
 	s->timed = false;
 	if (rc) return rc;
 	SPH_CUDA(cudaStreamSynchronize(s->stream));
-	if (visc_blocks) *visc_blocks = pickV;
-	if (delta_blocks) *delta_blocks = pickD;
+	if (shape) {
+		shape[0] = s->viscLean ? ViscLean::kWarps : ViscWide::kWarps;
+		shape[1] = s->viscBlocks;
+		shape[2] = s->deltaLean ? DeltaLean::kWarps : DeltaWide::kWarps;
+		shape[3] = s->deltaBlocks;
+	}
+	return SPH_OK;
+}
+
+int sph_get_sweep_shape(sph_sim *s, int *shape) {
+	if (!s || !shape) return SPH_ERR_INVALID_ARGUMENT;
+	shape[0] = s->viscLean ? ViscLean::kWarps : ViscWide::kWarps;
+	shape[1] = s->viscBlocks;
+	shape[2] = s->deltaLean ? DeltaLean::kWarps : DeltaWide::kWarps;
+	shape[3] = s->deltaBlocks;
+	return SPH_OK;
+}
+
+int sph_set_sweep_shape(sph_sim *s, const int *shape) {
+	if (!s || !shape) return SPH_ERR_INVALID_ARGUMENT;
+	const bool vOk = shape[0] == ViscLean::kWarps || shape[0] == ViscWide::kWarps;
+	const bool dOk = shape[2] == DeltaLean::kWarps || shape[2] == DeltaWide::kWarps;
+	if (!vOk || !dOk || shape[1] < 1 || shape[3] < 1 || shape[1] > (1 << 20) || shape[3] > (1 << 20))
+		return SPH_ERR_INVALID_ARGUMENT;
+	SPH_CUDA(cudaStreamSynchronize(s->stream));
+	s->viscLean = shape[0] == ViscLean::kWarps;
+	s->viscBlocks = shape[1];
+	s->deltaLean = shape[2] == DeltaLean::kWarps;
+	s->deltaBlocks = shape[3];
+	drop_graphs(s);
 	return SPH_OK;
 }
 

@@ -158,21 +158,22 @@ __global__ void k_integrate(Totals tt, Particles P, SimTables T) {
 // while warps 1..3 compute the compacted pair geometry of particle k+1
 // (positions do not change during this pass, so the geometry of every
 // particle of the task is known in advance).
-struct ViscSmem {
+// Two shapes (ViscWide, ViscLean in sph_kernels.cuh): the lean one uses two
+// warps and keeps the pair geometry of up to 256 pairs per particle (longer
+// lists run the geometry inline in the chain), so more tasks fit on an SM.
+template <class C>
+struct ViscSmemT {
 	float2 pos[kStageCap];
 	float2 vel[kStageCap];
-	int cslot[2][kStageCap];   // in-range pairs of a particle, list order
-	float2 cn[2][kStageCap];   // unit vector of the pair
-	float comq[2][kStageCap];  // 1 - q
+	int cslot[2][C::kGeom];   // in-range pairs of a particle, list order
+	float2 cn[2][C::kGeom];   // unit vector of the pair
+	float comq[2][C::kGeom];  // 1 - q
 	int m[2];
-	int warpCnt[2][kViscTaskWarps];
+	int warpCnt[2][C::kWarps];
 	int task;
 };
 
 namespace {
-
-constexpr int kVT = kViscTaskWarps * kWarp;  // threads per viscosity task
-constexpr int kVP = kVT - kWarp;             // producer threads (warps 1..)
 
 // Source index of flat position e of NSEG consecutive segments (segment s
 // starts at flat offset off[s] and at source index start[s]); selects only,
@@ -185,18 +186,20 @@ __device__ __forceinline__ int seg_src(int e, const int (&off)[NSEG], const int 
 	return src;
 }
 
+template <class C>
 __device__ __forceinline__ void producers_sync() {
-	asm volatile("bar.sync 1, %0;" ::"r"(kVP) : "memory");
+	asm volatile("bar.sync 1, %0;" ::"r"(C::kProducers) : "memory");
 }
 
 // Geometry of the particle at staged slot `slot` over the L staged entries
 // (its whole list): in-range pairs in list order with their unit vectors
 // and 1 - q (sph.h:497-505).  Run by the producer warps only.
-__device__ __forceinline__ void visc_geometry(ViscSmem &S, int buf, int slot, int L, const StepParams &s, int p) {
+template <class C>
+__device__ __forceinline__ void visc_geometry(ViscSmemT<C> &S, int buf, int slot, int L, const StepParams &s, int p) {
 	const int lane = p & (kWarp - 1), w = p / kWarp;
 	const float2 xi = S.pos[slot];
 	int m = 0, parity = 0;
-	for (int base = 0; base < L; base += kVP) {
+	for (int base = 0; base < L; base += C::kProducers) {
 		const int e = base + p;
 		bool in = false;
 		float rx = 0.f, ry = 0.f, r2 = 0.f;
@@ -209,16 +212,16 @@ __device__ __forceinline__ void visc_geometry(ViscSmem &S, int buf, int slot, in
 		}
 		const unsigned mask = __ballot_sync(kFull, in);
 		if (lane == 0) S.warpCnt[parity][w] = __popc(mask);
-		producers_sync();
+		producers_sync<C>();
 		int before = m, total = 0;
 #pragma unroll
-		for (int q = 0; q < kViscTaskWarps - 1; ++q) {
+		for (int q = 0; q < C::kWarps - 1; ++q) {
 			const int c = S.warpCnt[parity][q];
 			before += (q < w) ? c : 0;
 			total += c;
 		}
-		if (in) {
-			const int at = before + __popc(mask & lanemask_lt());
+		const int at = before + __popc(mask & lanemask_lt());
+		if (in && at < C::kGeom) {
 			const float r = sqrtf(r2);
 			const float qq = r * s.invH;
 			float len = r;  // Vec2Length(Rij) == rij
@@ -240,7 +243,8 @@ __device__ __forceinline__ void visc_geometry(ViscSmem &S, int buf, int slot, in
 // before this pair's store.  The impulse (f n * 0.5) * dt is computed as
 // (f n) * (0.5 dt): 0.5 dt is exact and halving is exact, so both round the
 // same real product once (unless |f n| < 2^-125).
-__device__ __forceinline__ void visc_pair(ViscSmem &S, int j, float2 n, float o, float2 vj, float2 &vi,
+template <class C>
+__device__ __forceinline__ void visc_pair(ViscSmemT<C> &S, int j, float2 n, float o, float2 vj, float2 &vi,
                                           const StepParams &s, float hdt) {
 	// Computed unconditionally and selected: only approaching pairs (u > 0)
 	// exchange an impulse.
@@ -254,10 +258,30 @@ __device__ __forceinline__ void visc_pair(ViscSmem &S, int j, float2 n, float o,
 	S.vel[j] = ap ? make_float2(ix + vj.x, iy + vj.y) : vj;
 }
 
-__device__ __forceinline__ void visc_chain(ViscSmem &S, int buf, int slot, const StepParams &s) {
+template <class C>
+__device__ __forceinline__ void visc_chain(ViscSmemT<C> &S, int buf, int slot, int L, const StepParams &s) {
 	const float hdt = 0.5f * s.dt;
 	const int m = S.m[buf];
 	float2 vi = S.vel[slot];
+	if (m > C::kGeom) {
+		// More in-range pairs than the geometry buffer holds: the same pair
+		// geometry (sph.h:497-505), computed here in list order.
+		const float2 xi = S.pos[slot];
+		for (int e = 0; e < L; ++e) {
+			const float2 xj = S.pos[e];
+			const float rx = xj.x - xi.x, ry = xj.y - xi.y;
+			const float r2 = rx * rx + ry * ry;
+			if (!(r2 < s.h2)) continue;
+			const float r = sqrtf(r2);
+			const float qq = r * s.invH;
+			float len = r;
+			if (len == 0.0f) len = 1.0f;
+			const float inv = 1.0f / len;
+			visc_pair(S, e, make_float2(rx * inv, ry * inv), 1.0f - qq, S.vel[e], vi, s, hdt);
+		}
+		S.vel[slot] = vi;
+		return;
+	}
 	int q = 0;
 	for (; q + 4 <= m; q += 4) {
 		int j[4];
@@ -283,9 +307,11 @@ __device__ __forceinline__ void visc_chain(ViscSmem &S, int buf, int slot, const
 
 }  // namespace
 
-__global__ void __launch_bounds__(kViscTaskWarps * kWarp, 4) k_viscosity(Totals tt, Particles P, SimTables T) {
+template <class C>
+__global__ void __launch_bounds__(C::kWarps * kWarp, C::kMinBlocks) k_viscosity(Totals tt, Particles P, SimTables T) {
+	constexpr int kVT = C::kWarps * kWarp;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
-	ViscSmem &S = *reinterpret_cast<ViscSmem *>(smem_raw);
+	ViscSmemT<C> &S = *reinterpret_cast<ViscSmemT<C> *>(smem_raw);
 	const int tid = threadIdx.x, warp = tid / kWarp;
 	for (;;) {
 		if (tid == 0) S.task = atomicAdd(&T.taskCounter[0], 1);
@@ -357,13 +383,13 @@ __global__ void __launch_bounds__(kViscTaskWarps * kWarp, 4) k_viscosity(Totals 
 				}
 				__syncthreads();
 				stamp(T, 0, t, 2, tid);
-				if (warp > 0) visc_geometry(S, 0, own, L, s, tid - kWarp);
+				if (warp > 0) visc_geometry<C>(S, 0, own, L, s, tid - kWarp);
 				__syncthreads();
 				for (int k = 0; k < cnt; ++k) {
 					if (warp == 0) {
-						if (tid == 0) visc_chain(S, k & 1, own + k, s);
+						if (tid == 0) visc_chain<C>(S, k & 1, own + k, L, s);
 					} else if (k + 1 < cnt) {
-						visc_geometry(S, (k + 1) & 1, own + k + 1, L, s, tid - kWarp);
+						visc_geometry<C>(S, (k + 1) & 1, own + k + 1, L, s, tid - kWarp);
 					}
 					__syncthreads();
 				}
@@ -785,23 +811,25 @@ __global__ void __launch_bounds__(kDensWarps * kWarp) k_density(Totals tt, Parti
 // task's region, and for each particle scans the list, compacts the in-range
 // pairs and evaluates them in parallel; one thread then adds the halves to
 // dx in list order.
-struct DeltaSmem {
-	float2 pos[kDeltaStageCap];
-	float4 cand[kDeltaChainCap];  // in-range candidates: slot, x_j.x, x_j.y, r2
-	float2 half[kDeltaChainCap];  // delta * 0.5 of the buffered pairs, list order
-	int pnc[kPrefetch];           // prefetched per particle: new cell,
-	int pjk[kPrefetch];           // new number,
-	float2 ppk[kPrefetch];        // pressure and near pressure
+// Two shapes (DeltaWide, DeltaLean in sph_kernels.cuh): the lean one uses two
+// warps and smaller staging and pair buffers (regions that do not fit are
+// staged per particle), so more tasks fit on an SM.
+template <class C>
+struct DeltaSmemT {
+	float2 pos[C::kStage];
+	float4 cand[C::kChain];  // in-range candidates: slot, x_j.x, x_j.y, r2
+	float2 half[C::kChain];  // delta * 0.5 of the buffered pairs, list order
+	int pnc[C::kPrefetch];   // prefetched per particle: new cell,
+	int pjk[C::kPrefetch];   // new number,
+	float2 ppk[C::kPrefetch];  // pressure and near pressure
 	int segOff[kRegionCells + 1];
 	int segStart[kRegionCells];
 	int owned[kRegionCells];
-	int warpCnt[2][kDeltaTaskWarps];
+	int warpCnt[2][C::kWarps];
 	int task;
 };
 
 namespace {
-
-constexpr int kDT = kDeltaTaskWarps * kWarp;  // threads per delta task
 
 struct Region {
 	int x0, y0, x1, y1, w, ncells, L;
@@ -810,8 +838,10 @@ struct Region {
 // Stage the new cells of [x0,x1]x[y0,y1] (row-major) from the positions in
 // new-number order, where each cell is a contiguous range.  Collective over
 // the block; returns false (uniformly) if the region does not fit.
-__device__ __forceinline__ bool stage_region(DeltaSmem &S, Region &R, const Particles &Q, const SimTables &T,
+template <class C>
+__device__ __forceinline__ bool stage_region(DeltaSmemT<C> &S, Region &R, const Particles &Q, const SimTables &T,
                                              const StepParams &s, int cellBase, int tid) {
+	constexpr int kDT = C::kWarps * kWarp;
 	R.w = R.x1 - R.x0 + 1;
 	R.ncells = R.w * (R.y1 - R.y0 + 1);
 	if (R.ncells > kRegionCells) return false;
@@ -843,7 +873,7 @@ __device__ __forceinline__ bool stage_region(DeltaSmem &S, Region &R, const Part
 	}
 	__syncthreads();
 	R.L = S.segOff[R.ncells];
-	if (R.L > kDeltaStageCap) return false;
+	if (R.L > C::kStage) return false;
 	for (int b0 = 0; b0 < R.L; b0 += 4 * kDT) {
 		float2 xp[4];
 #pragma unroll
@@ -868,7 +898,9 @@ __device__ __forceinline__ bool stage_region(DeltaSmem &S, Region &R, const Part
 	return true;
 }
 
-__device__ __forceinline__ void write_back_owned(DeltaSmem &S, const Region &R, const Particles &Q, int tid) {
+template <class C>
+__device__ __forceinline__ void write_back_owned(DeltaSmemT<C> &S, const Region &R, const Particles &Q, int tid) {
+	constexpr int kDT = C::kWarps * kWarp;
 	for (int q = 0; q < R.ncells; ++q) {
 		if (!S.owned[q]) continue;
 		const int off = S.segOff[q], nn = S.segOff[q + 1] - off, st = S.segStart[q];
@@ -881,8 +913,10 @@ __device__ __forceinline__ void write_back_owned(DeltaSmem &S, const Region &R, 
 // In the row-major staged region the three cells of one block row are
 // consecutive, so the particle's list (y-major, then x, then cell order) is
 // three contiguous ranges of staged slots.  Collective over the block.
-__device__ __forceinline__ void relax_particle(DeltaSmem &S, const Region &R, int nc, int jk, float2 pk,
+template <class C>
+__device__ __forceinline__ void relax_particle(DeltaSmemT<C> &S, const Region &R, int nc, int jk, float2 pk,
                                                const SimTables &T, const StepParams &s, int cellBase, int tid) {
+	constexpr int kDT = C::kWarps * kWarp;
 	const int lane = tid & (kWarp - 1), warp = tid / kWarp;
 	const int x = (nc - cellBase) % s.gx, y = (nc - cellBase) / s.gx;
 	const int xa = max(x - 1, 0), xb = min(x + 1, s.gx - 1);
@@ -941,7 +975,7 @@ __device__ __forceinline__ void relax_particle(DeltaSmem &S, const Region &R, in
 		__syncthreads();
 		int before = m, total = 0;
 #pragma unroll
-		for (int w = 0; w < kDeltaTaskWarps; ++w) {
+		for (int w = 0; w < C::kWarps; ++w) {
 			const int c = S.warpCnt[parity][w];
 			before += (w < warp) ? c : 0;
 			total += c;
@@ -953,7 +987,7 @@ __device__ __forceinline__ void relax_particle(DeltaSmem &S, const Region &R, in
 			    make_float4(__int_as_float(slot[1]), xj[1].x, xj[1].y, r2[1]);
 		m += total;
 		parity ^= 1;
-		if (m > kDeltaChainCap - 2 * kDT || b0 + 2 * kDT >= L) {
+		if (m > C::kChain - 2 * kDT || b0 + 2 * kDT >= L) {
 			__syncthreads();
 			for (int q = tid; q < m; q += kDT) {
 				const float4 cd = S.cand[q];
@@ -1002,17 +1036,19 @@ __device__ __forceinline__ void relax_particle(DeltaSmem &S, const Region &R, in
 // Process particles [p0, p1) (old numbers) in order: one staged region if
 // it fits, otherwise one 3x3 region per particle.  Per-particle inputs (new
 // cell, new number, pressure) are prefetched in chunks, off the serial path.
-__device__ __forceinline__ void relax_group(DeltaSmem &S, int p0, int p1, int bx0, int by0, int bx1, int by1,
+template <class C>
+__device__ __forceinline__ void relax_group(DeltaSmemT<C> &S, int p0, int p1, int bx0, int by0, int bx1, int by1,
                                             const Particles &Q, const SimTables &T, const StepParams &s,
                                             int cellBase, int tid) {
+	constexpr int kDT = C::kWarps * kWarp;
 	Region R;
 	R.x0 = max(bx0 - 1, 0);
 	R.y0 = max(by0 - 1, 0);
 	R.x1 = min(bx1 + 1, s.gx - 1);
 	R.y1 = min(by1 + 1, s.gy - 1);
-	const bool staged = stage_region(S, R, Q, T, s, cellBase, tid);
-	for (int c0 = p0; c0 < p1; c0 += kPrefetch) {
-		const int c1 = min(p1, c0 + kPrefetch);
+	const bool staged = stage_region<C>(S, R, Q, T, s, cellBase, tid);
+	for (int c0 = p0; c0 < p1; c0 += C::kPrefetch) {
+		const int c1 = min(p1, c0 + C::kPrefetch);
 		for (int k = c0 + tid; k < c1; k += kDT) {
 			const int jk = T.newLabel[k];
 			S.pnc[k - c0] = T.newCell[k];
@@ -1024,7 +1060,7 @@ __device__ __forceinline__ void relax_group(DeltaSmem &S, int p0, int p1, int bx
 			const int nc = S.pnc[k - c0], jk = S.pjk[k - c0];
 			const float2 pk = S.ppk[k - c0];
 			if (staged) {
-				relax_particle(S, R, nc, jk, pk, T, s, cellBase, tid);
+				relax_particle<C>(S, R, nc, jk, pk, T, s, cellBase, tid);
 				continue;
 			}
 			Region R1;
@@ -1033,24 +1069,25 @@ __device__ __forceinline__ void relax_group(DeltaSmem &S, int p0, int p1, int bx
 			R1.y0 = max(y - 1, 0);
 			R1.x1 = min(x + 1, s.gx - 1);
 			R1.y1 = min(y + 1, s.gy - 1);
-			if (!stage_region(S, R1, Q, T, s, cellBase, tid)) {
+			if (!stage_region<C>(S, R1, Q, T, s, cellBase, tid)) {
 				if (tid == 0) atomicOr(T.error, kErrStageOverflow);
 				__syncthreads();
 				continue;
 			}
-			relax_particle(S, R1, nc, jk, pk, T, s, cellBase, tid);
-			write_back_owned(S, R1, Q, tid);
+			relax_particle<C>(S, R1, nc, jk, pk, T, s, cellBase, tid);
+			write_back_owned<C>(S, R1, Q, tid);
 			__syncthreads();
 		}
 		__syncthreads();
 	}
-	if (staged) write_back_owned(S, R, Q, tid);
+	if (staged) write_back_owned<C>(S, R, Q, tid);
 }
 
 // Wait for canonical tasks of the scene (old cells) near [bx0,bx1]x[by0,by1]
 // whose new-cell bounding boxes come within two cells of it and whose task
 // index is below `limit`.  Collective over the block; waits are converged
 // per warp.
+template <int kDT>
 __device__ __forceinline__ void wait_canonical(int bx0, int by0, int bx1, int by1, int moveMax, int limit,
                                                int selfCell, const SimTables &T, const StepParams &s,
                                                int cellBase, int tid) {
@@ -1077,9 +1114,11 @@ __device__ __forceinline__ void wait_canonical(int bx0, int by0, int bx1, int by
 
 }  // namespace
 
-__global__ void __launch_bounds__(kDeltaTaskWarps * kWarp, 4) k_delta(Totals tt, Particles Q, SimTables T) {
+template <class C>
+__global__ void __launch_bounds__(C::kWarps * kWarp, C::kMinBlocks) k_delta(Totals tt, Particles Q, SimTables T) {
+	constexpr int kDT = C::kWarps * kWarp;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
-	DeltaSmem &S = *reinterpret_cast<DeltaSmem *>(smem_raw);
+	DeltaSmemT<C> &S = *reinterpret_cast<DeltaSmemT<C> *>(smem_raw);
 	const int tid = threadIdx.x;
 	const int ntask = tt.ncell + tt.nApp;
 	const int moveMax = T.moverCount[1];
@@ -1097,9 +1136,9 @@ __global__ void __launch_bounds__(kDeltaTaskWarps * kWarp, 4) k_delta(Totals tt,
 				const SceneDev &sc = T.scenes[T.sceneOfCell[c]];
 				const StepParams s = sc.p;
 				const int4 b = *reinterpret_cast<const int4 *>(&T.bbox[4 * c]);
-				wait_canonical(b.x, b.y, b.z, b.w, moveMax, t, c, T, s, sc.cellBase, tid);
+				wait_canonical<kDT>(b.x, b.y, b.z, b.w, moveMax, t, c, T, s, sc.cellBase, tid);
 				stamp(T, 1, t, 1, tid);
-				relax_group(S, p0, p0 + cnt, b.x, b.y, b.z, b.w, Q, T, s, sc.cellBase, tid);
+				relax_group<C>(S, p0, p0 + cnt, b.x, b.y, b.z, b.w, Q, T, s, sc.cellBase, tid);
 				__syncthreads();
 				__threadfence();
 			}
@@ -1143,10 +1182,10 @@ __global__ void __launch_bounds__(kDeltaTaskWarps * kWarp, 4) k_delta(Totals tt,
 			bx1 = S.warpCnt[1][0];
 			by1 = S.warpCnt[1][1];
 			__syncthreads();
-			wait_canonical(bx0, by0, bx1, by1, moveMax, tt.ncell, -1, T, s, base, tid);
+			wait_canonical<kDT>(bx0, by0, bx1, by1, moveMax, tt.ncell, -1, T, s, base, tid);
 			if (tid < kWarp) warp_wait(tid == 0 && prev >= 0 ? &T.done[prev] : nullptr, T.abort, T.error);
 			__syncthreads();
-			relax_group(S, p0, p1, bx0, by0, bx1, by1, Q, T, s, base, tid);
+			relax_group<C>(S, p0, p1, bx0, by0, bx1, by1, Q, T, s, base, tid);
 			__syncthreads();
 			__threadfence();
 		}
@@ -1385,8 +1424,56 @@ __global__ void k_gather_by_id(int first, int count, const int *id, const float2
 	if (k >= 0 && k < count) dst[k] = src[first + j];
 }
 
-size_t visc_smem_bytes() { return sizeof(ViscSmem); }
-size_t delta_smem_bytes() { return sizeof(DeltaSmem); }
+template <class C>
+size_t visc_smem_bytes() {
+	return sizeof(ViscSmemT<C>);
+}
+template <class C>
+size_t delta_smem_bytes() {
+	return sizeof(DeltaSmemT<C>);
+}
+cudaError_t sweep_attributes() {
+	cudaError_t e = cudaFuncSetAttribute(k_viscosity<ViscWide>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+	                                     (int)visc_smem_bytes<ViscWide>());
+	if (e == cudaSuccess)
+		e = cudaFuncSetAttribute(k_viscosity<ViscLean>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                         (int)visc_smem_bytes<ViscLean>());
+	if (e == cudaSuccess)
+		e = cudaFuncSetAttribute(k_delta<DeltaWide>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                         (int)delta_smem_bytes<DeltaWide>());
+	if (e == cudaSuccess)
+		e = cudaFuncSetAttribute(k_delta<DeltaLean>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                         (int)delta_smem_bytes<DeltaLean>());
+	return e;
+}
+
+cudaError_t sweep_occupancy(bool viscLean, bool deltaLean, int *occV, int *occD) {
+	cudaError_t e = viscLean ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(occV, k_viscosity<ViscLean>,
+	                                                                         ViscLean::kWarps * kWarp,
+	                                                                         visc_smem_bytes<ViscLean>())
+	                         : cudaOccupancyMaxActiveBlocksPerMultiprocessor(occV, k_viscosity<ViscWide>,
+	                                                                         ViscWide::kWarps * kWarp,
+	                                                                         visc_smem_bytes<ViscWide>());
+	if (e != cudaSuccess) return e;
+	return deltaLean ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(occD, k_delta<DeltaLean>, DeltaLean::kWarps * kWarp,
+	                                                                 delta_smem_bytes<DeltaLean>())
+	                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(occD, k_delta<DeltaWide>, DeltaWide::kWarps * kWarp,
+	                                                                 delta_smem_bytes<DeltaWide>());
+}
+
+void launch_viscosity(bool lean, int blocks, cudaStream_t st, Totals tt, Particles P, SimTables T) {
+	if (lean)
+		k_viscosity<ViscLean><<<blocks, ViscLean::kWarps * kWarp, visc_smem_bytes<ViscLean>(), st>>>(tt, P, T);
+	else
+		k_viscosity<ViscWide><<<blocks, ViscWide::kWarps * kWarp, visc_smem_bytes<ViscWide>(), st>>>(tt, P, T);
+}
+
+void launch_delta(bool lean, int blocks, cudaStream_t st, Totals tt, Particles Q, SimTables T) {
+	if (lean)
+		k_delta<DeltaLean><<<blocks, DeltaLean::kWarps * kWarp, delta_smem_bytes<DeltaLean>(), st>>>(tt, Q, T);
+	else
+		k_delta<DeltaWide><<<blocks, DeltaWide::kWarps * kWarp, delta_smem_bytes<DeltaWide>(), st>>>(tt, Q, T);
+}
 size_t dens_smem_bytes() { return sizeof(DensWarp) * kDensWarps; }
 
 }  // namespace sphgb

@@ -5,8 +5,23 @@
 
 namespace sphgb {
 
-constexpr int kViscTaskWarps = 4;   // warps cooperating on one viscosity task (one task per block)
-constexpr int kDeltaTaskWarps = 4;  // warps cooperating on one delta task (one task per block)
+// Shapes of the two ordered sweeps (one task per block).  Wide: four warps
+// per task, buffers for the largest lists the reference accepts (short
+// critical path for one scene).  Lean: two warps and smaller buffers (more
+// tasks per SM for many scenes).  Results do not depend on the shape.
+struct ViscWide {
+	static constexpr int kWarps = 4, kProducers = 3 * kWarp, kGeom = kStageCap, kMinBlocks = 4;
+};
+struct ViscLean {
+	static constexpr int kWarps = 2, kProducers = kWarp, kGeom = 256, kMinBlocks = 8;
+};
+struct DeltaWide {
+	static constexpr int kWarps = 4, kStage = kDeltaStageCap, kChain = kDeltaChainCap, kPrefetch = 128,
+	                     kMinBlocks = 4;
+};
+struct DeltaLean {
+	static constexpr int kWarps = 2, kStage = 1536, kChain = 256, kPrefetch = 64, kMinBlocks = 8;
+};
 constexpr int kDensWarps = 8;
 constexpr int kGridWarps = 4;
 constexpr int kScanThreads = 1024;
@@ -15,17 +30,17 @@ constexpr int kElemThreads = 256;  // elementwise kernels
 constexpr int kCollideThreads = 256;
 constexpr int kSpringWarps = 4;
 
-struct ViscSmem;
-struct DeltaSmem;
 struct DensWarp;
 
-size_t visc_smem_bytes();
-size_t delta_smem_bytes();
+// The two ordered sweeps in a chosen shape (lean or wide), and their set-up.
+cudaError_t sweep_attributes();
+cudaError_t sweep_occupancy(bool viscLean, bool deltaLean, int *occV, int *occD);
+void launch_viscosity(bool lean, int blocks, cudaStream_t st, Totals tt, Particles P, SimTables T);
+void launch_delta(bool lean, int blocks, cudaStream_t st, Totals tt, Particles Q, SimTables T);
 size_t dens_smem_bytes();
 size_t springs_smem_bytes();
 
 __global__ void k_integrate(Totals tt, Particles P, SimTables T);
-__global__ void k_viscosity(Totals tt, Particles P, SimTables T);
 __global__ void k_predict(Totals tt, Particles P, SimTables T);
 __global__ void k_scan_reduce(Totals tt, SimTables T);
 __global__ void k_scan_tiles(Totals tt, SimTables T, int ntiles);
@@ -33,7 +48,6 @@ __global__ void k_scan_apply(Totals tt, SimTables T);
 __global__ void k_scatter(Totals tt, Particles P, SimTables T);
 __global__ void k_grid_update(Totals tt, Particles P, Particles Q, SimTables T);
 __global__ void k_density(Totals tt, Particles Q, SimTables T);
-__global__ void k_delta(Totals tt, Particles Q, SimTables T);
 __global__ void k_collide(Totals tt, Particles P, Particles Q, SimTables T);
 __global__ void k_add(int first, int count, int scene, int firstId, const float2 *pos, const float2 *force,
                       Particles P, SimTables T);

@@ -50,6 +50,18 @@ __device__ __forceinline__ int seg_number(int e, const int (&off)[NSEG], const i
 	return src;
 }
 
+// Staged index of number `num` in the 3x3 block (segments of consecutive
+// numbers), or -1 if it lies outside the block.
+__device__ __forceinline__ int staged_index(int num, const int (&off)[9], const int (&start)[9], int L) {
+	int e = -1;
+#pragma unroll
+	for (int q = 0; q < 9; ++q) {
+		const int len = (q < 8 ? off[q + 1] : L) - off[q];
+		if (num >= start[q] && num < start[q] + len) e = off[q] + (num - start[q]);
+	}
+	return e;
+}
+
 }  // namespace
 
 // One warp per new cell: the 3x3 block of new cells (positions, numbers'
@@ -65,6 +77,7 @@ struct SpringWarp {
 	float kr2[kSprings][kWarp];  // chosen candidates, sorted
 	int ktag[kSprings][kWarp];
 	int kj[kSprings][kWarp];
+	uint32_t exbits[kStageCap / 32][kWarp];  // per lane: staged entries that are existing partners
 };
 
 size_t springs_smem_bytes() { return sizeof(SpringWarp) * kSpringWarps; }
@@ -74,6 +87,7 @@ __global__ void __launch_bounds__(kSpringWarps * kWarp) k_springs_select(Totals 
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	SpringWarp &S = reinterpret_cast<SpringWarp *>(smem_raw)[threadIdx.x / kWarp];
 	const int lane = threadIdx.x & (kWarp - 1);
+	for (int w = 0; w < kStageCap / 32; ++w) S.exbits[w][lane] = 0u;
 	const int warpsTotal = gridDim.x * kSpringWarps;
 	for (int c = blockIdx.x * kSpringWarps + threadIdx.x / kWarp; c < tt.ncell; c += warpsTotal) {
 		const int cnt = T.newCount[c];
@@ -126,7 +140,9 @@ __global__ void __launch_bounds__(kSpringWarps * kWarp) k_springs_select(Totals 
 				for (int q = 0; q < ne; ++q) {
 					const int pn = T.newLabel[P.springP[o * kSprings + q]];
 					float rest = P.springL[o * kSprings + q];
-					S.ex[q][lane] = pn;
+					const int e = staged_index(pn, segOff, segStart, L);
+					S.ex[q][lane] = e;
+					if (e >= 0) S.exbits[e >> 5][lane] |= 1u << (e & 31);
 					const float2 xp = Q.pos[pn];
 					const float rx = xp.x - xi.x, ry = xp.y - xi.y;
 					const float r2 = rx * rx + ry * ry;
@@ -139,17 +155,18 @@ __global__ void __launch_bounds__(kSpringWarps * kWarp) k_springs_select(Totals 
 				}
 				freeSlots = s.springMax - m;
 			}
-			// Candidates: every list member in range without a spring.
-			for (int e = 0; e < L; ++e) {
+			// Candidates: every list member in range without a spring (the
+			// warp skips the scan when no lane has a free slot).
+			const bool scan = active && freeSlots > 0;
+			const int scanLen = __any_sync(kFullMask, scan) ? L : 0;
+			for (int e = 0; e < scanLen; ++e) {
 				const int num = seg_number<9>(e, segOff, segStart);
 				const float2 xj = S.pos[e];
-				if (!active || freeSlots <= 0 || num == j) continue;
+				if (!scan || num == j) continue;
 				const float rx = xj.x - xi.x, ry = xj.y - xi.y;
 				const float r2 = rx * rx + ry * ry;
 				if (!(r2 < s.h2)) continue;
-				bool has = false;
-				for (int q = 0; q < ne; ++q) has = has || S.ex[q][lane] == num;
-				if (has) continue;
+				if ((S.exbits[e >> 5][lane] >> (e & 31)) & 1u) continue;
 				const int tj = S.tag[e];
 				if (kc == freeSlots && !before(r2, tj, S.kr2[kc - 1][lane], S.ktag[kc - 1][lane])) continue;
 				int at = kc < freeSlots ? kc++ : kc - 1;
@@ -167,6 +184,10 @@ __global__ void __launch_bounds__(kSpringWarps * kWarp) k_springs_select(Totals 
 				T.accN[j] = kc;
 				for (int q = 0; q < kc; ++q) T.accP[j * kSprings + q] = S.kj[q][lane];
 				Q.springN[j] = m;
+				for (int q = 0; q < ne; ++q) {
+					const int e = S.ex[q][lane];
+					if (e >= 0) S.exbits[e >> 5][lane] = 0u;  // words touched by this particle
+				}
 			}
 			__syncwarp();
 		}

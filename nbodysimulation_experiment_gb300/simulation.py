@@ -189,7 +189,9 @@ def load_library(build_if_missing: bool = True):
         "sph_synchronize": [vp],
         "sph_kernel_launches": [vp, P(_c.c_uint64)],
         "sph_use_graphs": [vp, _c.c_int],
-        "sph_autotune": [vp, _c.c_float, P(_c.c_int), P(_c.c_int)],
+        "sph_autotune": [vp, _c.c_float, vp],
+        "sph_get_sweep_shape": [vp, vp],
+        "sph_set_sweep_shape": [vp, vp],
         "sph_set_springs": [vp, P(SpringParams)],
         "sph_get_spring_count": [vp, P(_c.c_uint64)],
         "sph_dump_springs": [vp, _c.c_size_t, vp, vp, vp],
@@ -238,7 +240,7 @@ C_SYMBOLS = (
     "sph_set_multithreading", "sph_is_multithreading_supported", "sph_is_multithreading",
     "sph_get_worker_thread_count", "sph_read_particles", "sph_state_info", "sph_dump_state", "sph_load_state",
     "sph_get_stream", "sph_device_arrays", "sph_synchronize", "sph_kernel_launches",
-    "sph_use_graphs", "sph_autotune", "sph_set_springs", "sph_get_spring_count", "sph_dump_springs", "sph_load_springs",
+    "sph_use_graphs", "sph_autotune", "sph_get_sweep_shape", "sph_set_sweep_shape", "sph_set_springs", "sph_get_spring_count", "sph_dump_springs", "sph_load_springs",
     "sph_mpnn_create", "sph_mpnn_destroy", "sph_mpnn_param_count", "sph_mpnn_get_params", "sph_mpnn_set_params",
     "sph_mpnn_capture", "sph_mpnn_sample_count", "sph_mpnn_clear_samples", "sph_mpnn_sample_info",
     "sph_mpnn_read_sample", "sph_mpnn_eval", "sph_mpnn_gradient", "sph_mpnn_train_step", "sph_learned_frame",
@@ -465,11 +467,21 @@ class Simulation:
         """Replay repeated updates from a per-step CUDA graph (default on)."""
         self._call("sph_use_graphs", 1 if enable else 0)
 
-    def autotune(self, delta_time: float) -> Tuple[int, int]:
-        """Pick the sweeps' resident block counts by timing (state kept)."""
-        v, d = _c.c_int(), _c.c_int()
-        self._call("sph_autotune", float(np.float32(delta_time)), _c.byref(v), _c.byref(d))
-        return v.value, d.value
+    def autotune(self, delta_time: float) -> Tuple[int, int, int, int]:
+        """Pick the sweeps' launch shapes by timing (state kept); returns
+        (viscosity warps, viscosity blocks, delta warps, delta blocks)."""
+        shape = np.zeros(4, np.int32)
+        self._call("sph_autotune", float(np.float32(delta_time)), shape.ctypes.data)
+        return tuple(int(v) for v in shape)
+
+    def sweep_shape(self) -> Tuple[int, int, int, int]:
+        shape = np.zeros(4, np.int32)
+        self._call("sph_get_sweep_shape", shape.ctypes.data)
+        return tuple(int(v) for v in shape)
+
+    def set_sweep_shape(self, shape) -> None:
+        a = np.ascontiguousarray(shape, np.int32)
+        self._call("sph_set_sweep_shape", a.ctypes.data)
 
     # --- viscoelastic springs (no reference counterpart) ----------------------
     def set_springs(self, enabled: bool = True, yield_ratio: float = 0.1, plasticity: float = 0.3,
@@ -638,11 +650,21 @@ class BatchSimulation:
         """Replay repeated updates from a per-step CUDA graph (default on)."""
         self._call("sph_use_graphs", 1 if enable else 0)
 
-    def autotune(self, delta_time: float) -> Tuple[int, int]:
-        """Pick the sweeps' resident block counts by timing (state kept)."""
-        v, d = _c.c_int(), _c.c_int()
-        self._call("sph_autotune", float(np.float32(delta_time)), _c.byref(v), _c.byref(d))
-        return v.value, d.value
+    def autotune(self, delta_time: float) -> Tuple[int, int, int, int]:
+        """Pick the sweeps' launch shapes by timing (state kept); returns
+        (viscosity warps, viscosity blocks, delta warps, delta blocks)."""
+        shape = np.zeros(4, np.int32)
+        self._call("sph_autotune", float(np.float32(delta_time)), shape.ctypes.data)
+        return tuple(int(v) for v in shape)
+
+    def sweep_shape(self) -> Tuple[int, int, int, int]:
+        shape = np.zeros(4, np.int32)
+        self._call("sph_get_sweep_shape", shape.ctypes.data)
+        return tuple(int(v) for v in shape)
+
+    def set_sweep_shape(self, shape) -> None:
+        a = np.ascontiguousarray(shape, np.int32)
+        self._call("sph_set_sweep_shape", a.ctypes.data)
 
 
 class Mpnn:

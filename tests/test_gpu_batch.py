@@ -137,11 +137,49 @@ def test_autotune_keeps_results_and_state():
         batch = pkg.BatchSimulation(mix)
         batch.update(float(scenes.DT))
         if tune:
-            v, d = batch.autotune(float(scenes.DT))
-            assert v > 0 and d > 0
+            shape = batch.autotune(float(scenes.DT))
+            assert shape[0] in (2, 4) and shape[2] in (2, 4) and shape[1] > 0 and shape[3] > 0
         for _ in range(10):
             batch.update(float(scenes.DT))
         runs.append([batch.dump_state(k) for k in range(len(mix))])
         batch.close()
     for a, b in zip(*runs):
         _assert_same_state(a, b, "autotune")
+
+
+def _run_with_shape(scene, shape, steps):
+    sim = pkg.Simulation(scene.domain())
+    scene.apply(sim)
+    sim.update(float(scenes.DT))
+    if shape is not None:
+        base = sim.sweep_shape()
+        sim.set_sweep_shape((shape[0], base[1] if shape[1] is None else shape[1],
+                             shape[2], base[3] if shape[3] is None else shape[3]))
+    for _ in range(steps):
+        sim.update(float(scenes.DT))
+    st = sim.dump_state()
+    sim.close()
+    return st
+
+
+@pytest.mark.parametrize("shape", [(2, None, 2, None), (2, 152, 4, 152), (4, 152 * 3, 2, 152 * 5)])
+def test_sweep_shapes_give_identical_results(shape):
+    """Lean (2-warp) and wide (4-warp) sweeps, with any resident block count,
+    compute the same update."""
+    scene = scenes.scaled_block(64, seed=13)
+    want = _run_with_shape(scene, None, 12)
+    got = _run_with_shape(scene, shape, 12)
+    _assert_same_state(got, want, str(shape))
+
+
+def test_lean_viscosity_with_long_pair_lists():
+    """Particles with more in-range pairs than the lean sweep's geometry
+    buffer (spacing h/10: ~300 pairs) take the inline path, with the same
+    result."""
+    h = float(scenes.H)
+    pos = scenes.jittered_lattice(28, 28, -1.4, -2.5, spacing=h / 10, jitter=h / 200, seed=3)
+    scene = scenes.Scene("dense", scenes.REF_WIDTH, scenes.REF_HEIGHT, pos,
+                         scenes.box_planes(scenes.REF_WIDTH, scenes.REF_HEIGHT))
+    want = _run_with_shape(scene, None, 6)
+    got = _run_with_shape(scene, (2, None, 2, None), 6)
+    _assert_same_state(got, want, "dense")
