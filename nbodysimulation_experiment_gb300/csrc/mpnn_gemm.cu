@@ -151,21 +151,50 @@ __device__ __forceinline__ void epilogue(const GemmArgs &g, uint32_t tmem, int r
 		    : "memory");
 		asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 		if (row >= g.M) continue;
+		// N is a multiple of 16, so all 16 columns exist.
+		float x[16];
+		const float rs = g.rowScale ? g.rowScale[row] : 0.0f;
 #pragma unroll
 		for (int u = 0; u < 16; ++u) {
 			const int col = c0 + u;
-			if (col >= g.N) break;
-			float x = __uint_as_float(v[u]);
-			if (g.bias) x += g.bias[col];
-			if (g.rowScale) x += g.rowScale[row] * g.bias2[col];
-			if (g.relu) x = fmaxf(x, 0.0f);
-			if (g.C) {
-				float *dst = g.C + (size_t)row * g.ldc + col;
-				if (g.accumulate) atomicAdd(dst, x);
-				else *dst = x;
+			x[u] = __uint_as_float(v[u]);
+			if (g.bias) x[u] += g.bias[col];
+			if (g.rowScale) x[u] += rs * g.bias2[col];
+			if (g.relu) x[u] = fmaxf(x[u], 0.0f);
+		}
+		if (g.C) {
+			float *dst = g.C + (size_t)row * g.ldc + c0;
+			if (g.accumulate) {
+#pragma unroll
+				for (int u = 0; u < 16; ++u) atomicAdd(dst + u, x[u]);
+			} else if ((g.ldc & 3) == 0 && (reinterpret_cast<uintptr_t>(g.C) & 15) == 0) {
+#pragma unroll
+				for (int u = 0; u < 16; u += 4)
+					*reinterpret_cast<float4 *>(dst + u) = make_float4(x[u], x[u + 1], x[u + 2], x[u + 3]);
+			} else {
+#pragma unroll
+				for (int u = 0; u < 16; ++u) dst[u] = x[u];
 			}
-			if (g.Cb) g.Cb[(size_t)row * g.ldcb + col] = __float2bfloat16_rn(x);
-			if (g.CbT) g.CbT[(size_t)col * g.ldcbT + row] = __float2bfloat16_rn(x);
+		}
+		if (g.Cb) {
+			__nv_bfloat16 *dst = g.Cb + (size_t)row * g.ldcb + c0;
+			if ((g.ldcb & 7) == 0 && (reinterpret_cast<uintptr_t>(g.Cb) & 15) == 0) {
+#pragma unroll
+				for (int u = 0; u < 16; u += 8) {
+					uint4 pk;
+					__nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(&pk);
+#pragma unroll
+					for (int w = 0; w < 4; ++w) h[w] = __floats2bfloat162_rn(x[u + 2 * w], x[u + 2 * w + 1]);
+					*reinterpret_cast<uint4 *>(dst + u) = pk;
+				}
+			} else {
+#pragma unroll
+				for (int u = 0; u < 16; ++u) dst[u] = __float2bfloat16_rn(x[u]);
+			}
+		}
+		if (g.CbT) {
+#pragma unroll
+			for (int u = 0; u < 16; ++u) g.CbT[(size_t)(c0 + u) * g.ldcbT + row] = __float2bfloat16_rn(x[u]);
 		}
 	}
 }

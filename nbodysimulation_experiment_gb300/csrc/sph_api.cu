@@ -413,11 +413,12 @@ int check_device_errors(sph_sim *s) {
 
 // Appendix runs (particles added since the last update, kAppendixRun at a
 // time) of every scene as delta-sweep tasks after the canonical ones,
-// interleaved across scenes; each run waits for the previous run of its
-// scene, so a scene's appendix is relaxed in AddParticle order.
+// interleaved across scenes.  A run waits for the earlier runs of its scene
+// whose particles' new cells come within two cells of its own, so a scene's
+// appendix is relaxed as in AddParticle order.
 int upload_appendix_tasks(sph_sim *s) {
 	const size_t S = s->scenes.size();
-	std::vector<int> runs(S), lastTask(S, -1);
+	std::vector<int> runs(S);
 	int maxRuns = 0;
 	for (size_t k = 0; k < S; ++k) {
 		const Scene &sc = s->scenes[k];
@@ -426,14 +427,12 @@ int upload_appendix_tasks(sph_sim *s) {
 	}
 	s->nApp = 0;
 	if (maxRuns == 0) return SPH_OK;
-	std::vector<int> scene, run, prev;
+	std::vector<int> scene, run;
 	for (int r = 0; r < maxRuns; ++r) {
 		for (size_t k = 0; k < S; ++k) {
 			if (r >= runs[k]) continue;
 			scene.push_back((int)k);
 			run.push_back(r);
-			prev.push_back(lastTask[k]);
-			lastTask[k] = s->ncellTotal + (int)scene.size() - 1;
 		}
 	}
 	if ((size_t)s->ncellTotal + scene.size() > s->doneDCap) return SPH_ERR_CAPACITY;
@@ -441,7 +440,6 @@ int upload_appendix_tasks(sph_sim *s) {
 	const size_t bytes = scene.size() * sizeof(int);
 	SPH_CUDA(cudaMemcpyAsync(s->T.appScene, scene.data(), bytes, cudaMemcpyHostToDevice, s->stream));
 	SPH_CUDA(cudaMemcpyAsync(s->T.appRun, run.data(), bytes, cudaMemcpyHostToDevice, s->stream));
-	SPH_CUDA(cudaMemcpyAsync(s->T.appPrev, prev.data(), bytes, cudaMemcpyHostToDevice, s->stream));
 	return SPH_OK;
 }
 
@@ -514,6 +512,10 @@ int enqueue_step(sph_sim *s, bool capturing) {
 	SPH_LAUNCHED(s);
 	SPH_CUDA(mark(kEvDensity));
 
+	if (tt.nApp > 0) {
+		k_app_boxes<<<blocks_for((size_t)tt.nApp * kWarp, kElemThreads), kElemThreads, 0, st>>>(tt, T);
+		SPH_LAUNCHED(s);
+	}
 	SPH_CUDA(cudaMemsetAsync(s->doneD, 0, sizeof(uint32_t) * (s->ncellTotal + s->nApp), st));
 	SPH_CUDA(cudaMemsetAsync(T.taskCounter + 1, 0, sizeof(int), st));
 	{
@@ -655,7 +657,7 @@ int allocate(sph_sim *s) {
 	const size_t appCap = (N + kAppendixRun - 1) / kAppendixRun + S + 1;
 	s->doneDCap = C + appCap;
 	if ((rc = dalloc(&s->doneD, s->doneDCap)) || (rc = dalloc(&T.appScene, appCap)) ||
-	    (rc = dalloc(&T.appRun, appCap)) || (rc = dalloc(&T.appPrev, appCap)))
+	    (rc = dalloc(&T.appRun, appCap)) || (rc = dalloc(&T.appBox, 4 * appCap)))
 		return rc;
 	T.moverList = nullptr;
 
@@ -1195,7 +1197,7 @@ int sph_destroy(sph_sim *s) {
 	SimTables &T = s->T;
 	void *ptrs[] = {s->cellStartA, s->cellCountA, s->cellStartB, s->cellCountB, T.taskOfCell,  T.taskCell,
 	                T.numberOrder, T.sceneOfCell, T.sceneOf,     T.scenes,      T.appScene,    T.appRun,
-	                T.appPrev,     T.appCount,    T.appStart,    T.appIdx,      T.appCursor,   T.newCell,
+	                T.appBox,      T.appCount,    T.appStart,    T.appIdx,      T.appCursor,   T.newCell,
 	                T.enterCount,  T.leaveCount,  T.enterOffset, T.enterCursor, T.enterList,   T.moverCount,
 	                T.bbox,        T.newIdx,      T.newLabel,    T.taskCounter, T.stats,       T.error,
 	                T.scanTiles,

@@ -123,7 +123,8 @@ struct SimTables {
 	int *numberOrder;                  // global cells in numbering order (scene-major, colour rank)
 	int *sceneOfCell, *sceneOf;        // scene of a global cell / of a particle number
 	SceneDev *scenes;
-	int *appScene, *appRun, *appPrev;  // appendix run tasks: scene, run, previous task of the scene (-1)
+	int *appScene, *appRun;            // appendix run tasks: scene, run within the scene
+	int *appBox;                       // per appendix run: x0, y0, x1, y1 of its particles' new cells
 	int *appCount, *appStart, *appIdx, *appCursor;  // appendix members per cell
 	int *newCell;                      // cell after predict, per particle
 	int *enterCount, *leaveCount, *enterOffset, *enterCursor, *enterList;

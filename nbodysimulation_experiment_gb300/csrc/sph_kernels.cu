@@ -714,6 +714,33 @@ __global__ void __launch_bounds__(kGridWarps * kWarp) k_grid_update(Totals tt, P
 	}
 }
 
+// Bounding box (scene-local cell coordinates) of the new cells of each
+// appendix run; one warp per run.
+__global__ void k_app_boxes(Totals tt, SimTables T) {
+	const int a = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+	const int lane = threadIdx.x & (kWarp - 1);
+	if (a >= tt.nApp) return;
+	const SceneDev &sc = T.scenes[T.appScene[a]];
+	const int gx = sc.p.gx;
+	const int p0 = sc.pBase + sc.n0 + T.appRun[a] * kAppendixRun;
+	const int p1 = min(sc.pBase + sc.n, p0 + kAppendixRun);
+	int bx0 = sc.p.gx, by0 = sc.p.gy, bx1 = -1, by1 = -1;
+	for (int k = p0 + lane; k < p1; k += kWarp) {
+		const int lc = T.newCell[k] - sc.cellBase;
+		bx0 = min(bx0, lc % gx);
+		bx1 = max(bx1, lc % gx);
+		by0 = min(by0, lc / gx);
+		by1 = max(by1, lc / gx);
+	}
+	for (int o = 16; o > 0; o >>= 1) {
+		bx0 = min(bx0, __shfl_xor_sync(kFull, bx0, o));
+		by0 = min(by0, __shfl_xor_sync(kFull, by0, o));
+		bx1 = max(bx1, __shfl_xor_sync(kFull, bx1, o));
+		by1 = max(by1, __shfl_xor_sync(kFull, by1, o));
+	}
+	if (lane == 0) *reinterpret_cast<int4 *>(&T.appBox[4 * a]) = make_int4(bx0, by0, bx1, by1);
+}
+
 // ---------------------------------------------------------------------------
 // Density and pressure (demo4.cpp:208-221): a pure gather.  One warp per new
 // cell stages the 3x3 block of the new cell arrays (the particle's neighbour
@@ -1143,47 +1170,28 @@ __global__ void __launch_bounds__(C::kWarps * kWarp, C::kMinBlocks) k_delta(Tota
 				__threadfence();
 			}
 		} else {
-			// Appendix run: particles added since the last update, swept run
-			// after run within their scene, after all canonical tasks.
+			// Appendix run: particles added since the last update, after all
+			// canonical tasks; it waits for the earlier runs of its scene
+			// whose new cells come within two cells of its own.
 			const int a = t - tt.ncell;
-			const SceneDev &sc = T.scenes[T.appScene[a]];
+			const int scene = T.appScene[a];
+			const SceneDev &sc = T.scenes[scene];
 			const StepParams s = sc.p;
 			const int base = sc.cellBase;
 			const int p0 = sc.pBase + sc.n0 + T.appRun[a] * kAppendixRun;
 			const int p1 = min(sc.pBase + sc.n, p0 + kAppendixRun);
-			const int prev = T.appPrev[a];
-			int bx0 = s.gx, by0 = s.gy, bx1 = -1, by1 = -1;
-			for (int k = p0 + tid; k < p1; k += kDT) {
-				const int lc = T.newCell[k] - base;
-				bx0 = min(bx0, lc % s.gx);
-				bx1 = max(bx1, lc % s.gx);
-				by0 = min(by0, lc / s.gx);
-				by1 = max(by1, lc / s.gx);
-			}
-			// Block-wide min/max of the run's new cells (kAppendixRun <= 32:
-			// only warp 0 holds values).
-			if (tid < kWarp) {
-				for (int o = 16; o > 0; o >>= 1) {
-					bx0 = min(bx0, __shfl_xor_sync(kFull, bx0, o));
-					by0 = min(by0, __shfl_xor_sync(kFull, by0, o));
-					bx1 = max(bx1, __shfl_xor_sync(kFull, bx1, o));
-					by1 = max(by1, __shfl_xor_sync(kFull, by1, o));
-				}
-				if (tid == 0) {
-					S.warpCnt[0][0] = bx0;
-					S.warpCnt[0][1] = by0;
-					S.warpCnt[1][0] = bx1;
-					S.warpCnt[1][1] = by1;
-				}
-			}
-			__syncthreads();
-			bx0 = S.warpCnt[0][0];
-			by0 = S.warpCnt[0][1];
-			bx1 = S.warpCnt[1][0];
-			by1 = S.warpCnt[1][1];
-			__syncthreads();
+			const int4 box = *reinterpret_cast<const int4 *>(&T.appBox[4 * a]);
+			const int bx0 = box.x, by0 = box.y, bx1 = box.z, by1 = box.w;
 			wait_canonical<kDT>(bx0, by0, bx1, by1, moveMax, tt.ncell, -1, T, s, base, tid);
-			if (tid < kWarp) warp_wait(tid == 0 && prev >= 0 ? &T.done[prev] : nullptr, T.abort, T.error);
+			for (int q0 = 0; q0 < a; q0 += kDT) {
+				const int q = q0 + tid;
+				const uint32_t *flag = nullptr;
+				if (q < a && T.appScene[q] == scene) {
+					const int4 o = *reinterpret_cast<const int4 *>(&T.appBox[4 * q]);
+					if (rect_dist(o.x, o.y, o.z, o.w, bx0, by0, bx1, by1) <= 2) flag = &T.done[tt.ncell + q];
+				}
+				warp_wait(flag, T.abort, T.error);
+			}
 			__syncthreads();
 			relax_group<C>(S, p0, p1, bx0, by0, bx1, by1, Q, T, s, base, tid);
 			__syncthreads();

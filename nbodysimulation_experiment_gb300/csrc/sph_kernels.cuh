@@ -47,6 +47,7 @@ __global__ void k_scan_tiles(Totals tt, SimTables T, int ntiles);
 __global__ void k_scan_apply(Totals tt, SimTables T);
 __global__ void k_scatter(Totals tt, Particles P, SimTables T);
 __global__ void k_grid_update(Totals tt, Particles P, Particles Q, SimTables T);
+__global__ void k_app_boxes(Totals tt, SimTables T);
 __global__ void k_density(Totals tt, Particles Q, SimTables T);
 __global__ void k_collide(Totals tt, Particles P, Particles Q, SimTables T);
 __global__ void k_add(int first, int count, int scene, int firstId, const float2 *pos, const float2 *force,
