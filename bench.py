@@ -19,6 +19,18 @@ segments, gravity (0, -10), the reference's sph.h constants, FP32.
   multithreaded like the reference's ThreadPool on all host cores, on a
   bounded sample of the same workload.
 
+Further objects in the same line (forms of the step beyond the reference):
+
+* ``batched``: 512 independent scenes (log-uniform 1,024..65,536 particles,
+  ~8.1M in all) advanced by one update per step from the per-step CUDA graph,
+  sweep shapes chosen by the autotuner.
+* ``block_1m``: the 1,048,576-particle block, plain and with viscoelastic
+  springs.
+* ``learned``: the message-passing network trained on the GPU on plain
+  frames of seeded 65,536-particle scenes, then learned frames on a
+  262,144-particle dam break with obstacles against plain frames (four
+  updates of dt/4), under the density-deviation judge.
+
 ``--impl reference`` times that CPU implementation alone (rank 0 only).
 Multi-GPU runs are independent replicas (the step does not shard).
 """
