@@ -463,6 +463,16 @@ int enqueue_step(sph_sim *s, bool capturing) {
 	SPH_CUDA(mark(kEvBegin));
 	k_integrate<<<blocks_for(cellOrN, kElemThreads), kElemThreads, 0, st>>>(tt, A.view(), T);
 	SPH_LAUNCHED(s);
+	{
+		// The sweeps' task list: occupied canonical cells in task order.
+		const int ntiles = (tt.ncell + kScanTile - 1) / kScanTile;
+		k_live_reduce<<<ntiles, kScanThreads, 0, st>>>(tt, T);
+		SPH_LAUNCHED(s);
+		k_live_tiles<<<1, kScanThreads, 0, st>>>(T, ntiles);
+		SPH_LAUNCHED(s);
+		k_live_apply<<<ntiles, kScanThreads, 0, st>>>(tt, T);
+		SPH_LAUNCHED(s);
+	}
 	SPH_CUDA(mark(kEvIntegrate));
 
 	if (anyCanonical) {
@@ -651,6 +661,8 @@ int allocate(sph_sim *s) {
 	    (rc = dalloc(&T.bbox, 4 * C)) || (rc = dalloc(&T.newIdx, N)) || (rc = dalloc(&T.newLabel, N)) ||
 	    (rc = dalloc(&T.taskCounter, 2)) || (rc = dalloc(&T.stats, 4 * S)) || (rc = dalloc(&T.error, 1)) ||
 	    (rc = dalloc(&T.scanTiles, 3 * ((C + kScanTile - 1) / kScanTile))) ||
+	    (rc = dalloc(&T.liveTask, C)) || (rc = dalloc(&T.liveTiles, (C + kScanTile - 1) / kScanTile)) ||
+	    (rc = dalloc(&T.nLive, 1)) ||
 	    (rc = dalloc(&T.abort, 1)) || (rc = dalloc(&T.bodies, s->bodyCap)) || (rc = dalloc(&s->doneV, C)))
 		return rc;
 	// Appendix runs: at most one partial run per scene beyond N / kAppendixRun.
@@ -1200,7 +1212,7 @@ int sph_destroy(sph_sim *s) {
 	                T.appBox,      T.appCount,    T.appStart,    T.appIdx,      T.appCursor,   T.newCell,
 	                T.enterCount,  T.leaveCount,  T.enterOffset, T.enterCursor, T.enterList,   T.moverCount,
 	                T.bbox,        T.newIdx,      T.newLabel,    T.taskCounter, T.stats,       T.error,
-	                T.scanTiles,
+	                T.scanTiles,   T.liveTask,    T.liveTiles,   T.nLive,
 	                T.abort,       T.bodies,      s->doneV,      s->doneD,      s->stagePos,   s->stageForce,
 	                s->prof,       T.accN,        T.accP,        T.springPos,   T.springTotal,
 	                s->snap.pos,   s->snap.prev,  s->snap.vel,   s->snap.acc,   s->snap.dens,  s->snap.press,

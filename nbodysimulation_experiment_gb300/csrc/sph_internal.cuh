@@ -132,6 +132,7 @@ struct SimTables {
 	int *bbox;                         // per cell: x0, y0, x1, y1 of new cells
 	int *newCount, *newStart;
 	int *scanTiles;                    // 3 x tiles: per-tile sums, then tile offsets
+	int *liveTask, *liveTiles, *nLive;  // occupied canonical cells' tasks in order, per-tile offsets, count
 	int *newIdx;    // new number -> old number (the new cell arrays, concatenated)
 	int *newLabel;  // old number -> new number
 	uint32_t *done;                    // per sweep task

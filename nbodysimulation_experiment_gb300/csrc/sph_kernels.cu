@@ -313,12 +313,14 @@ __global__ void __launch_bounds__(C::kWarps * kWarp, C::kMinBlocks) k_viscosity(
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	ViscSmemT<C> &S = *reinterpret_cast<ViscSmemT<C> *>(smem_raw);
 	const int tid = threadIdx.x, warp = tid / kWarp;
+	const int nLive = *T.nLive;
 	for (;;) {
 		if (tid == 0) S.task = atomicAdd(&T.taskCounter[0], 1);
 		__syncthreads();
-		const int t = S.task;
+		const int i = S.task;
 		__syncthreads();
-		if (t >= tt.ncell) break;
+		if (i >= nLive) break;
+		const int t = T.liveTask[i];
 		stamp(T, 0, t, 0, tid);
 		const int c = T.taskCell[t];
 		const int cnt = T.cellCount[c];
@@ -433,6 +435,62 @@ __global__ void k_predict(Totals tt, Particles P, SimTables T) {
 		atomicMax(&T.bbox[4 * oc + 3], ny);
 		atomicMax(&T.moverCount[1], max(abs(nx - ox), abs(ny - oy)));
 		atomicAdd(&T.moverCount[0], 1);
+	}
+}
+
+// ---------------------------------------------------------------------------
+// The occupied canonical cells in task order (both sweeps skip empty cells):
+// per-tile counts, a scan of the tile counts, then the compacted list.
+
+__global__ void __launch_bounds__(kScanThreads) k_live_reduce(Totals tt, SimTables T) {
+	__shared__ int part[kScanThreads / kWarp];
+	const int tile = blockIdx.x;
+	int cnt = 0;
+	for (int k = 0; k < kScanTile / kScanThreads; ++k) {
+		const int t = tile * kScanTile + k * kScanThreads + threadIdx.x;
+		if (t < tt.ncell) cnt += T.cellCount[T.taskCell[t]] > 0;
+	}
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(kFull, cnt, o);
+	if ((threadIdx.x & (kWarp - 1)) == 0) part[threadIdx.x / kWarp] = cnt;
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		int sum = 0;
+		for (int w = 0; w < kScanThreads / kWarp; ++w) sum += part[w];
+		T.liveTiles[tile] = sum;
+	}
+}
+
+namespace {
+__device__ __forceinline__ int block_exscan(int v, int *warpSums, int *total);
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_live_tiles(SimTables T, int ntiles) {
+	__shared__ int warpSums[kScanThreads / kWarp];
+	__shared__ int total;
+	int carry = 0;
+	for (int base = 0; base < ntiles; base += kScanThreads) {
+		const int i = base + threadIdx.x;
+		const int x = i < ntiles ? T.liveTiles[i] : 0;
+		const int ex = block_exscan(x, warpSums, &total);
+		if (i < ntiles) T.liveTiles[i] = carry + ex;
+		carry += total;
+		__syncthreads();
+	}
+	if (threadIdx.x == 0) *T.nLive = carry;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_live_apply(Totals tt, SimTables T) {
+	__shared__ int warpSums[kScanThreads / kWarp];
+	__shared__ int total;
+	const int tile = blockIdx.x;
+	int carry = T.liveTiles[tile];
+	for (int k = 0; k < kScanTile / kScanThreads; ++k) {
+		const int t = tile * kScanTile + k * kScanThreads + threadIdx.x;
+		const bool live = t < tt.ncell && T.cellCount[T.taskCell[t]] > 0;
+		const int ex = block_exscan(live ? 1 : 0, warpSums, &total);
+		if (live) T.liveTask[carry + ex] = t;
+		carry += total;
 	}
 }
 
@@ -1147,16 +1205,19 @@ __global__ void __launch_bounds__(C::kWarps * kWarp, C::kMinBlocks) k_delta(Tota
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	DeltaSmemT<C> &S = *reinterpret_cast<DeltaSmemT<C> *>(smem_raw);
 	const int tid = threadIdx.x;
-	const int ntask = tt.ncell + tt.nApp;
+	const int nLive = *T.nLive;
+	const int ntask = nLive + tt.nApp;
 	const int moveMax = T.moverCount[1];
 	for (;;) {
 		if (tid == 0) S.task = atomicAdd(&T.taskCounter[1], 1);
 		__syncthreads();
-		const int t = S.task;
+		const int i = S.task;
 		__syncthreads();
-		if (t >= ntask) break;
+		if (i >= ntask) break;
+		// Task index (done flag): canonical cell task, or ncell + appendix run.
+		const int t = i < nLive ? T.liveTask[i] : tt.ncell + (i - nLive);
 		stamp(T, 1, t, 0, tid);
-		if (t < tt.ncell) {
+		if (i < nLive) {
 			const int c = T.taskCell[t];
 			const int p0 = T.cellStart[c], cnt = T.cellCount[c];
 			if (cnt > 0) {

@@ -42,6 +42,9 @@ size_t springs_smem_bytes();
 
 __global__ void k_integrate(Totals tt, Particles P, SimTables T);
 __global__ void k_predict(Totals tt, Particles P, SimTables T);
+__global__ void k_live_reduce(Totals tt, SimTables T);
+__global__ void k_live_tiles(SimTables T, int ntiles);
+__global__ void k_live_apply(Totals tt, SimTables T);
 __global__ void k_scan_reduce(Totals tt, SimTables T);
 __global__ void k_scan_tiles(Totals tt, SimTables T, int ntiles);
 __global__ void k_scan_apply(Totals tt, SimTables T);
