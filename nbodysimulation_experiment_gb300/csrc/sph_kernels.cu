@@ -113,9 +113,17 @@ __device__ __forceinline__ int rect_dist(int ax0, int ay0, int ax1, int ay1, int
 
 // ---------------------------------------------------------------------------
 // Integrate forces (demo4.cpp:302-309) and reset the per-step cell tables.
+// The first kernel of an update also pulls the arrays the ordered sweeps
+// read on their critical path (positions, cell ranges, task indices) into
+// L2, so that their staging does not wait on DRAM.
+__device__ __forceinline__ void prefetch_l2(const void *p) {
+	asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 __global__ void k_integrate(Totals tt, Particles P, SimTables T) {
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i < tt.n) {
+		prefetch_l2(&P.pos[i]);
 		const StepParams &s = T.scenes[T.sceneOf[i]].p;
 		float2 a = P.acc[i];
 		float2 v = P.vel[i];
@@ -127,6 +135,8 @@ __global__ void k_integrate(Totals tt, Particles P, SimTables T) {
 		P.acc[i] = make_float2(0.0f, 0.0f);
 	}
 	if (i < tt.ncell) {
+		prefetch_l2(&T.cellStart[i]);
+		prefetch_l2(&T.taskOfCell[i]);
 		const SceneDev &sc = T.scenes[T.sceneOfCell[i]];
 		const int local = i - sc.cellBase;
 		T.enterCount[i] = 0;
@@ -165,9 +175,7 @@ template <class C>
 struct ViscSmemT {
 	float2 pos[kStageCap];
 	float2 vel[kStageCap];
-	int cslot[2][C::kGeom];   // in-range pairs of a particle, list order
-	float2 cn[2][C::kGeom];   // unit vector of the pair
-	float comq[2][C::kGeom];  // 1 - q
+	float4 geo[2][C::kGeom];  // in-range pairs of a particle, list order: slot, unit vector, 1 - q
 	int m[2];
 	int warpCnt[2][C::kWarps];
 	int task;
@@ -227,9 +235,7 @@ __device__ __forceinline__ void visc_geometry(ViscSmemT<C> &S, int buf, int slot
 			float len = r;  // Vec2Length(Rij) == rij
 			if (len == 0.0f) len = 1.0f;
 			const float inv = 1.0f / len;
-			S.cslot[buf][at] = e;
-			S.cn[buf][at] = make_float2(rx * inv, ry * inv);
-			S.comq[buf][at] = 1.0f - qq;
+			S.geo[buf][at] = make_float4(__int_as_float(e), rx * inv, ry * inv, 1.0f - qq);
 		}
 		m += total;
 		parity ^= 1;
@@ -246,9 +252,21 @@ __device__ __forceinline__ void visc_geometry(ViscSmemT<C> &S, int buf, int slot
 template <class C>
 __device__ __forceinline__ void visc_pair(ViscSmemT<C> &S, int j, float2 n, float o, float2 vj, float2 &vi,
                                           const StepParams &s, float hdt) {
-	// Computed unconditionally and selected: only approaching pairs (u > 0)
-	// exchange an impulse.
+	// Only approaching pairs (u > 0) exchange an impulse.  The wide shape
+	// (latency) computes it unconditionally and selects; the lean shape
+	// (issue-bound with many chains per SM) skips it.
 	const float uu = (vi.x - vj.x) * n.x + (vi.y - vj.y) * n.y;
+	if (C::kBranchy) {
+		if (uu > 0.0f) {
+			const float f = o * (s.sigma * uu + s.beta * (uu * uu));
+			const float ix = (f * n.x) * hdt;
+			const float iy = (f * n.y) * hdt;
+			vi.x = vi.x - ix;
+			vi.y = vi.y - iy;
+			S.vel[j] = make_float2(ix + vj.x, iy + vj.y);
+		}
+		return;
+	}
 	const float f = o * (s.sigma * uu + s.beta * (uu * uu));
 	const float ix = (f * n.x) * hdt;
 	const float iy = (f * n.y) * hdt;
@@ -284,23 +302,20 @@ __device__ __forceinline__ void visc_chain(ViscSmemT<C> &S, int buf, int slot, i
 	}
 	int q = 0;
 	for (; q + 4 <= m; q += 4) {
-		int j[4];
-		float2 n[4], vj[4];
-		float o[4];
+		float4 g[4];
+		float2 vj[4];
 #pragma unroll
-		for (int u = 0; u < 4; ++u) {
-			j[u] = S.cslot[buf][q + u];
-			n[u] = S.cn[buf][q + u];
-			o[u] = S.comq[buf][q + u];
-		}
+		for (int u = 0; u < 4; ++u) g[u] = S.geo[buf][q + u];
 #pragma unroll
-		for (int u = 0; u < 4; ++u) vj[u] = S.vel[j[u]];
+		for (int u = 0; u < 4; ++u) vj[u] = S.vel[__float_as_int(g[u].x)];
 #pragma unroll
-		for (int u = 0; u < 4; ++u) visc_pair(S, j[u], n[u], o[u], vj[u], vi, s, hdt);
+		for (int u = 0; u < 4; ++u)
+			visc_pair(S, __float_as_int(g[u].x), make_float2(g[u].y, g[u].z), g[u].w, vj[u], vi, s, hdt);
 	}
 	for (; q < m; ++q) {
-		const int j = S.cslot[buf][q];
-		visc_pair(S, j, S.cn[buf][q], S.comq[buf][q], S.vel[j], vi, s, hdt);
+		const float4 g = S.geo[buf][q];
+		const int j = __float_as_int(g.x);
+		visc_pair(S, j, make_float2(g.y, g.z), g.w, S.vel[j], vi, s, hdt);
 	}
 	S.vel[slot] = vi;
 }

@@ -11,9 +11,11 @@ namespace sphgb {
 // tasks per SM for many scenes).  Results do not depend on the shape.
 struct ViscWide {
 	static constexpr int kWarps = 4, kProducers = 3 * kWarp, kGeom = kStageCap, kMinBlocks = 4;
+	static constexpr bool kBranchy = false;
 };
 struct ViscLean {
 	static constexpr int kWarps = 2, kProducers = kWarp, kGeom = 256, kMinBlocks = 8;
+	static constexpr bool kBranchy = true;
 };
 struct DeltaWide {
 	static constexpr int kWarps = 4, kStage = kDeltaStageCap, kChain = kDeltaChainCap, kPrefetch = 128,

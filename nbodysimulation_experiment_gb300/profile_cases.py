@@ -41,9 +41,13 @@ def mpnn(steps: int = 3) -> None:
 
 
 def batched(updates: int = 3) -> None:
-    """64 scenes of the batched workload's distribution."""
+    """64 scenes of the batched workload's distribution, lean (2-warp) sweep
+    shapes with 8 resident blocks per SM."""
     mix = scenes.batch_scenes(count=64, seed=11)
     batch = BatchSimulation(mix)
+    batch.update(float(scenes.DT))
+    sms = batch.sweep_shape()[1] // 4  # the default shape runs 4 blocks per SM
+    batch.set_sweep_shape((2, 8 * sms, 2, 8 * sms))
     for _ in range(updates):
         batch.update(float(scenes.DT))
     batch.synchronize()
