@@ -466,16 +466,25 @@ int gemm_check(const GemmArgs &g, int splits) {
 }
 
 cudaError_t gemm_launch(const GemmArgs &g, int splits, cudaStream_t stream) {
-	static std::once_flag once;
-	static cudaError_t attrErr = cudaSuccess;
-	std::call_once(once, [] {
-		attrErr = cudaFuncSetAttribute(k_gemm_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize,
-		                               (int)gemm_smem_bytes());
-		if (attrErr == cudaSuccess)
-			attrErr = cudaFuncSetAttribute(k_gemm_bf16_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
-			                               (int)gemm_tma_smem_bytes(kMaxN));
-	});
-	if (attrErr != cudaSuccess) return attrErr;
+	// Kernel attributes are per device: set them once on each device used.
+	static std::mutex mu;
+	static bool done[64] = {};
+	int device = 0;
+	cudaError_t e = cudaGetDevice(&device);
+	if (e != cudaSuccess) return e;
+	{
+		std::lock_guard<std::mutex> lock(mu);
+		if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
+		if (!done[device]) {
+			e = cudaFuncSetAttribute(k_gemm_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			                         (int)gemm_smem_bytes());
+			if (e == cudaSuccess)
+				e = cudaFuncSetAttribute(k_gemm_bf16_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+				                         (int)gemm_tma_smem_bytes(kMaxN));
+			if (e != cudaSuccess) return e;
+			done[device] = true;
+		}
+	}
 	dim3 grid((g.M + kTileM - 1) / kTileM, splits);
 	CUtensorMap mapA, mapB;
 	if (!g.noTma && encode(&mapA, g.A, g.M, g.K, g.lda, kTileM) && encode(&mapB, g.B, g.N, g.K, g.ldb, g.N)) {
