@@ -113,17 +113,9 @@ __device__ __forceinline__ int rect_dist(int ax0, int ay0, int ax1, int ay1, int
 
 // ---------------------------------------------------------------------------
 // Integrate forces (demo4.cpp:302-309) and reset the per-step cell tables.
-// The first kernel of an update also pulls the arrays the ordered sweeps
-// read on their critical path (positions, cell ranges, task indices) into
-// L2, so that their staging does not wait on DRAM.
-__device__ __forceinline__ void prefetch_l2(const void *p) {
-	asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
-}
-
 __global__ void k_integrate(Totals tt, Particles P, SimTables T) {
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i < tt.n) {
-		prefetch_l2(&P.pos[i]);
 		const StepParams &s = T.scenes[T.sceneOf[i]].p;
 		float2 a = P.acc[i];
 		float2 v = P.vel[i];
@@ -135,8 +127,6 @@ __global__ void k_integrate(Totals tt, Particles P, SimTables T) {
 		P.acc[i] = make_float2(0.0f, 0.0f);
 	}
 	if (i < tt.ncell) {
-		prefetch_l2(&T.cellStart[i]);
-		prefetch_l2(&T.taskOfCell[i]);
 		const SceneDev &sc = T.scenes[T.sceneOfCell[i]];
 		const int local = i - sc.cellBase;
 		T.enterCount[i] = 0;
