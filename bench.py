@@ -256,6 +256,7 @@ def bench_block_1m(torch, pkg, scenes, device: int, steps: int, warmup: int, spr
     for _ in range(warmup):
         sim.update(dt)
     sim.synchronize()
+    tuned = sim.autotune(dt)
     ms, spring_ms = [], []
     for _ in range(steps):
         with torch.cuda.stream(stream):
@@ -269,7 +270,9 @@ def bench_block_1m(torch, pkg, scenes, device: int, steps: int, warmup: int, spr
         ms.append(e0.elapsed_time(e1))
         spring_ms.append(sim.get_stats().time_neighbor_search)
     out = {"value": scene.n * steps / (sum(ms) / 1e3), "unit": UNIT, "ms_per_step": statistics.mean(ms),
-           "steps": steps, "warmup": warmup, "particles": scene.n, "springs": springs}
+           "steps": steps, "warmup": warmup, "particles": scene.n, "springs": springs,
+           "autotuned_shape": {"viscosity_warps": tuned[0], "viscosity_blocks": tuned[1],
+                               "delta_warps": tuned[2], "delta_blocks": tuned[3]}}
     if springs:
         out["spring_phase_ms"] = statistics.mean(spring_ms)
         out["spring_count"] = sim.spring_count()
@@ -391,6 +394,7 @@ def main():
     for _ in range(args.warmup):
         sim.update(dt)
     sim.synchronize()
+    tuned = sim.autotune(dt)
 
     # --- device-resident timed region -------------------------------------
     launches0 = sim.kernel_launches()
@@ -487,6 +491,8 @@ def main():
             "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
             "config": {"workload": WORKLOAD, "particles": scene.n, "l2": "flushed between steps (256 MiB write)",
+                       "sweep_shape": {"viscosity_warps": tuned[0], "viscosity_blocks": tuned[1],
+                                       "delta_warps": tuned[2], "delta_blocks": tuned[3]},
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "density_error": dens_err},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(h2d)},

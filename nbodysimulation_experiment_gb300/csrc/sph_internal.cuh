@@ -19,8 +19,6 @@ constexpr int kDeltaStageCap = 4096;
 // In-range pairs buffered between the parallel geometry phase and the serial
 // chain of one particle; longer lists are drained in several rounds.
 constexpr int kChainCap = 256;
-// In-range pairs buffered per particle by a delta-sweep block.
-constexpr int kDeltaChainCap = 512;
 // Per-particle inputs of the delta sweep prefetched per chunk of a task.
 constexpr int kPrefetch = 128;
 // Working array of one cell during the grid update (kSPHMaxCellParticleCount

@@ -191,7 +191,9 @@ __device__ __forceinline__ void producers_sync() {
 
 // Geometry of the particle at staged slot `slot` over the L staged entries
 // (its whole list): in-range pairs in list order with their unit vectors
-// and 1 - q (sph.h:497-505).  Run by the producer warps only.
+// and 1 - q (sph.h:497-505).  Run by the producer warps only, in two passes:
+// the in-range entries are compacted first (slot, r, r^2), then the square
+// roots and divisions run over the dense compacted list.
 template <class C>
 __device__ __forceinline__ void visc_geometry(ViscSmemT<C> &S, int buf, int slot, int L, const StepParams &s, int p) {
 	const int lane = p & (kWarp - 1), w = p / kWarp;
@@ -209,26 +211,33 @@ __device__ __forceinline__ void visc_geometry(ViscSmemT<C> &S, int buf, int slot
 			in = r2 < s.h2;
 		}
 		const unsigned mask = __ballot_sync(kFull, in);
-		if (lane == 0) S.warpCnt[parity][w] = __popc(mask);
-		producers_sync<C>();
-		int before = m, total = 0;
+		int before = m, total = __popc(mask);
+		if (C::kProducers > kWarp) {
+			if (lane == 0) S.warpCnt[parity][w] = total;
+			producers_sync<C>();
+			total = 0;
 #pragma unroll
-		for (int q = 0; q < C::kWarps - 1; ++q) {
-			const int c = S.warpCnt[parity][q];
-			before += (q < w) ? c : 0;
-			total += c;
+			for (int q = 0; q < C::kWarps - 1; ++q) {
+				const int c = S.warpCnt[parity][q];
+				before += (q < w) ? c : 0;
+				total += c;
+			}
+			parity ^= 1;
 		}
 		const int at = before + __popc(mask & lanemask_lt());
-		if (in && at < C::kGeom) {
-			const float r = sqrtf(r2);
-			const float qq = r * s.invH;
-			float len = r;  // Vec2Length(Rij) == rij
-			if (len == 0.0f) len = 1.0f;
-			const float inv = 1.0f / len;
-			S.geo[buf][at] = make_float4(__int_as_float(e), rx * inv, ry * inv, 1.0f - qq);
-		}
+		if (in && at < C::kGeom) S.geo[buf][at] = make_float4(__int_as_float(e), rx, ry, r2);
 		m += total;
-		parity ^= 1;
+	}
+	if (C::kProducers > kWarp) producers_sync<C>(); else __syncwarp();
+	const int mm = min(m, C::kGeom);
+	for (int q = p; q < mm; q += C::kProducers) {
+		const float4 g = S.geo[buf][q];
+		const float r = sqrtf(g.w);
+		const float qq = r * s.invH;
+		float len = r;  // Vec2Length(Rij) == rij
+		if (len == 0.0f) len = 1.0f;
+		const float inv = 1.0f / len;
+		S.geo[buf][q] = make_float4(g.x, g.y * inv, g.z * inv, 1.0f - qq);
 	}
 	if (p == 0) S.m[buf] = m;
 }
@@ -290,23 +299,56 @@ __device__ __forceinline__ void visc_chain(ViscSmemT<C> &S, int buf, int slot, i
 		S.vel[slot] = vi;
 		return;
 	}
+	// Software pipeline: the geometry and partner velocities of the next four
+	// pairs are loaded while the chain runs over the current four.  Each slot
+	// occurs once per list, so a prefetched velocity is never one this
+	// particle has already changed.
+	const float4 *G = S.geo[buf];
+	float4 g[4];
+	float2 vj[4];
+#pragma unroll
+	for (int u = 0; u < 4; ++u) g[u] = u < m ? G[u] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+	for (int u = 0; u < 4; ++u) vj[u] = S.vel[__float_as_int(g[u].x)];
 	int q = 0;
-	for (; q + 4 <= m; q += 4) {
-		float4 g[4];
-		float2 vj[4];
+	for (; q + 8 <= m; q += 4) {
+		float4 gn[4];
+		float2 vn[4];
 #pragma unroll
-		for (int u = 0; u < 4; ++u) g[u] = S.geo[buf][q + u];
+		for (int u = 0; u < 4; ++u) gn[u] = G[q + 4 + u];
 #pragma unroll
-		for (int u = 0; u < 4; ++u) vj[u] = S.vel[__float_as_int(g[u].x)];
+		for (int u = 0; u < 4; ++u) vn[u] = S.vel[__float_as_int(gn[u].x)];
 #pragma unroll
 		for (int u = 0; u < 4; ++u)
 			visc_pair(S, __float_as_int(g[u].x), make_float2(g[u].y, g[u].z), g[u].w, vj[u], vi, s, hdt);
+#pragma unroll
+		for (int u = 0; u < 4; ++u) {
+			g[u] = gn[u];
+			vj[u] = vn[u];
+		}
 	}
-	for (; q < m; ++q) {
-		const float4 g = S.geo[buf][q];
-		const int j = __float_as_int(g.x);
-		visc_pair(S, j, make_float2(g.y, g.z), g.w, S.vel[j], vi, s, hdt);
+	// At most seven pairs left, the first four of them loaded.
+	if (q + 4 <= m) {
+		float4 gn[4];
+		float2 vn[4];
+#pragma unroll
+		for (int u = 0; u < 4; ++u) gn[u] = q + 4 + u < m ? G[q + 4 + u] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+		for (int u = 0; u < 4; ++u) vn[u] = S.vel[__float_as_int(gn[u].x)];
+#pragma unroll
+		for (int u = 0; u < 4; ++u)
+			visc_pair(S, __float_as_int(g[u].x), make_float2(g[u].y, g[u].z), g[u].w, vj[u], vi, s, hdt);
+#pragma unroll
+		for (int u = 0; u < 4; ++u) {
+			g[u] = gn[u];
+			vj[u] = vn[u];
+		}
+		q += 4;
 	}
+#pragma unroll
+	for (int u = 0; u < 4; ++u)
+		if (q + u < m)
+			visc_pair(S, __float_as_int(g[u].x), make_float2(g[u].y, g[u].z), g[u].w, vj[u], vi, s, hdt);
 	S.vel[slot] = vi;
 }
 
@@ -897,25 +939,50 @@ __global__ void __launch_bounds__(kDensWarps * kWarp) k_density(Totals tt, Parti
 // cells of its bounding box grown by one, processes its particles in order,
 // and writes back only cells inside its particles' 3x3 blocks.  Earlier tasks
 // of the scene whose bounding boxes come within two cells are waited for.
-// One task per block of kDeltaTaskWarps warps: the whole block stages the
-// task's region, and for each particle scans the list, compacts the in-range
-// pairs and evaluates them in parallel; one thread then adds the halves to
-// dx in list order.
-// Two shapes (DeltaWide, DeltaLean in sph_kernels.cuh): the lean one uses two
-// warps and smaller staging and pair buffers (regions that do not fit are
-// staged per particle), so more tasks fit on an SM.
+// One task per block.  The block stages the task's region once.  A
+// particle's list slots (three row ranges of the staged region and its own
+// slot) are worked out for a chunk of particles at once, off the serial path.
+//
+// Particles are relaxed in a two-stage pipeline.  In phase k the producer
+// warps (all but the last) scan particle k's list, compact the in-range pairs
+// in list order and evaluate them (x_j += D/2), while the summer warp (the
+// last) finishes particle k-1: its ordered sum dx -= D/2 and x_{k-1} += dx.
+// The only pair of particle k that needs x_{k-1} after that sum is
+// (k, k-1): the producers reserve its place in list order, and the summer,
+// which knows from k's list ranges whether k-1 is in the list, evaluates it
+// right after the sum (x_{k-1} += D/2) and keeps D/2 until the next phase,
+// when it fills the reserved place before summing k.  The two roles share no
+// data within a phase, so they meet only at the phase's end.  k's own (self)
+// pair is kept aside (ownAfter) so that no warp sees k's position change
+// before reading it.
+// Particles whose lists exceed one pass, and regions staged particle by
+// particle, drain the pipeline and run on the whole block in turn.
+// Two shapes (DeltaWide, DeltaLean in sph_kernels.cuh): wide is pipelined
+// with seven producer warps (short per-particle latency, one scene); lean is
+// two warps without the pipeline and with smaller staging (more tasks per
+// SM, many scenes).
 template <class C>
 struct DeltaSmemT {
+	static constexpr int kProd = C::kWarps - 1;         // producer warps
+	static constexpr int kPass = kProd * C::kChainW;    // list entries per pipelined particle
+	static constexpr int kSeqPass = C::kWarps * C::kChainW;  // list entries per pass, whole block
+	static constexpr int kHalf = (kSeqPass > kPass ? kSeqPass : kPass) + 16;
+	static constexpr int kPhases = C::kPipelined ? 2 : 1;  // half buffers
 	float2 pos[C::kStage];
-	float4 cand[C::kChain];  // in-range candidates: slot, x_j.x, x_j.y, r2
-	float2 half[C::kChain];  // delta * 0.5 of the buffered pairs, list order
-	int pnc[C::kPrefetch];   // prefetched per particle: new cell,
-	int pjk[C::kPrefetch];   // new number,
+	float4 cand[C::kWarps][C::kChainW];  // per warp: in-range candidates: slot, x_j.x, x_j.y, r2
+	float2 half[kPhases][kHalf];  // per phase: delta * 0.5 of the in-range pairs, list order, +0 padded
+	int4 meta[2];             // per phase: pairs, reserved index of (k, k-1) or -1, own slot
+	float2 ownAfter[2];       // per phase: the particle's position after its self pair
+	int4 pslot[C::kPrefetch];  // prefetched per particle: row ranges' first slots, own slot (or -1)
+	int4 plen[C::kPrefetch];   // row ranges' lengths
+	int pnc[C::kPrefetch];     // new cell and new number (per-particle staging only)
+	int pjk[C::kPrefetch];
 	float2 ppk[C::kPrefetch];  // pressure and near pressure
 	int segOff[kRegionCells + 1];
 	int segStart[kRegionCells];
 	int owned[kRegionCells];
-	int warpCnt[2][C::kWarps];
+	int wcnt[C::kWarps];
+	int4 oneSlot, oneLen;  // slots of a particle staged on its own
 	int task;
 };
 
@@ -998,161 +1065,311 @@ __device__ __forceinline__ void write_back_owned(DeltaSmemT<C> &S, const Region 
 	}
 }
 
-// Relax one particle (new cell nc, new number jk, pressures pk) whose 3x3
-// block lies inside the staged region (demo4.cpp:240-254, sph.h:483-495).
-// In the row-major staged region the three cells of one block row are
-// consecutive, so the particle's list (y-major, then x, then cell order) is
-// three contiguous ranges of staged slots.  Collective over the block.
+// List slots of the particle with new cell nc and new number jk, whose 3x3
+// block lies inside the staged region: in the row-major region the three
+// cells of one block row are consecutive, so the list (y-major, then x, then
+// cell order, demo4.cpp:188-201) is three contiguous ranges of slots.  Marks
+// the block's cells as written back.  One thread per particle.
 template <class C>
-__device__ __forceinline__ void relax_particle(DeltaSmemT<C> &S, const Region &R, int nc, int jk, float2 pk,
-                                               const SimTables &T, const StepParams &s, int cellBase, int tid) {
-	constexpr int kDT = C::kWarps * kWarp;
-	const int lane = tid & (kWarp - 1), warp = tid / kWarp;
+__device__ __forceinline__ void particle_slots(DeltaSmemT<C> &S, const Region &R, int nc, int jk, const StepParams &s,
+                                               int cellBase, uint32_t *err, int4 &slot, int4 &len) {
 	const int x = (nc - cellBase) % s.gx, y = (nc - cellBase) / s.gx;
 	const int xa = max(x - 1, 0), xb = min(x + 1, s.gx - 1);
-	int off0 = 0, off1 = 0, off2 = 0, len0 = 0, len1 = 0, len2 = 0;
+	int o[3], n[3];
 #pragma unroll
 	for (int r = 0; r < 3; ++r) {
 		const int yy = y + r - 1;
-		int o = 0, len = 0;
+		o[r] = 0;
+		n[r] = 0;
 		if (yy >= 0 && yy < s.gy) {
 			const int rq0 = (yy - R.y0) * R.w + (xa - R.x0);
 			const int rq1 = rq0 + (xb - xa);
-			o = S.segOff[rq0];
-			len = S.segOff[rq1 + 1] - o;
-			if (tid <= xb - xa) S.owned[rq0 + tid] = 1;
+			o[r] = S.segOff[rq0];
+			n[r] = S.segOff[rq1 + 1] - o[r];
+			for (int q = rq0; q <= rq1; ++q) S.owned[q] = 1;
 		}
-		if (r == 0) { off0 = o; len0 = len; }
-		if (r == 1) { off1 = o; len1 = len; }
-		if (r == 2) { off2 = o; len2 = len; }
 	}
-	const int L = len0 + len1 + len2;
 	const int ownSeg = (y - R.y0) * R.w + (x - R.x0);
 	const int inCell = jk - S.segStart[ownSeg];
+	int own = S.segOff[ownSeg] + inCell;
 	if (inCell < 0 || inCell >= S.segOff[ownSeg + 1] - S.segOff[ownSeg]) {
-		if (tid == 0) atomicOr(T.error, kErrIndex);
-		__syncthreads();
-		return;
+		atomicOr(err, kErrIndex);
+		own = -1;
 	}
-	const int own = S.segOff[ownSeg] + inCell;
-	const float2 xk = S.pos[own];
-	const int l01 = len0 + len1;
-	float2 dx = make_float2(0.0f, 0.0f);  // thread 0
-	int m = 0, parity = 0;
-	for (int b0 = 0; b0 < L; b0 += 2 * kDT) {
-		bool in[2];
-		int slot[2];
-		float2 xj[2];
-		float r2[2];
+	slot = make_int4(o[0], o[1], o[2], own);
+	len = make_int4(n[0], n[1], n[2], 0);
+}
+
+// delta * 0.5 of one in-range pair (sph.h:483-495 with demo4.cpp:250-251):
+// particle at xk with pressures pk, neighbour at xj, r2 = |xj - xk|^2.
+__device__ __forceinline__ float2 delta_half(float2 xj, float2 xk, float r2, float2 pk, const StepParams &s) {
+	const float rx = xj.x - xk.x, ry = xj.y - xk.y;
+	const float rij = sqrtf(r2);
+	float len = rij;
+	if (len == 0.0f) len = 1.0f;
+	const float inv = 1.0f / len;
+	const float nx = rx * inv, ny = ry * inv;
+	const float term = 1.0f - rij * s.invH;
+	const float d = s.dt2 * (pk.x * term + pk.y * (term * term));
+	return make_float2(d * nx * 0.5f, d * ny * 0.5f);
+}
+
+// dx -= delta * 0.5 over the n buffered halves, in list order
+// (demo4.cpp:251), in batches of eight loaded one batch ahead.  The buffer
+// is padded with +0 for sixteen entries past n, and dx - (+0) == dx exactly.
+__device__ __forceinline__ void sum_halves(const float2 *H, int n, float2 &dx) {
+	float2 h[8];
 #pragma unroll
-		for (int u = 0; u < 2; ++u) {
-			const int e = b0 + warp * 2 * kWarp + u * kWarp + lane;
-			in[u] = false;
-			slot[u] = 0;
-			xj[u] = make_float2(0.f, 0.f);
-			r2[u] = 0.f;
-			if (e < L) {
-				slot[u] = e < len0 ? off0 + e : (e < l01 ? off1 + (e - len0) : off2 + (e - l01));
-				xj[u] = S.pos[slot[u]];
-				const float rx = xj[u].x - xk.x, ry = xj[u].y - xk.y;
-				r2[u] = rx * rx + ry * ry;
-				in[u] = r2[u] < s.h2;
+	for (int u = 0; u < 8; ++u) h[u] = H[u];
+	for (int b = 8; b < n + 8; b += 8) {
+		float2 hn[8];
+#pragma unroll
+		for (int u = 0; u < 8; ++u) hn[u] = H[b + u];
+#pragma unroll
+		for (int u = 0; u < 8; ++u) {
+			dx.x = dx.x - h[u].x;
+			dx.y = dx.y - h[u].y;
+		}
+#pragma unroll
+		for (int u = 0; u < 8; ++u) h[u] = hn[u];
+	}
+}
+
+// Scan and compaction of one particle's list entries [p0, p0 + pl) over
+// `nw` warps (this thread is warp `w` of them): each warp takes a contiguous
+// range and compacts its in-range entries, in list order, into cand[w].
+// Slot `skip` (or -1) is reserved whatever its distance (marked r2 = -1);
+// slot `own` records the particle's unmoved position in *ownAfter.
+__device__ __forceinline__ int scan_range(float4 *cand, int nw, int w, int lane, int p0, int pl, int4 sl, int len0,
+                                          int l01, float2 xk, int own, int skip, const float2 *pos, float h2,
+                                          float2 *ownAfter) {
+	const int per = (pl + nw - 1) / nw;
+	const int e0 = p0 + w * per, e1 = min(p0 + pl, e0 + per);
+	int cnt = 0;
+	for (int eb = e0; eb < e1; eb += kWarp) {
+		const int e = eb + lane;
+		bool in = false;
+		int slot = 0;
+		float2 xj = make_float2(0.f, 0.f);
+		float r2 = 0.f;
+		if (e < e1) {
+			slot = e < len0 ? sl.x + e : (e < l01 ? sl.y + (e - len0) : sl.z + (e - l01));
+			if (slot == skip) {
+				in = true;
+				r2 = -1.0f;
+			} else {
+				xj = pos[slot];
+				const float rx = xj.x - xk.x, ry = xj.y - xk.y;
+				r2 = rx * rx + ry * ry;
+				in = r2 < h2;
+				if (slot == own) *ownAfter = xj;  // out of range: no displacement
 			}
 		}
-		const unsigned m0 = __ballot_sync(kFull, in[0]);
-		const unsigned m1 = __ballot_sync(kFull, in[1]);
-		if (lane == 0) S.warpCnt[parity][warp] = __popc(m0) + __popc(m1);
+		const unsigned mk = __ballot_sync(kFull, in);
+		if (in) cand[cnt + __popc(mk & lanemask_lt())] = make_float4(__int_as_float(slot), xj.x, xj.y, r2);
+		cnt += __popc(mk);
+	}
+	return cnt;
+}
+
+// Relax one particle on the whole block, not pipelined (demo4.cpp:240-254):
+// lists of any length, in passes of kSeqPass entries.  Thread 0 sums.
+template <class C>
+__device__ __forceinline__ void relax_particle(DeltaSmemT<C> &S, int4 sl, int4 ln, float2 pk, const StepParams &s,
+                                               int tid) {
+	constexpr int kW = C::kWarps, kPass = DeltaSmemT<C>::kSeqPass;
+	const int lane = tid & (kWarp - 1), warp = tid / kWarp;
+	const int own = sl.w;
+	if (own < 0) return;  // index check failed (uniform)
+	const int len0 = ln.x, l01 = ln.x + ln.y, L = l01 + ln.z;
+	const float2 xk = S.pos[own];
+	float2 *H = S.half[0];
+	float2 dx = make_float2(0.0f, 0.0f);  // thread 0
+	for (int p0 = 0; p0 < L; p0 += kPass) {
+		const int pl = min(L - p0, kPass);
+		const int cnt = scan_range(S.cand[warp], kW, warp, lane, p0, pl, sl, len0, l01, xk, own, -1, S.pos, s.h2,
+		                           &S.ownAfter[0]);
+		if (lane == 0) S.wcnt[warp] = cnt;
 		__syncthreads();
-		int before = m, total = 0;
+		int before = 0, total = 0;
 #pragma unroll
-		for (int w = 0; w < C::kWarps; ++w) {
-			const int c = S.warpCnt[parity][w];
+		for (int w = 0; w < kW; ++w) {
+			const int c = S.wcnt[w];
 			before += (w < warp) ? c : 0;
 			total += c;
 		}
-		const unsigned lt = lanemask_lt();
-		if (in[0]) S.cand[before + __popc(m0 & lt)] = make_float4(__int_as_float(slot[0]), xj[0].x, xj[0].y, r2[0]);
-		if (in[1])
-			S.cand[before + __popc(m0) + __popc(m1 & lt)] =
-			    make_float4(__int_as_float(slot[1]), xj[1].x, xj[1].y, r2[1]);
-		m += total;
-		parity ^= 1;
-		if (m > C::kChain - 2 * kDT || b0 + 2 * kDT >= L) {
-			__syncthreads();
-			for (int q = tid; q < m; q += kDT) {
-				const float4 cd = S.cand[q];
-				const float rx = cd.y - xk.x, ry = cd.z - xk.y;
-				const float rij = sqrtf(cd.w);
-				float len = rij;
-				if (len == 0.0f) len = 1.0f;
-				const float inv = 1.0f / len;
-				const float nx = rx * inv, ny = ry * inv;
-				const float term = 1.0f - rij * s.invH;
-				const float d = s.dt2 * (pk.x * term + pk.y * (term * term));
-				const float2 half = make_float2(d * nx * 0.5f, d * ny * 0.5f);
-				S.pos[__float_as_int(cd.x)] = make_float2(half.x + cd.y, half.y + cd.z);
-				S.half[q] = half;
-			}
-			__syncthreads();
-			if (tid == 0) {
-				// dx -= delta * 0.5 in list order (demo4.cpp:251).
-				int q = 0;
-				for (; q + 8 <= m; q += 8) {
-					float2 h[8];
-#pragma unroll
-					for (int u = 0; u < 8; ++u) h[u] = S.half[q + u];
-#pragma unroll
-					for (int u = 0; u < 8; ++u) {
-						dx.x = dx.x - h[u].x;
-						dx.y = dx.y - h[u].y;
-					}
-				}
-				for (; q < m; ++q) {
-					const float2 h = S.half[q];
-					dx.x = dx.x - h.x;
-					dx.y = dx.y - h.y;
-				}
-			}
-			m = 0;
+		if (tid < 16) H[total + tid] = make_float2(0.0f, 0.0f);
+		for (int q = lane; q < cnt; q += kWarp) {
+			const float4 cd = S.cand[warp][q];
+			const float2 xj = make_float2(cd.y, cd.z);
+			const float2 h = delta_half(xj, xk, cd.w, pk, s);
+			const int slot = __float_as_int(cd.x);
+			const float2 moved = make_float2(h.x + xj.x, h.y + xj.y);
+			if (slot == own) S.ownAfter[0] = moved; else S.pos[slot] = moved;
+			H[before + q] = h;
 		}
+		__syncthreads();
+		if (tid == 0) {
+			sum_halves(H, total, dx);
+			if (p0 + kPass >= L) {
+				const float2 xo = S.ownAfter[0];
+				S.pos[own] = make_float2(dx.x + xo.x, dx.y + xo.y);
+			}
+		}
+		__syncthreads();
+	}
+}
+
+// Summer warp, lane 0: finish the particle of phase buffer b (fill its
+// reserved pair with hres, its ordered dx sum, its final position).
+// Returns the final position.
+template <class C>
+__device__ __forceinline__ float2 finish_particle(DeltaSmemT<C> &S, int b, float2 hres) {
+	const int4 m = S.meta[b];
+	float2 *H = S.half[b];
+	if (m.y >= 0) H[m.y] = hres;
+	float2 dx = make_float2(0.0f, 0.0f);
+	sum_halves(H, m.x, dx);
+	const float2 xo = S.ownAfter[b];
+	const float2 xp = make_float2(dx.x + xo.x, dx.y + xo.y);
+	S.pos[m.z] = xp;
+	return xp;
+}
+
+template <class C>
+__device__ __forceinline__ void producers_bar() {
+	__syncwarp();
+	asm volatile("bar.sync 1, %0;" ::"r"(DeltaSmemT<C>::kProd * kWarp) : "memory");
+}
+
+// Producers' part of phase b for particle (sl, ln, pk): everything but the
+// pair with slot `prev` (the particle still being finished, or -1).
+template <class C>
+__device__ __forceinline__ void produce(DeltaSmemT<C> &S, int b, int4 sl, int4 ln, float2 pk, int prev,
+                                        const StepParams &s, int tid) {
+	constexpr int kP = DeltaSmemT<C>::kProd;
+	const int lane = tid & (kWarp - 1), warp = tid / kWarp;
+	const int own = sl.w;
+	const int len0 = ln.x, l01 = ln.x + ln.y, L = l01 + ln.z;
+	const float2 xk = S.pos[own];
+	float2 *H = S.half[b];
+	if (tid == 0) S.meta[b].y = -1;
+	const int cnt = scan_range(S.cand[warp], kP, warp, lane, 0, L, sl, len0, l01, xk, own, prev, S.pos, s.h2,
+	                           &S.ownAfter[b]);
+	int before = 0, total = cnt;
+	if (kP > 1) {
+		if (lane == 0) S.wcnt[warp] = cnt;
+		producers_bar<C>();
+		total = 0;
+#pragma unroll
+		for (int w = 0; w < kP; ++w) {
+			const int c = S.wcnt[w];
+			before += (w < warp) ? c : 0;
+			total += c;
+		}
+	} else {
+		__syncwarp();
+	}
+	if (tid < 16) H[total + tid] = make_float2(0.0f, 0.0f);
+	for (int q = lane; q < cnt; q += kWarp) {
+		const float4 cd = S.cand[warp][q];
+		if (cd.w < 0.0f) {
+			S.meta[b].y = before + q;  // (k, k-1): the summer evaluates it
+			continue;
+		}
+		const float2 xj = make_float2(cd.y, cd.z);
+		const float2 h = delta_half(xj, xk, cd.w, pk, s);
+		const int slot = __float_as_int(cd.x);
+		const float2 moved = make_float2(h.x + xj.x, h.y + xj.y);
+		if (slot == own) S.ownAfter[b] = moved; else S.pos[slot] = moved;
+		H[before + q] = h;
 	}
 	if (tid == 0) {
-		const float2 xo = S.pos[own];
-		S.pos[own] = make_float2(dx.x + xo.x, dx.y + xo.y);
+		S.meta[b].x = total;
+		S.meta[b].z = own;
 	}
-	__syncthreads();
+}
+
+// Summer's part of phase b (lane 0): finish the previous particle (buffer
+// b ^ 1), then evaluate the pair (k, k-1) of particle k (list slots sl, ln,
+// pressures pk) if k-1 is in k's list; its D/2 goes to hres.
+template <class C>
+__device__ __forceinline__ void summer(DeltaSmemT<C> &S, int b, int4 sl, int4 ln, float2 pk, const StepParams &s,
+                                       float2 &hres) {
+	const int prev = S.meta[b ^ 1].z;
+	const float2 xp = finish_particle<C>(S, b ^ 1, hres);
+	hres = make_float2(0.0f, 0.0f);
+	const bool inList = (prev >= sl.x && prev < sl.x + ln.x) || (prev >= sl.y && prev < sl.y + ln.y) ||
+	                    (prev >= sl.z && prev < sl.z + ln.z);
+	if (!inList) return;
+	const float2 xk = S.pos[sl.w];
+	const float rx = xp.x - xk.x, ry = xp.y - xk.y;
+	const float r2 = rx * rx + ry * ry;
+	if (r2 < s.h2) {
+		const float2 h = delta_half(xp, xk, r2, pk, s);
+		S.pos[prev] = make_float2(h.x + xp.x, h.y + xp.y);
+		hres = h;
+	}
 }
 
 // Process particles [p0, p1) (old numbers) in order: one staged region if
-// it fits, otherwise one 3x3 region per particle.  Per-particle inputs (new
-// cell, new number, pressure) are prefetched in chunks, off the serial path.
+// it fits (pipelined), otherwise one 3x3 region per particle.  Per-particle
+// inputs (new cell, new number, pressure, list slots) are prefetched in
+// chunks, off the serial path.
 template <class C>
 __device__ __forceinline__ void relax_group(DeltaSmemT<C> &S, int p0, int p1, int bx0, int by0, int bx1, int by1,
                                             const Particles &Q, const SimTables &T, const StepParams &s,
                                             int cellBase, int tid) {
 	constexpr int kDT = C::kWarps * kWarp;
+	constexpr int kP = DeltaSmemT<C>::kProd;
+	const int warp = tid / kWarp, lane = tid & (kWarp - 1);
 	Region R;
 	R.x0 = max(bx0 - 1, 0);
 	R.y0 = max(by0 - 1, 0);
 	R.x1 = min(bx1 + 1, s.gx - 1);
 	R.y1 = min(by1 + 1, s.gy - 1);
 	const bool staged = stage_region<C>(S, R, Q, T, s, cellBase, tid);
+	bool pending = false;  // the previous particle still needs its sum (buffer ph ^ 1)
+	int ph = 0;
+	float2 hres = make_float2(0.0f, 0.0f);  // summer: D/2 of the pending particle's reserved pair
 	for (int c0 = p0; c0 < p1; c0 += C::kPrefetch) {
 		const int c1 = min(p1, c0 + C::kPrefetch);
 		for (int k = c0 + tid; k < c1; k += kDT) {
 			const int jk = T.newLabel[k];
-			S.pnc[k - c0] = T.newCell[k];
-			S.pjk[k - c0] = jk;
+			const int nc = T.newCell[k];
 			S.ppk[k - c0] = Q.press[jk];
+			if (staged) {
+				particle_slots<C>(S, R, nc, jk, s, cellBase, T.error, S.pslot[k - c0], S.plen[k - c0]);
+			} else {
+				S.pnc[k - c0] = nc;
+				S.pjk[k - c0] = jk;
+			}
 		}
 		__syncthreads();
 		for (int k = c0; k < c1; ++k) {
-			const int nc = S.pnc[k - c0], jk = S.pjk[k - c0];
 			const float2 pk = S.ppk[k - c0];
 			if (staged) {
-				relax_particle<C>(S, R, nc, jk, pk, T, s, cellBase, tid);
+				const int4 sl = S.pslot[k - c0], ln = S.plen[k - c0];
+				if (C::kPipelined && sl.w >= 0 && ln.x + ln.y + ln.z <= DeltaSmemT<C>::kPass) {
+					const int b = (ph & 1) % DeltaSmemT<C>::kPhases;
+					if (warp < kP) {
+						produce<C>(S, b, sl, ln, pk, pending ? S.meta[b ^ 1].z : -1, s, tid);
+					} else if (pending && lane == 0) {
+						summer<C>(S, b, sl, ln, pk, s, hres);
+					}
+					__syncthreads();
+					pending = true;
+					++ph;
+					continue;
+				}
+				// Drain the pipeline, then relax this particle on the whole block.
+				if (C::kPipelined && pending && warp == kP && lane == 0) finish_particle<C>(S, (ph & 1) ^ 1, hres);
+				__syncthreads();
+				pending = false;
+				relax_particle<C>(S, sl, ln, pk, s, tid);
 				continue;
 			}
+			const int nc = S.pnc[k - c0], jk = S.pjk[k - c0];
 			Region R1;
 			const int x = (nc - cellBase) % s.gx, y = (nc - cellBase) / s.gx;
 			R1.x0 = max(x - 1, 0);
@@ -1164,12 +1381,16 @@ __device__ __forceinline__ void relax_group(DeltaSmemT<C> &S, int p0, int p1, in
 				__syncthreads();
 				continue;
 			}
-			relax_particle<C>(S, R1, nc, jk, pk, T, s, cellBase, tid);
+			if (tid == 0) particle_slots<C>(S, R1, nc, jk, s, cellBase, T.error, S.oneSlot, S.oneLen);
+			__syncthreads();
+			relax_particle<C>(S, S.oneSlot, S.oneLen, pk, s, tid);
 			write_back_owned<C>(S, R1, Q, tid);
 			__syncthreads();
 		}
 		__syncthreads();
 	}
+	if (C::kPipelined && pending && warp == kP && lane == 0) finish_particle<C>(S, (ph & 1) ^ 1, hres);
+	__syncthreads();
 	if (staged) write_back_owned<C>(S, R, Q, tid);
 }
 

@@ -5,9 +5,9 @@
 
 namespace sphgb {
 
-// Shapes of the two ordered sweeps (one task per block).  Wide: four warps
-// per task, buffers for the largest lists the reference accepts (short
-// critical path for one scene).  Lean: two warps and smaller buffers (more
+// Shapes of the two ordered sweeps (one task per block).  Wide: more warps
+// per task and buffers for the largest lists the reference accepts (short
+// critical path for one scene).  Lean: fewer warps and smaller buffers (more
 // tasks per SM for many scenes).  Results do not depend on the shape.
 struct ViscWide {
 	static constexpr int kWarps = 4, kProducers = 3 * kWarp, kGeom = kStageCap, kMinBlocks = 4;
@@ -17,12 +17,20 @@ struct ViscLean {
 	static constexpr int kWarps = 2, kProducers = kWarp, kGeom = 256, kMinBlocks = 8;
 	static constexpr bool kBranchy = true;
 };
+// Delta sweep.  Pipelined shapes run kWarps - 1 producer warps and one
+// summer warp per task; the others relax one particle at a time on the
+// whole block.  kChainW in-range pairs are buffered per warp; a particle's
+// list is relaxed in the pipeline when it has at most (kWarps - 1) * kChainW
+// entries.  Wide: pipelined, eight warps (short per-particle latency for one
+// scene).  Lean: two warps, not pipelined, smaller staging (more tasks per SM
+// for many scenes).
 struct DeltaWide {
-	static constexpr int kWarps = 4, kStage = kDeltaStageCap, kChain = kDeltaChainCap, kPrefetch = 128,
-	                     kMinBlocks = 4;
+	static constexpr int kWarps = 8, kStage = kDeltaStageCap, kChainW = 128, kPrefetch = 128, kMinBlocks = 2;
+	static constexpr bool kPipelined = true;
 };
 struct DeltaLean {
-	static constexpr int kWarps = 2, kStage = 1536, kChain = 256, kPrefetch = 64, kMinBlocks = 8;
+	static constexpr int kWarps = 2, kStage = 1536, kChainW = 192, kPrefetch = 64, kMinBlocks = 8;
+	static constexpr bool kPipelined = false;
 };
 constexpr int kDensWarps = 8;
 constexpr int kGridWarps = 4;

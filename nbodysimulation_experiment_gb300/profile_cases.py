@@ -14,7 +14,7 @@ import sys
 import numpy as np
 
 from . import learned, scenes
-from .simulation import BatchSimulation, Mpnn, Simulation
+from .simulation import DELTA_WARPS, VISC_WARPS, BatchSimulation, Mpnn, Simulation
 
 
 def springs(updates: int = 3) -> None:
@@ -41,13 +41,13 @@ def mpnn(steps: int = 3) -> None:
 
 
 def batched(updates: int = 3) -> None:
-    """64 scenes of the batched workload's distribution, lean (2-warp) sweep
-    shapes with 8 resident blocks per SM."""
+    """64 scenes of the batched workload's distribution, lean sweep shapes
+    with 8 resident blocks per SM."""
     mix = scenes.batch_scenes(count=64, seed=11)
     batch = BatchSimulation(mix)
     batch.update(float(scenes.DT))
-    sms = batch.sweep_shape()[1] // 4  # the default shape runs 4 blocks per SM
-    batch.set_sweep_shape((2, 8 * sms, 2, 8 * sms))
+    sms = batch.sweep_shape()[1] // 4  # the default viscosity shape runs 4 blocks per SM
+    batch.set_sweep_shape((VISC_WARPS[1], 8 * sms, DELTA_WARPS[1], 8 * sms))
     for _ in range(updates):
         batch.update(float(scenes.DT))
     batch.synchronize()

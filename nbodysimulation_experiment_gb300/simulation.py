@@ -95,6 +95,10 @@ class SpringParams(ctypes.Structure):
 
 
 SPRING_SLOTS = 16
+#: Warps per task of the ordered sweeps' two launch shapes, (wide, lean):
+#: the values ``sph_set_sweep_shape`` accepts (csrc/sph_kernels.cuh).
+VISC_WARPS = (4, 2)
+DELTA_WARPS = (8, 2)
 
 
 class BodyDesc(ctypes.Structure):
@@ -475,6 +479,8 @@ class Simulation:
         return tuple(int(v) for v in shape)
 
     def sweep_shape(self) -> Tuple[int, int, int, int]:
+        """(viscosity warps, viscosity blocks, delta warps, delta blocks); the
+        warp counts name the shapes (``VISC_WARPS``, ``DELTA_WARPS``)."""
         shape = np.zeros(4, np.int32)
         self._call("sph_get_sweep_shape", shape.ctypes.data)
         return tuple(int(v) for v in shape)

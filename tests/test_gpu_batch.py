@@ -15,6 +15,7 @@ import pytest
 
 import nbodysimulation_experiment_gb300 as pkg
 from nbodysimulation_experiment_gb300 import scenes, simulation
+from nbodysimulation_experiment_gb300.simulation import DELTA_WARPS, VISC_WARPS
 
 pytestmark = pytest.mark.gpu
 
@@ -138,7 +139,7 @@ def test_autotune_keeps_results_and_state():
         batch.update(float(scenes.DT))
         if tune:
             shape = batch.autotune(float(scenes.DT))
-            assert shape[0] in (2, 4) and shape[2] in (2, 4) and shape[1] > 0 and shape[3] > 0
+            assert shape[0] in VISC_WARPS and shape[2] in DELTA_WARPS and shape[1] > 0 and shape[3] > 0
         for _ in range(10):
             batch.update(float(scenes.DT))
         runs.append([batch.dump_state(k) for k in range(len(mix))])
@@ -162,10 +163,12 @@ def _run_with_shape(scene, shape, steps):
     return st
 
 
-@pytest.mark.parametrize("shape", [(2, None, 2, None), (2, 152, 4, 152), (4, 152 * 3, 2, 152 * 5)])
+@pytest.mark.parametrize("shape", [(VISC_WARPS[1], None, DELTA_WARPS[1], None),
+                                   (VISC_WARPS[1], 152, DELTA_WARPS[0], 152),
+                                   (VISC_WARPS[0], 152 * 3, DELTA_WARPS[1], 152 * 5)])
 def test_sweep_shapes_give_identical_results(shape):
-    """Lean (2-warp) and wide (4-warp) sweeps, with any resident block count,
-    compute the same update."""
+    """Lean and wide sweeps, with any resident block count, compute the same
+    update."""
     scene = scenes.scaled_block(64, seed=13)
     want = _run_with_shape(scene, None, 12)
     got = _run_with_shape(scene, shape, 12)
@@ -181,5 +184,5 @@ def test_lean_viscosity_with_long_pair_lists():
     scene = scenes.Scene("dense", scenes.REF_WIDTH, scenes.REF_HEIGHT, pos,
                          scenes.box_planes(scenes.REF_WIDTH, scenes.REF_HEIGHT))
     want = _run_with_shape(scene, None, 6)
-    got = _run_with_shape(scene, (2, None, 2, None), 6)
+    got = _run_with_shape(scene, (VISC_WARPS[1], None, DELTA_WARPS[1], None), 6)
     _assert_same_state(got, want, "dense")
