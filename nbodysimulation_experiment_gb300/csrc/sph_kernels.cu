@@ -248,31 +248,86 @@ __device__ __forceinline__ void visc_geometry(ViscSmemT<C> &S, int buf, int slot
 // before this pair's store.  The impulse (f n * 0.5) * dt is computed as
 // (f n) * (0.5 dt): 0.5 dt is exact and halving is exact, so both round the
 // same real product once (unless |f n| < 2^-125).
-template <class C>
-__device__ __forceinline__ void visc_pair(ViscSmemT<C> &S, int j, float2 n, float o, float2 vj, float2 &vi,
-                                          const StepParams &s, float hdt) {
-	// Only approaching pairs (u > 0) exchange an impulse.  The wide shape
-	// (latency) computes it unconditionally and selects; the lean shape
-	// (issue-bound with many chains per SM) skips it.
+template <bool kBranchy>
+__device__ __forceinline__ void visc_pair(float2 *vel, int j, float2 n, float o, float2 vj, float2 &vi, float sigma,
+                                          float beta, float hdt) {
+	// Only approaching pairs (u > 0) exchange an impulse: computed
+	// unconditionally and selected, or (kBranchy) skipped.
 	const float uu = (vi.x - vj.x) * n.x + (vi.y - vj.y) * n.y;
-	if (C::kBranchy) {
+	if (kBranchy) {
 		if (uu > 0.0f) {
-			const float f = o * (s.sigma * uu + s.beta * (uu * uu));
+			const float f = o * (sigma * uu + beta * (uu * uu));
 			const float ix = (f * n.x) * hdt;
 			const float iy = (f * n.y) * hdt;
 			vi.x = vi.x - ix;
 			vi.y = vi.y - iy;
-			S.vel[j] = make_float2(ix + vj.x, iy + vj.y);
+			vel[j] = make_float2(ix + vj.x, iy + vj.y);
 		}
 		return;
 	}
-	const float f = o * (s.sigma * uu + s.beta * (uu * uu));
+	const float f = o * (sigma * uu + beta * (uu * uu));
 	const float ix = (f * n.x) * hdt;
 	const float iy = (f * n.y) * hdt;
 	const bool ap = uu > 0.0f;
 	vi.x = ap ? vi.x - ix : vi.x;
 	vi.y = ap ? vi.y - iy : vi.y;
-	S.vel[j] = ap ? make_float2(ix + vj.x, iy + vj.y) : vj;
+	vel[j] = ap ? make_float2(ix + vj.x, iy + vj.y) : vj;
+}
+
+// The chain over m buffered pairs G (slot, unit vector, 1 - q) with the
+// velocities vel.  Software pipeline: the geometry and partner velocities of
+// the next four pairs are loaded while the chain runs over the current four.
+template <bool kBranchy>
+__device__ __forceinline__ void visc_run(float2 *vel, const float4 *G, int m, float2 &vi, float sigma, float beta,
+                                         float hdt) {
+	float4 g[4];
+	float2 vj[4];
+#pragma unroll
+	for (int u = 0; u < 4; ++u) g[u] = u < m ? G[u] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+	for (int u = 0; u < 4; ++u) vj[u] = vel[__float_as_int(g[u].x)];
+	int q = 0;
+	for (; q + 8 <= m; q += 4) {
+		float4 gn[4];
+		float2 vn[4];
+#pragma unroll
+		for (int u = 0; u < 4; ++u) gn[u] = G[q + 4 + u];
+#pragma unroll
+		for (int u = 0; u < 4; ++u) vn[u] = vel[__float_as_int(gn[u].x)];
+#pragma unroll
+		for (int u = 0; u < 4; ++u)
+			visc_pair<kBranchy>(vel, __float_as_int(g[u].x), make_float2(g[u].y, g[u].z), g[u].w, vj[u], vi, sigma,
+			                    beta, hdt);
+#pragma unroll
+		for (int u = 0; u < 4; ++u) {
+			g[u] = gn[u];
+			vj[u] = vn[u];
+		}
+	}
+	// At most seven pairs left, the first four of them loaded.
+	if (q + 4 <= m) {
+		float4 gn[4];
+		float2 vn[4];
+#pragma unroll
+		for (int u = 0; u < 4; ++u) gn[u] = q + 4 + u < m ? G[q + 4 + u] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+		for (int u = 0; u < 4; ++u) vn[u] = vel[__float_as_int(gn[u].x)];
+#pragma unroll
+		for (int u = 0; u < 4; ++u)
+			visc_pair<kBranchy>(vel, __float_as_int(g[u].x), make_float2(g[u].y, g[u].z), g[u].w, vj[u], vi, sigma,
+			                    beta, hdt);
+#pragma unroll
+		for (int u = 0; u < 4; ++u) {
+			g[u] = gn[u];
+			vj[u] = vn[u];
+		}
+		q += 4;
+	}
+#pragma unroll
+	for (int u = 0; u < 4; ++u)
+		if (q + u < m)
+			visc_pair<kBranchy>(vel, __float_as_int(g[u].x), make_float2(g[u].y, g[u].z), g[u].w, vj[u], vi, sigma,
+			                    beta, hdt);
 }
 
 template <class C>
@@ -294,61 +349,13 @@ __device__ __forceinline__ void visc_chain(ViscSmemT<C> &S, int buf, int slot, i
 			float len = r;
 			if (len == 0.0f) len = 1.0f;
 			const float inv = 1.0f / len;
-			visc_pair(S, e, make_float2(rx * inv, ry * inv), 1.0f - qq, S.vel[e], vi, s, hdt);
+			visc_pair<C::kBranchy>(S.vel, e, make_float2(rx * inv, ry * inv), 1.0f - qq, S.vel[e], vi, s.sigma,
+			                       s.beta, hdt);
 		}
 		S.vel[slot] = vi;
 		return;
 	}
-	// Software pipeline: the geometry and partner velocities of the next four
-	// pairs are loaded while the chain runs over the current four.  Each slot
-	// occurs once per list, so a prefetched velocity is never one this
-	// particle has already changed.
-	const float4 *G = S.geo[buf];
-	float4 g[4];
-	float2 vj[4];
-#pragma unroll
-	for (int u = 0; u < 4; ++u) g[u] = u < m ? G[u] : make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-	for (int u = 0; u < 4; ++u) vj[u] = S.vel[__float_as_int(g[u].x)];
-	int q = 0;
-	for (; q + 8 <= m; q += 4) {
-		float4 gn[4];
-		float2 vn[4];
-#pragma unroll
-		for (int u = 0; u < 4; ++u) gn[u] = G[q + 4 + u];
-#pragma unroll
-		for (int u = 0; u < 4; ++u) vn[u] = S.vel[__float_as_int(gn[u].x)];
-#pragma unroll
-		for (int u = 0; u < 4; ++u)
-			visc_pair(S, __float_as_int(g[u].x), make_float2(g[u].y, g[u].z), g[u].w, vj[u], vi, s, hdt);
-#pragma unroll
-		for (int u = 0; u < 4; ++u) {
-			g[u] = gn[u];
-			vj[u] = vn[u];
-		}
-	}
-	// At most seven pairs left, the first four of them loaded.
-	if (q + 4 <= m) {
-		float4 gn[4];
-		float2 vn[4];
-#pragma unroll
-		for (int u = 0; u < 4; ++u) gn[u] = q + 4 + u < m ? G[q + 4 + u] : make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-		for (int u = 0; u < 4; ++u) vn[u] = S.vel[__float_as_int(gn[u].x)];
-#pragma unroll
-		for (int u = 0; u < 4; ++u)
-			visc_pair(S, __float_as_int(g[u].x), make_float2(g[u].y, g[u].z), g[u].w, vj[u], vi, s, hdt);
-#pragma unroll
-		for (int u = 0; u < 4; ++u) {
-			g[u] = gn[u];
-			vj[u] = vn[u];
-		}
-		q += 4;
-	}
-#pragma unroll
-	for (int u = 0; u < 4; ++u)
-		if (q + u < m)
-			visc_pair(S, __float_as_int(g[u].x), make_float2(g[u].y, g[u].z), g[u].w, vj[u], vi, s, hdt);
+	visc_run<C::kBranchy>(S.vel, S.geo[buf], m, vi, s.sigma, s.beta, hdt);
 	S.vel[slot] = vi;
 }
 
@@ -450,6 +457,332 @@ __global__ void __launch_bounds__(C::kWarps * kWarp, C::kMinBlocks) k_viscosity(
 		__syncthreads();
 		stamp(T, 0, t, 3, tid);
 		if (tid == 0) st_release(&T.done[t], 1u);
+	}
+}
+
+// ---------------------------------------------------------------------------
+// Viscosity sweep, many chains per block (the lean shape, ViscLean): the
+// same tasks, waits and arithmetic as k_viscosity, laid out for throughput.
+// A block holds kSlots tasks at once.  Lane s of warp 0 runs the ordered
+// velocity chain of slot s's current particle (the slots' chains share one
+// instruction stream), while producer warp 1 + (s % kProd) looks after slot
+// s: it claims a task, polls the task's earlier conflicting tasks (without
+// blocking), stages the velocities of its 3x3 block, computes the pair
+// geometry of the slot's next particle (positions, which this pass does not
+// change, are read through L1), and writes the velocities back and releases
+// the task when its chain is done.  The block advances in phases: one
+// particle per running slot per phase.
+template <class C>
+struct ViscSlotT {
+	float2 vel[kStageCap];    // velocities of the 3x3 block, list order
+	float4 geo[2][C::kGeom];  // per buffer: in-range pairs (slot, unit vector, 1 - q) of one particle
+	float4 pad;               // consecutive slots start 16 bytes apart in the bank space
+};
+template <class C>
+struct ViscMultiSmemT {
+	ViscSlotT<C> slot[C::kSlots];
+	int segStart[C::kSlots][9], segOff[C::kSlots][9];
+	int state[C::kSlots], task[C::kSlots], first[C::kSlots], cnt[C::kSlots], own[C::kSlots], L[C::kSlots],
+	    k[C::kSlots], cell[C::kSlots];
+	int m[C::kSlots][2];
+	float h2[C::kSlots], invH[C::kSlots], sigma[C::kSlots], beta[C::kSlots], hdt[C::kSlots];
+	unsigned long long waitSince[C::kSlots];
+	int exhausted, exit;
+};
+
+namespace {
+
+enum : int { kSlotFree = 0, kSlotWait = 1, kSlotStaged = 2, kSlotRun = 3, kSlotDone = 4 };
+
+// Pair geometry of particle k of slot s (one warp): in-range pairs in list
+// order (sph.h:497-505), compacted first, then the square roots and
+// divisions over the dense list.
+template <class C>
+__device__ __forceinline__ void slot_geometry(ViscMultiSmemT<C> &S, int s, int k, const Particles &P, int lane) {
+	const int buf = k & 1;
+	float4 *G = S.slot[s].geo[buf];
+	int segStart[9], segOff[9];
+#pragma unroll
+	for (int q = 0; q < 9; ++q) {
+		segStart[q] = S.segStart[s][q];
+		segOff[q] = S.segOff[s][q];
+	}
+	const int L = S.L[s];
+	const float h2 = S.h2[s], invH = S.invH[s];
+	const float2 xi = __ldg(&P.pos[S.first[s] + k]);
+	int m = 0;
+	for (int b0 = 0; b0 < L; b0 += 4 * kWarp) {
+		float2 xj[4];
+#pragma unroll
+		for (int u = 0; u < 4; ++u) {
+			const int e = b0 + u * kWarp + lane;
+			xj[u] = e < L ? __ldg(&P.pos[seg_src<9>(e, segOff, segStart)]) : make_float2(0.f, 0.f);
+		}
+#pragma unroll
+		for (int u = 0; u < 4; ++u) {
+			const int e = b0 + u * kWarp + lane;
+			const float rx = xj[u].x - xi.x, ry = xj[u].y - xi.y;
+			const float r2 = rx * rx + ry * ry;
+			const bool in = e < L && r2 < h2;
+			const unsigned mask = __ballot_sync(kFull, in);
+			const int at = m + __popc(mask & lanemask_lt());
+			if (in && at < C::kGeom) G[at] = make_float4(__int_as_float(e), rx, ry, r2);
+			m += __popc(mask);
+		}
+	}
+	__syncwarp();
+	const int mm = min(m, C::kGeom);
+	for (int q = lane; q < mm; q += kWarp) {
+		const float4 g = G[q];
+		const float r = sqrtf(g.w);
+		const float qq = r * invH;
+		float len = r;  // Vec2Length(Rij) == rij
+		if (len == 0.0f) len = 1.0f;
+		const float inv = 1.0f / len;
+		G[q] = make_float4(g.x, g.y * inv, g.z * inv, 1.0f - qq);
+	}
+	if (lane == 0) S.m[s][buf] = m;
+}
+
+// Claim the next task into slot s (one warp).  Returns false when none is
+// left.
+template <class C>
+__device__ __forceinline__ bool slot_claim(ViscMultiSmemT<C> &S, int s, const SimTables &T, int nLive, int lane) {
+	int i = 0;
+	if (lane == 0) i = atomicAdd(&T.taskCounter[0], 1);
+	i = __shfl_sync(kFull, i, 0);
+	if (i >= nLive) return false;
+	const int t = T.liveTask[i];
+	const int c = T.taskCell[t];
+	const SceneDev &sc = T.scenes[T.sceneOfCell[c]];
+	const int base = sc.cellBase, gx = sc.p.gx, gy = sc.p.gy;
+	const int cx = (c - base) % gx, cy = (c - base) / gx;
+	// Segments of the 3x3 block in list order (lanes 0..8, then a scan).
+	int st = 0, nn = 0;
+	if (lane < 9) {
+		const int x = cx + lane % 3 - 1, y = cy + lane / 3 - 1;
+		if (x >= 0 && x < gx && y >= 0 && y < gy) {
+			const int c2 = base + y * gx + x;
+			st = T.cellStart[c2];
+			nn = T.cellCount[c2];
+		}
+	}
+	int incl = nn;
+#pragma unroll
+	for (int o = 1; o < 16; o <<= 1) {
+		const int v = __shfl_up_sync(kFull, incl, o);
+		if (lane >= o) incl += v;
+	}
+	if (lane < 9) {
+		S.segStart[s][lane] = st;
+		S.segOff[s][lane] = incl - nn;
+	}
+	const int L = __shfl_sync(kFull, incl, 8);
+	const int own = __shfl_sync(kFull, incl - nn, 4);
+	if (lane == 0) {
+		S.task[s] = t;
+		S.cell[s] = c;
+		S.first[s] = T.cellStart[c];
+		S.cnt[s] = T.cellCount[c];
+		S.own[s] = own;
+		S.L[s] = L;
+		S.h2[s] = sc.p.h2;
+		S.invH[s] = sc.p.invH;
+		S.sigma[s] = sc.p.sigma;
+		S.beta[s] = sc.p.beta;
+		S.hdt[s] = 0.5f * sc.p.dt;
+		S.state[s] = kSlotWait;
+		S.waitSince[s] = global_ns();
+	}
+	__syncwarp();
+	return true;
+}
+
+// One non-blocking poll of slot s's earlier conflicting tasks (cells of the
+// scene at most two apart, as k_viscosity).  True when all are done.
+template <class C>
+__device__ __forceinline__ bool slot_ready(ViscMultiSmemT<C> &S, int s, const SimTables &T, int lane) {
+	const int t = S.task[s], c = S.cell[s];
+	const SceneDev &sc = T.scenes[T.sceneOfCell[c]];
+	const int base = sc.cellBase, gx = sc.p.gx, gy = sc.p.gy;
+	const int cx = (c - base) % gx, cy = (c - base) / gx;
+	bool pending = false;
+	const int x = cx + lane % 5 - 2, y = cy + lane / 5 - 2;
+	if (lane < 25 && lane != 12 && x >= 0 && x < gx && y >= 0 && y < gy) {
+		const int c2 = base + y * gx + x;
+		const int r2 = T.taskOfCell[c2];
+		if (r2 < t && T.cellCount[c2] > 0) pending = ld_acquire(&T.done[r2]) == 0u;
+	}
+	return !__any_sync(kFull, pending);
+}
+
+template <class C>
+__device__ __forceinline__ void slot_copy_vel(ViscMultiSmemT<C> &S, int s, const Particles &P, int lane, bool in) {
+	int segStart[9], segOff[9];
+#pragma unroll
+	for (int q = 0; q < 9; ++q) {
+		segStart[q] = S.segStart[s][q];
+		segOff[q] = S.segOff[s][q];
+	}
+	const int L = S.L[s];
+	float2 *V = S.slot[s].vel;
+	for (int b0 = 0; b0 < L; b0 += 4 * kWarp) {
+		if (in) {
+			float2 v[4];
+#pragma unroll
+			for (int u = 0; u < 4; ++u) {
+				const int e = b0 + u * kWarp + lane;
+				if (e < L) v[u] = __ldcg(&P.vel[seg_src<9>(e, segOff, segStart)]);
+			}
+#pragma unroll
+			for (int u = 0; u < 4; ++u) {
+				const int e = b0 + u * kWarp + lane;
+				if (e < L) V[e] = v[u];
+			}
+		} else {
+#pragma unroll
+			for (int u = 0; u < 4; ++u) {
+				const int e = b0 + u * kWarp + lane;
+				if (e < L) __stcg(&P.vel[seg_src<9>(e, segOff, segStart)], V[e]);
+			}
+		}
+	}
+}
+
+// The producer warp's turn for slot s in one phase.
+template <class C>
+__device__ __forceinline__ void slot_produce(ViscMultiSmemT<C> &S, int s, const Particles &P, const SimTables &T,
+                                             int nLive, int lane) {
+	int state = S.state[s];
+	if (state == kSlotDone) {
+		// Chain finished: write the block's velocities back and release.
+		slot_copy_vel<C>(S, s, P, lane, false);
+		__threadfence();
+		__syncwarp();
+		if (lane == 0) {
+			st_release(&T.done[S.task[s]], 1u);
+			S.state[s] = kSlotFree;
+		}
+		__syncwarp();
+		state = kSlotFree;
+	}
+	if (state == kSlotFree) {
+		if (__shfl_sync(kFull, S.exhausted, 0)) return;
+		if (!slot_claim<C>(S, s, T, nLive, lane)) {
+			if (lane == 0) S.exhausted = 1;
+			return;
+		}
+		state = kSlotWait;
+	}
+	if (state == kSlotWait) {
+		if (!slot_ready<C>(S, s, T, lane)) {
+			if (lane == 0 && global_ns() - S.waitSince[s] > kWaitLimitNs) {
+				atomicOr(T.error, kErrTimeout);
+				atomicExch(T.abort, 1u);
+			}
+			return;
+		}
+		if (S.L[s] > kStageCap) {
+			// The block does not fit: flag it and release the task untouched.
+			if (lane == 0) {
+				atomicOr(T.error, kErrStageOverflow);
+				st_release(&T.done[S.task[s]], 1u);
+				S.state[s] = kSlotFree;
+			}
+			__syncwarp();
+			return;
+		}
+		slot_copy_vel<C>(S, s, P, lane, true);
+		slot_geometry<C>(S, s, 0, P, lane);
+		if (lane == 0) S.state[s] = kSlotStaged;
+		__syncwarp();
+		return;
+	}
+	if (state == kSlotRun) {
+		const int k = S.k[s];
+		if (k + 1 < S.cnt[s]) slot_geometry<C>(S, s, k + 1, P, lane);
+	}
+}
+
+// The chain of slot s's current particle (lane s of warp 0).
+template <class C>
+__device__ __forceinline__ void slot_chain(ViscMultiSmemT<C> &S, int s, const Particles &P) {
+	const int k = S.k[s], buf = k & 1, m = S.m[s][buf];
+	const int own = S.own[s] + k;
+	float2 *V = S.slot[s].vel;
+	const float sigma = S.sigma[s], beta = S.beta[s], hdt = S.hdt[s];
+	float2 vi = V[own];
+	if (m > C::kGeom) {
+		// More in-range pairs than the geometry buffer holds: the same pair
+		// geometry (sph.h:497-505), computed here in list order.
+		int segStart[9], segOff[9];
+#pragma unroll
+		for (int q = 0; q < 9; ++q) {
+			segStart[q] = S.segStart[s][q];
+			segOff[q] = S.segOff[s][q];
+		}
+		const int L = S.L[s];
+		const float h2 = S.h2[s], invH = S.invH[s];
+		const float2 xi = __ldg(&P.pos[S.first[s] + k]);
+		for (int e = 0; e < L; ++e) {
+			const float2 xj = __ldg(&P.pos[seg_src<9>(e, segOff, segStart)]);
+			const float rx = xj.x - xi.x, ry = xj.y - xi.y;
+			const float r2 = rx * rx + ry * ry;
+			if (!(r2 < h2)) continue;
+			const float r = sqrtf(r2);
+			const float qq = r * invH;
+			float len = r;
+			if (len == 0.0f) len = 1.0f;
+			const float inv = 1.0f / len;
+			visc_pair<false>(V, e, make_float2(rx * inv, ry * inv), 1.0f - qq, V[e], vi, sigma, beta, hdt);
+		}
+	} else {
+		visc_run<false>(V, S.slot[s].geo[buf], m, vi, sigma, beta, hdt);
+	}
+	V[own] = vi;
+}
+
+}  // namespace
+
+template <class C>
+__global__ void __launch_bounds__(C::kWarps * kWarp, C::kMinBlocks) k_viscosity_multi(Totals tt, Particles P,
+                                                                                     SimTables T) {
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	ViscMultiSmemT<C> &S = *reinterpret_cast<ViscMultiSmemT<C> *>(smem_raw);
+	const int tid = threadIdx.x, warp = tid / kWarp, lane = tid & (kWarp - 1);
+	const int nLive = *T.nLive;
+	if (tid < C::kSlots) {
+		S.state[tid] = kSlotFree;
+		S.k[tid] = 0;
+	}
+	if (tid == 0) S.exhausted = 0;
+	__syncthreads();
+	for (;;) {
+		// Bookkeeping of the phase just ended.
+		if (tid == 0) {
+			bool busy = false;
+			for (int s = 0; s < C::kSlots; ++s) {
+				const int st = S.state[s];
+				if (st == kSlotStaged) {
+					S.state[s] = kSlotRun;
+					S.k[s] = 0;
+				} else if (st == kSlotRun) {
+					const int k = S.k[s] + 1;
+					S.k[s] = k;
+					if (k == S.cnt[s]) S.state[s] = kSlotDone;
+				}
+				busy = busy || S.state[s] != kSlotFree;
+			}
+			S.exit = (!busy && S.exhausted) || ld_acquire(T.abort) != 0u;
+		}
+		__syncthreads();
+		if (S.exit) break;
+		if (warp == 0) {
+			if (lane < C::kSlots && S.state[lane] == kSlotRun) slot_chain<C>(S, lane, P);
+		} else {
+			for (int s = warp - 1; s < C::kSlots; s += C::kProd) slot_produce<C>(S, s, P, T, nLive, lane);
+		}
+		__syncthreads();
 	}
 }
 
@@ -1731,8 +2064,8 @@ cudaError_t sweep_attributes() {
 	cudaError_t e = cudaFuncSetAttribute(k_viscosity<ViscWide>, cudaFuncAttributeMaxDynamicSharedMemorySize,
 	                                     (int)visc_smem_bytes<ViscWide>());
 	if (e == cudaSuccess)
-		e = cudaFuncSetAttribute(k_viscosity<ViscLean>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-		                         (int)visc_smem_bytes<ViscLean>());
+		e = cudaFuncSetAttribute(k_viscosity_multi<ViscLean>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                         (int)sizeof(ViscMultiSmemT<ViscLean>));
 	if (e == cudaSuccess)
 		e = cudaFuncSetAttribute(k_delta<DeltaWide>, cudaFuncAttributeMaxDynamicSharedMemorySize,
 		                         (int)delta_smem_bytes<DeltaWide>());
@@ -1743,9 +2076,9 @@ cudaError_t sweep_attributes() {
 }
 
 cudaError_t sweep_occupancy(bool viscLean, bool deltaLean, int *occV, int *occD) {
-	cudaError_t e = viscLean ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(occV, k_viscosity<ViscLean>,
+	cudaError_t e = viscLean ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(occV, k_viscosity_multi<ViscLean>,
 	                                                                         ViscLean::kWarps * kWarp,
-	                                                                         visc_smem_bytes<ViscLean>())
+	                                                                         sizeof(ViscMultiSmemT<ViscLean>))
 	                         : cudaOccupancyMaxActiveBlocksPerMultiprocessor(occV, k_viscosity<ViscWide>,
 	                                                                         ViscWide::kWarps * kWarp,
 	                                                                         visc_smem_bytes<ViscWide>());
@@ -1758,7 +2091,8 @@ cudaError_t sweep_occupancy(bool viscLean, bool deltaLean, int *occV, int *occD)
 
 void launch_viscosity(bool lean, int blocks, cudaStream_t st, Totals tt, Particles P, SimTables T) {
 	if (lean)
-		k_viscosity<ViscLean><<<blocks, ViscLean::kWarps * kWarp, visc_smem_bytes<ViscLean>(), st>>>(tt, P, T);
+		k_viscosity_multi<ViscLean>
+		    <<<blocks, ViscLean::kWarps * kWarp, sizeof(ViscMultiSmemT<ViscLean>), st>>>(tt, P, T);
 	else
 		k_viscosity<ViscWide><<<blocks, ViscWide::kWarps * kWarp, visc_smem_bytes<ViscWide>(), st>>>(tt, P, T);
 }

@@ -13,9 +13,10 @@ struct ViscWide {
 	static constexpr int kWarps = 4, kProducers = 3 * kWarp, kGeom = kStageCap, kMinBlocks = 4;
 	static constexpr bool kBranchy = false;
 };
+// Lean viscosity: kSlots tasks per block; warp 0's lanes run their chains,
+// kProd producer warps serve them (k_viscosity_multi).
 struct ViscLean {
-	static constexpr int kWarps = 2, kProducers = kWarp, kGeom = 256, kMinBlocks = 8;
-	static constexpr bool kBranchy = true;
+	static constexpr int kSlots = 5, kProd = 4, kWarps = 1 + kProd, kGeom = 192, kMinBlocks = 3;
 };
 // Delta sweep.  Pipelined shapes run kWarps - 1 producer warps and one
 // summer warp per task; the others relax one particle at a time on the

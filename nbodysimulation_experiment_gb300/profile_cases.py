@@ -42,12 +42,12 @@ def mpnn(steps: int = 3) -> None:
 
 def batched(updates: int = 3) -> None:
     """64 scenes of the batched workload's distribution, lean sweep shapes
-    with 8 resident blocks per SM."""
+    (3 viscosity and 8 delta blocks per SM)."""
     mix = scenes.batch_scenes(count=64, seed=11)
     batch = BatchSimulation(mix)
     batch.update(float(scenes.DT))
     sms = batch.sweep_shape()[1] // 4  # the default viscosity shape runs 4 blocks per SM
-    batch.set_sweep_shape((VISC_WARPS[1], 8 * sms, DELTA_WARPS[1], 8 * sms))
+    batch.set_sweep_shape((VISC_WARPS[1], 3 * sms, DELTA_WARPS[1], 8 * sms))
     for _ in range(updates):
         batch.update(float(scenes.DT))
     batch.synchronize()

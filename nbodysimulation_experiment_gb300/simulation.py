@@ -97,7 +97,7 @@ class SpringParams(ctypes.Structure):
 SPRING_SLOTS = 16
 #: Warps per task of the ordered sweeps' two launch shapes, (wide, lean):
 #: the values ``sph_set_sweep_shape`` accepts (csrc/sph_kernels.cuh).
-VISC_WARPS = (4, 2)
+VISC_WARPS = (4, 5)
 DELTA_WARPS = (8, 2)
 
 
