@@ -404,6 +404,9 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     step_ms, delta_ms = [], []
+    stage_names = ("time_integration", "time_viscosity_forces", "time_predict", "time_update_grid",
+                   "time_neighbor_search", "time_density_and_pressure", "time_delta_positions", "time_collisions")
+    stage_sum = dict.fromkeys(stage_names, 0.0)
     for _ in range(args.steps):
         with torch.cuda.stream(stream):
             flush.zero_()
@@ -415,7 +418,10 @@ def main():
             e1.record(stream)
         e1.synchronize()
         step_ms.append(e0.elapsed_time(e1))
-        delta_ms.append(sim.get_stats().time_delta_positions)
+        stats = sim.get_stats()
+        delta_ms.append(stats.time_delta_positions)
+        for k in stage_names:
+            stage_sum[k] += getattr(stats, k)
     torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
@@ -497,6 +503,7 @@ def main():
                        "density_error": dens_err},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(h2d)},
             "gpu_launches": int(launches),
+            "stage_ms": {k[5:]: v / args.steps for k, v in stage_sum.items()},
             "roofline": {"bound": "hbm", "kernel": "k_delta", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": traffic,
                          "algorithmic_bytes": DELTA_BYTES_PER_PARTICLE * scene.n,

@@ -487,7 +487,8 @@ struct ViscMultiSmemT {
 	int m[C::kSlots][2];
 	float h2[C::kSlots], invH[C::kSlots], sigma[C::kSlots], beta[C::kSlots], hdt[C::kSlots];
 	unsigned long long waitSince[C::kSlots];
-	int exhausted, exit;
+	int exhausted;  // no tasks left to claim
+	int aborted;    // the abort flag was seen set
 };
 
 namespace {
@@ -755,31 +756,34 @@ __global__ void __launch_bounds__(C::kWarps * kWarp, C::kMinBlocks) k_viscosity_
 		S.state[tid] = kSlotFree;
 		S.k[tid] = 0;
 	}
-	if (tid == 0) S.exhausted = 0;
+	if (tid == 0) {
+		S.exhausted = 0;
+		S.aborted = 0;
+	}
 	__syncthreads();
 	for (;;) {
-		// Bookkeeping of the phase just ended.
-		if (tid == 0) {
-			bool busy = false;
-			for (int s = 0; s < C::kSlots; ++s) {
-				const int st = S.state[s];
-				if (st == kSlotStaged) {
-					S.state[s] = kSlotRun;
-					S.k[s] = 0;
-				} else if (st == kSlotRun) {
-					const int k = S.k[s] + 1;
-					S.k[s] = k;
-					if (k == S.cnt[s]) S.state[s] = kSlotDone;
-				}
-				busy = busy || S.state[s] != kSlotFree;
+		// Bookkeeping of the phase just ended: thread s advances slot s.
+		int busy = 0;
+		if (tid < C::kSlots) {
+			int st = S.state[tid];
+			if (st == kSlotStaged) {
+				st = kSlotRun;
+				S.k[tid] = 0;
+			} else if (st == kSlotRun) {
+				const int k = S.k[tid] + 1;
+				S.k[tid] = k;
+				if (k == S.cnt[tid]) st = kSlotDone;
 			}
-			S.exit = (!busy && S.exhausted) || ld_acquire(T.abort) != 0u;
+			S.state[tid] = st;
+			busy = st != kSlotFree;
 		}
-		__syncthreads();
-		if (S.exit) break;
+		const int anyBusy = __syncthreads_or(busy);
+		if ((!anyBusy && S.exhausted) || S.aborted) break;
 		if (warp == 0) {
 			if (lane < C::kSlots && S.state[lane] == kSlotRun) slot_chain<C>(S, lane, P);
 		} else {
+			if (tid == kWarp && ld_acquire(T.abort) != 0u) S.aborted = 1;
+			__syncwarp();
 			for (int s = warp - 1; s < C::kSlots; s += C::kProd) slot_produce<C>(S, s, P, T, nLive, lane);
 		}
 		__syncthreads();
