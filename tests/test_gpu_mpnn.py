@@ -83,7 +83,9 @@ def test_training_reduces_the_loss():
     model = pkg.Mpnn(8192, seed=2)
     _samples(model, scenes.dam_break_4096(seed=1), 6)
     before = np.mean([model.eval(k) for k in range(model.sample_count)])
-    for it in range(240):
+    # Weight gradients are summed with atomics, so the trajectory varies a
+    # little from run to run; 400 steps leave a clear margin under one half.
+    for it in range(400):
         model.train_step(it % model.sample_count, 1e-3)
     after = np.mean([model.eval(k) for k in range(model.sample_count)])
     assert after < 0.5 * before, (before, after)
