@@ -212,6 +212,9 @@ def bench_batched(torch, pkg, scenes, device: int, steps: int, warmup: int):
     tuned = batch.autotune(dt)
     launches0 = batch.kernel_launches()
     ms = []
+    stage_names = ("time_integration", "time_viscosity_forces", "time_predict", "time_update_grid",
+                   "time_density_and_pressure", "time_delta_positions", "time_collisions")
+    stage_sum = dict.fromkeys(stage_names, 0.0)
     for _ in range(steps):
         with torch.cuda.stream(stream):
             e0 = torch.cuda.Event(enable_timing=True)
@@ -222,6 +225,9 @@ def bench_batched(torch, pkg, scenes, device: int, steps: int, warmup: int):
             e1.record(stream)
         e1.synchronize()
         ms.append(e0.elapsed_time(e1))
+        stats = batch.get_stats(0)  # stage times cover every scene of the batch
+        for k in stage_names:
+            stage_sum[k] += getattr(stats, k)
     batch.synchronize()
     launches = batch.kernel_launches() - launches0
     total = batch.get_particle_count()
@@ -234,6 +240,7 @@ def bench_batched(torch, pkg, scenes, device: int, steps: int, warmup: int):
     return {"value": total * steps / (sum(ms) / 1e3), "unit": UNIT, "ms_per_step": statistics.mean(ms),
             "steps": steps, "warmup": warmup, "scenes": len(mix), "particles": int(total),
             "gpu_launches": int(launches), "graphs": True,
+            "stage_ms": {k[5:]: v / steps for k, v in stage_sum.items()},
             "autotuned_shape": {"viscosity_warps": tuned[0], "viscosity_blocks": tuned[1],
                                 "delta_warps": tuned[2], "delta_blocks": tuned[3]},
             "density_error": float(np.mean(errs)),
@@ -307,6 +314,7 @@ def bench_learned(torch, pkg, scenes, device: int, args):
         scene.apply(sim)
         for _ in range(3):
             sim.update(frame / sub)
+        sim.autotune(frame / sub)
         stream = torch.cuda.ExternalStream(sim.stream())
         ms, used, errs = [], 0, []
         for f in range(args.learned_warmup + args.learned_eval_frames):

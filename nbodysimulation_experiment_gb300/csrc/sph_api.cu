@@ -96,7 +96,7 @@ struct sph_sim {
 	cudaStream_t stream = nullptr;
 	int numSMs = 0;
 	int viscBlocks = 0, deltaBlocks = 0, densBlocks = 0, gridBlocks = 0;
-	int viscLean = 0, deltaLean = 0;  // sweep shapes: 0 = wide (4 warps), 1 = lean (2 warps)
+	int viscLean = 0, deltaLean = 0;  // sweep shapes: 0 = wide, 1 = lean (sph_kernels.cuh)
 	bool batch = false;
 	int multithreading = 0;
 
@@ -1703,11 +1703,11 @@ int sph_load_springs(sph_sim *s, size_t count, const int32_t *spring_count, cons
 }
 
 // Launch-shape autotuner: the ordered sweeps are persistent kernels; each
-// has two shapes (wide: four warps per task; lean: two warps, more tasks per
-// SM) and a resident block count that trades parallel tasks against polling
-// traffic.  Every shape gives the same results (the task order fixes them),
-// so each candidate is timed on the same update from a snapshot and the
-// fastest kept for each sweep.
+// has two shapes (wide: short per-particle latency for one scene; lean: more
+// tasks per SM for many scenes) and a resident block count that trades
+// parallel tasks against polling traffic.  Every shape gives the same results
+// (the task order fixes them), so each candidate is timed on the same update
+// from a snapshot and the fastest kept for each sweep.
 int sph_autotune(sph_sim *s, float dt, int *shape) {
 	if (!s || !(dt > 0.0f)) return SPH_ERR_INVALID_ARGUMENT;
 	SPH_CUDA(cudaSetDevice(s->device));

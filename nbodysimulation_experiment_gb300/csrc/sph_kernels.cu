@@ -158,9 +158,10 @@ __global__ void k_integrate(Totals tt, Particles P, SimTables T) {
 // while warps 1..3 compute the compacted pair geometry of particle k+1
 // (positions do not change during this pass, so the geometry of every
 // particle of the task is known in advance).
-// Two shapes (ViscWide, ViscLean in sph_kernels.cuh): the lean one uses two
-// warps and keeps the pair geometry of up to 256 pairs per particle (longer
-// lists run the geometry inline in the chain), so more tasks fit on an SM.
+// This is the wide shape (ViscWide); the lean one, k_viscosity_multi below,
+// runs several tasks per block for throughput.  Both run the geometry inline
+// in the chain for particles with more in-range pairs than their geometry
+// buffer holds.
 template <class C>
 struct ViscSmemT {
 	float2 pos[kStageCap];
