@@ -1186,14 +1186,33 @@ __global__ void k_app_boxes(Totals tt, SimTables T) {
 
 // ---------------------------------------------------------------------------
 // Density and pressure (demo4.cpp:208-221): a pure gather.  One warp per new
-// cell stages the 3x3 block of the new cell arrays (the particle's neighbour
-// list, demo4.cpp:183-206), then each lane sums its particle's list in order.
+// cell; each lane sums the lists of two of the cell's particles (the 3x3
+// block of the new cell arrays, demo4.cpp:183-206) in list order.  The block
+// is staged in chunks of kDensChunk entries, so a warp needs little shared
+// memory and many warps fit on an SM.
 
+constexpr int kDensChunk = 256;
 struct DensWarp {
-	float2 pos[kStageCap];
+	float2 pos[kDensChunk];
 };
 
-__global__ void __launch_bounds__(kDensWarps * kWarp) k_density(Totals tt, Particles Q, SimTables T) {
+namespace {
+
+// One list entry for one particle (sph.h:465-476): sums in list order.
+__device__ __forceinline__ void dens_entry(float2 xj, float2 xi, float h2, float invH, float &d0, float &d1) {
+	const float rx = xj.x - xi.x, ry = xj.y - xi.y;
+	const float r2 = rx * rx + ry * ry;
+	if (r2 < h2) {
+		const float r = sqrtf(r2);
+		const float term = 1.0f - r * invH;
+		d0 = d0 + term * term;
+		d1 = d1 + term * term * term;
+	}
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kDensWarps * kWarp, 4) k_density(Totals tt, Particles Q, SimTables T) {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	DensWarp &S = reinterpret_cast<DensWarp *>(smem_raw)[threadIdx.x / kWarp];
 	const int lane = threadIdx.x & (kWarp - 1);
@@ -1207,7 +1226,7 @@ __global__ void __launch_bounds__(kDensWarps * kWarp) k_density(Totals tt, Parti
 		const int base = sc.cellBase;
 		const int cx = (c - base) % s.gx, cy = (c - base) / s.gx;
 		int segStart[9], segOff[9];
-		int L = 0, own = 0;
+		int L = 0;
 #pragma unroll
 		for (int q = 0; q < 9; ++q) {
 			const int x = cx + q % 3 - 1, y = cy + q / 3 - 1;
@@ -1219,7 +1238,6 @@ __global__ void __launch_bounds__(kDensWarps * kWarp) k_density(Totals tt, Parti
 			}
 			segStart[q] = st;
 			segOff[q] = L;
-			if (q == 4) own = L;
 			L += nn;
 		}
 		if (lane == 0) {
@@ -1230,39 +1248,44 @@ __global__ void __launch_bounds__(kDensWarps * kWarp) k_density(Totals tt, Parti
 			if (lane == 0) atomicOr(T.error, kErrStageOverflow);
 			continue;
 		}
-		for (int b0 = 0; b0 < L; b0 += 4 * kWarp) {
-			float2 xp[4];
-#pragma unroll
-			for (int u = 0; u < 4; ++u) {
-				const int e = b0 + u * kWarp + lane;
-				if (e < L) xp[u] = Q.pos[seg_src<9>(e, segOff, segStart)];
-			}
-#pragma unroll
-			for (int u = 0; u < 4; ++u) {
-				const int e = b0 + u * kWarp + lane;
-				if (e < L) S.pos[e] = xp[u];
-			}
-		}
-		__syncwarp();
+		const float h2 = s.h2, invH = s.invH;
 		const int st = T.newStart[c];
-		for (int g = 0; g < cnt; g += kWarp) {
-			const int j = g + lane;
-			if (j < cnt) {
-				const float2 xi = S.pos[own + j];
-				float d0 = 0.0f, d1 = 0.0f;
-				for (int e = 0; e < L; ++e) {
-					const float2 xj = S.pos[e];
-					const float rx = xj.x - xi.x, ry = xj.y - xi.y;
-					const float r2 = rx * rx + ry * ry;
-					if (r2 < s.h2) {
-						const float r = sqrtf(r2);
-						const float term = 1.0f - r * s.invH;
-						d0 = d0 + term * term;
-						d1 = d1 + term * term * term;
+		for (int g = 0; g < cnt; g += 2 * kWarp) {
+			const int j0 = g + lane, j1 = g + kWarp + lane;
+			// Lanes without a particle use a position no entry is in range of.
+			const float2 far = make_float2(3.0e38f, 3.0e38f);
+			const float2 xi0 = j0 < cnt ? Q.pos[st + j0] : far;
+			const float2 xi1 = j1 < cnt ? Q.pos[st + j1] : far;
+			float d00 = 0.0f, d01 = 0.0f, d10 = 0.0f, d11 = 0.0f;
+			for (int c0 = 0; c0 < L; c0 += kDensChunk) {
+				const int n = min(kDensChunk, L - c0);
+				__syncwarp();
+				for (int e = lane; e < n; e += kWarp) S.pos[e] = Q.pos[seg_src<9>(c0 + e, segOff, segStart)];
+				__syncwarp();
+				int e = 0;
+				for (; e + 4 <= n; e += 4) {
+					float2 xj[4];
+#pragma unroll
+					for (int u = 0; u < 4; ++u) xj[u] = S.pos[e + u];
+#pragma unroll
+					for (int u = 0; u < 4; ++u) {
+						dens_entry(xj[u], xi0, h2, invH, d00, d01);
+						dens_entry(xj[u], xi1, h2, invH, d10, d11);
 					}
 				}
-				Q.dens[st + j] = make_float2(d0, d1);
-				Q.press[st + j] = make_float2(s.k * (d0 - s.rho0), s.kNear * d1);
+				for (; e < n; ++e) {
+					const float2 xj = S.pos[e];
+					dens_entry(xj, xi0, h2, invH, d00, d01);
+					dens_entry(xj, xi1, h2, invH, d10, d11);
+				}
+			}
+			if (j0 < cnt) {
+				Q.dens[st + j0] = make_float2(d00, d01);
+				Q.press[st + j0] = make_float2(s.k * (d00 - s.rho0), s.kNear * d01);
+			}
+			if (j1 < cnt) {
+				Q.dens[st + j1] = make_float2(d10, d11);
+				Q.press[st + j1] = make_float2(s.k * (d10 - s.rho0), s.kNear * d11);
 			}
 		}
 		__syncwarp();
