@@ -204,6 +204,74 @@ int sph_load_state(sph_sim *sim, const sph_state_view *in);
  * that changes the simulation. */
 int sph_get_stream(sph_sim *sim, void **stream);
 int sph_device_arrays(sph_sim *sim, const void **pos, const void **vel, const void **dens, const void **press);
+
+/* Replaces the colouring and point drawing of Render (base.h:25,
+ * demo4.cpp:453-532) without a graphics API.  sph_particle_colors: RGBA
+ * (4 floats per particle) of the first `count` particles in AddParticle
+ * order, SPHGetParticleColor (sph.h:683-695) of the rest density, density,
+ * pressure and velocity.  sph_render_points: a width x height RGBA8 image of
+ * the box (row 0 at the top, pixel (x, y) spans world x in
+ * [-W/2 + x W/width, ...)); each particle colours the pixel under it with
+ * its colour rounded to 8 bits, later particles (AddParticle order) over
+ * earlier ones; empty pixels are 0.  Both act on the first scene. */
+int sph_particle_colors(sph_sim *sim, size_t count, float *rgba);
+int sph_render_points(sph_sim *sim, int width, int height, unsigned char *rgba);
+
+/* ---- Built-in scenarios (SPHScenarios[], sph.h:315-437) --------------------
+ * The reference application loads a scenario with DemoApplication::
+ * LoadScenario (app.cpp:477-534): reset stats, clear bodies, particles and
+ * emitters, set gravity and parameters, add the bodies (planes at distance
+ * dot(normal, position); segment and polygon vertices rotated by the body's
+ * orientation and moved to its position), the volumes and the emitters.
+ * sph_scenario_describe reports exactly the calls it makes, in order; its
+ * volume loop walks the first body_count entries of the scenario's
+ * zero-filled volume table (a reference quirk, app.cpp:522), so volumes past
+ * the scenario's own are empty.  Scenario parameters come from the
+ * 8-argument SPHParameters constructor, which keeps kSPHKernelHeight and
+ * kSPHRestDensity whatever is passed (sph.h:112-122).  sph_load_scenario
+ * makes those calls on `sim` (which should have the reference domain,
+ * sph_reference_domain); volume and emitter jitter use the C library's
+ * rand(), as the reference does. */
+#define SPH_SCENARIO_MAX_BODIES 32
+#define SPH_SCENARIO_MAX_VOLUMES 32
+#define SPH_SCENARIO_MAX_EMITTERS 8
+enum { SPH_BODY_PLANE = 1, SPH_BODY_CIRCLE = 2, SPH_BODY_LINE_SEGMENT = 3, SPH_BODY_POLYGON = 4 };
+typedef struct sph_scenario_body {
+	int type;           /* SPH_BODY_* */
+	int vertex_count;   /* segment: 2; polygon: 3..8 */
+	sph_vec2 normal;    /* plane: sph_add_plane(normal, distance) */
+	float distance;
+	sph_vec2 center;    /* circle: sph_add_circle(center, radius) */
+	float radius;
+	sph_vec2 verts[8];  /* segment a, b; polygon vertices (world coordinates) */
+} sph_scenario_body;
+typedef struct sph_scenario_volume {
+	sph_vec2 center;
+	sph_vec2 force;
+	int count_x, count_y;  /* (int)floor(size / particle_spacing) */
+	float spacing;
+} sph_scenario_volume;
+typedef struct sph_scenario_emitter {
+	sph_vec2 position, direction;
+	float radius, speed, rate, duration;
+} sph_scenario_emitter;
+typedef struct sph_scenario_desc {
+	char name[100];
+	sph_vec2 gravity;
+	sph_params params;
+	uint32_t body_count;
+	sph_scenario_body bodies[SPH_SCENARIO_MAX_BODIES];
+	uint32_t volume_count;
+	sph_scenario_volume volumes[SPH_SCENARIO_MAX_VOLUMES];
+	uint32_t emitter_count;
+	sph_scenario_emitter emitters[SPH_SCENARIO_MAX_EMITTERS];
+} sph_scenario_desc;
+/* Number of built-in scenarios (8). */
+int sph_scenario_count(int *count);
+/* The calls LoadScenario makes for scenario `index`; `out` is zeroed first. */
+int sph_scenario_describe(int index, sph_scenario_desc *out);
+/* DemoApplication::LoadScenario (app.cpp:477-534) on this simulation. */
+int sph_load_scenario(sph_sim *sim, int index);
 int sph_synchronize(sph_sim *sim);
 /* Number of kernels this library launched for `sim` since creation. */
 int sph_kernel_launches(sph_sim *sim, uint64_t *out);

@@ -19,8 +19,8 @@ LIB_PATH = os.path.join(PKG_DIR, LIB_NAME)
 BUILD_DIR = os.path.join(PKG_DIR, "_build")
 
 SOURCES = [
-    "sph_kernels.cu", "sph_springs.cu", "sph_learned.cu", "sph_api.cu", "sph_noalloc.cu", "mpnn_gemm.cu",
-    "mpnn_kernels.cu", "mpnn.cu",
+    "sph_kernels.cu", "sph_springs.cu", "sph_learned.cu", "sph_render.cu", "sph_api.cu", "sph_noalloc.cu", "mpnn_gemm.cu",
+    "mpnn_kernels.cu", "mpnn.cu", "sph_scenarios.cpp",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off"]
@@ -45,7 +45,7 @@ def nvcc() -> str:
 def _deps() -> List[str]:
     out = []
     for name in os.listdir(CSRC):
-        if name.endswith((".cu", ".cuh", ".h")):
+        if name.endswith((".cu", ".cuh", ".h", ".cpp")):
             out.append(os.path.join(CSRC, name))
     for h in ("sph_gb300.h", "sph_mpnn.h"):
         out.append(os.path.join(os.path.dirname(PKG_DIR), "include", h))
@@ -68,7 +68,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     procs = []
     objs = []
     for src in SOURCES:
-        obj = os.path.join(BUILD_DIR, src.replace(".cu", ".o"))
+        obj = os.path.join(BUILD_DIR, os.path.splitext(src)[0] + ".o")
         objs.append(obj)
         cmd = [cc] + ARCH + _flags(src) + ["-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:

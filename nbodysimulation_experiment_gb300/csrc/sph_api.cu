@@ -135,6 +135,13 @@ struct sph_sim {
 	float *lerr = nullptr;
 	uint32_t *lstats = nullptr;
 
+	// Headless render output (allocated on first use).
+	float4 *colorBuf = nullptr;
+	size_t colorCap = 0;
+	unsigned long long *imgKeys = nullptr;
+	uint32_t *imgRgba = nullptr;
+	size_t imgCap = 0;
+
 	cudaEvent_t ev[kEvCount] = {};
 	bool timed = false;
 	float emitterMs = 0.0f;
@@ -1217,7 +1224,8 @@ int sph_destroy(sph_sim *s) {
 	                s->prof,       T.accN,        T.accP,        T.springPos,   T.springTotal,
 	                s->snap.pos,   s->snap.prev,  s->snap.vel,   s->snap.acc,   s->snap.dens,  s->snap.press,
 	                s->snap.id,    s->snap.cellOf, s->snapCellStart, s->snapCellCount, s->lz0, s->lu,
-	                s->lbyId,      s->ldens,      s->lerr,       s->lstats};
+	                s->lbyId,      s->ldens,      s->lerr,       s->lstats,     s->colorBuf,   s->imgKeys,
+	                s->imgRgba};
 	for (void *p : ptrs)
 		if (p) cudaFree(p);
 	if (s->hostPos) cudaFreeHost(s->hostPos);
@@ -1487,6 +1495,77 @@ int sph_read_particles(sph_sim *s, size_t count, sph_vec2 *pos, sph_vec2 *prev, 
 int sph_batch_read_particles(sph_sim *s, size_t scene, size_t count, sph_vec2 *pos, sph_vec2 *vel, sph_vec2 *dens,
                              sph_vec2 *press) {
 	return read_scene(s, scene, count, pos, nullptr, vel, nullptr, dens, press);
+}
+
+// Demo4::Render (demo4.cpp:520-531) colours every particle with
+// SPHGetParticleColor (sph.h:683-695) from its density, pressure and
+// velocity; here the colours are computed on the device and copied out in
+// AddParticle order.
+int sph_particle_colors(sph_sim *s, size_t count, float *rgba) {
+	if (!s || (count && !rgba)) return SPH_ERR_INVALID_ARGUMENT;
+	SPH_CUDA(cudaSetDevice(s->device));
+	int rc = flush_adds(s);
+	if (rc) return rc;
+	const Scene &sc = s->scenes[0];
+	if (count > sc.n) return SPH_ERR_INVALID_ARGUMENT;
+	if (count == 0) return SPH_OK;
+	if (s->colorCap < sc.n) {
+		SPH_CUDA(cudaStreamSynchronize(s->stream));
+		if (s->colorBuf) cudaFree(s->colorBuf);
+		s->colorBuf = nullptr;
+		s->colorCap = 0;
+		if ((rc = dalloc(&s->colorBuf, sc.n))) return rc;
+		s->colorCap = sc.n;
+	}
+	const BufferSet &A = s->buf[s->cur];
+	const int n = (int)sc.n;
+	k_particle_colors<<<blocks_for(n, kElemThreads), kElemThreads, 0, s->stream>>>(
+	    sc.pBase, n, A.id, A.dens, A.press, A.vel, sc.params.rest_density, s->colorBuf);
+	SPH_LAUNCHED(s);
+	SPH_CUDA(cudaMemcpyAsync(rgba, s->colorBuf, count * sizeof(float4), cudaMemcpyDeviceToHost, s->stream));
+	SPH_CUDA(cudaStreamSynchronize(s->stream));
+	return check_device_errors(s);
+}
+
+// A point image of the scene instead of Render's OpenGL points: width x
+// height RGBA8 pixels spanning the box (row 0 at the top); each particle
+// colours the pixel under it, later particles (AddParticle order) over
+// earlier ones; empty pixels are 0.
+int sph_render_points(sph_sim *s, int width, int height, unsigned char *rgba) {
+	if (!s || !rgba || width <= 0 || height <= 0 || (int64_t)width * height > (1 << 26))
+		return SPH_ERR_INVALID_ARGUMENT;
+	SPH_CUDA(cudaSetDevice(s->device));
+	int rc = flush_adds(s);
+	if (rc) return rc;
+	const Scene &sc = s->scenes[0];
+	const size_t pixels = (size_t)width * height;
+	if (s->imgCap < pixels) {
+		SPH_CUDA(cudaStreamSynchronize(s->stream));
+		if (s->imgKeys) cudaFree(s->imgKeys);
+		if (s->imgRgba) cudaFree(s->imgRgba);
+		s->imgKeys = nullptr;
+		s->imgRgba = nullptr;
+		s->imgCap = 0;
+		if ((rc = dalloc(&s->imgKeys, pixels)) || (rc = dalloc(&s->imgRgba, pixels))) return rc;
+		s->imgCap = pixels;
+	}
+	SPH_CUDA(cudaMemsetAsync(s->imgKeys, 0, pixels * sizeof(unsigned long long), s->stream));
+	const BufferSet &A = s->buf[s->cur];
+	const int n = (int)sc.n;
+	const float halfW = sc.dom.width * 0.5f, halfH = sc.dom.height * 0.5f;
+	const float sx = (float)width / sc.dom.width, sy = (float)height / sc.dom.height;
+	if (n > 0) {
+		k_splat_points<<<blocks_for(n, kElemThreads), kElemThreads, 0, s->stream>>>(
+		    sc.pBase, n, A.id, A.pos, A.dens, A.press, A.vel, sc.params.rest_density, halfW, halfH, sx, sy, width,
+		    height, s->imgKeys);
+		SPH_LAUNCHED(s);
+	}
+	k_keys_to_rgba8<<<blocks_for(pixels, kElemThreads), kElemThreads, 0, s->stream>>>((int)pixels, s->imgKeys,
+	                                                                                    s->imgRgba);
+	SPH_LAUNCHED(s);
+	SPH_CUDA(cudaMemcpyAsync(rgba, s->imgRgba, pixels * 4, cudaMemcpyDeviceToHost, s->stream));
+	SPH_CUDA(cudaStreamSynchronize(s->stream));
+	return check_device_errors(s);
 }
 
 int sph_state_info(sph_sim *s, size_t *count, size_t *canonical, int *gx, int *gy) {

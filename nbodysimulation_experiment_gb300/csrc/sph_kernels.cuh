@@ -67,6 +67,12 @@ __global__ void k_collide(Totals tt, Particles P, Particles Q, SimTables T);
 __global__ void k_add(int first, int count, int scene, int firstId, const float2 *pos, const float2 *force,
                       Particles P, SimTables T);
 __global__ void k_gather_by_id(int first, int count, const int *id, const float2 *src, float2 *dst);
+__global__ void k_particle_colors(int first, int count, const int *id, const float2 *dens, const float2 *press,
+                                  const float2 *vel, float rho0, float4 *out);
+__global__ void k_splat_points(int first, int count, const int *id, const float2 *pos, const float2 *dens,
+                               const float2 *press, const float2 *vel, float rho0, float halfW, float halfH,
+                               float sx, float sy, int width, int height, unsigned long long *keys);
+__global__ void k_keys_to_rgba8(int pixels, const unsigned long long *keys, uint32_t *rgba);
 __global__ void k_springs_select(Totals tt, Particles P, Particles Q, SimTables T);
 __global__ void k_springs_commit(Totals tt, Particles Q, SimTables T);
 __global__ void k_springs_apply(Totals tt, Particles Q, SimTables T);

@@ -87,6 +87,36 @@ class StateView(ctypes.Structure):
     ]
 
 
+class ScenarioBody(ctypes.Structure):
+    """``sph_scenario_body``: one AddPlane/AddCircle/AddLineSegment/AddPolygon."""
+
+    _fields_ = [("type", _c.c_int), ("vertex_count", _c.c_int), ("normal", Vec2), ("distance", _c.c_float),
+                ("center", Vec2), ("radius", _c.c_float), ("verts", Vec2 * 8)]
+
+
+class ScenarioVolume(ctypes.Structure):
+    _fields_ = [("center", Vec2), ("force", Vec2), ("count_x", _c.c_int), ("count_y", _c.c_int),
+                ("spacing", _c.c_float)]
+
+
+class ScenarioEmitter(ctypes.Structure):
+    _fields_ = [("position", Vec2), ("direction", Vec2), ("radius", _c.c_float), ("speed", _c.c_float),
+                ("rate", _c.c_float), ("duration", _c.c_float)]
+
+
+class ScenarioDesc(ctypes.Structure):
+    """``sph_scenario_desc``: the calls DemoApplication::LoadScenario
+    (app.cpp:477-534) makes for one built-in scenario (sph.h:315-437)."""
+
+    _fields_ = [("name", _c.c_char * 100), ("gravity", Vec2), ("params", Params),
+                ("body_count", _c.c_uint32), ("bodies", ScenarioBody * 32),
+                ("volume_count", _c.c_uint32), ("volumes", ScenarioVolume * 32),
+                ("emitter_count", _c.c_uint32), ("emitters", ScenarioEmitter * 8)]
+
+
+SPH_BODY_PLANE, SPH_BODY_CIRCLE, SPH_BODY_LINE_SEGMENT, SPH_BODY_POLYGON = 1, 2, 3, 4
+
+
 class SpringParams(ctypes.Structure):
     """``sph_spring_params``: viscoelastic springs (Clavet et al. 2005)."""
 
@@ -190,6 +220,11 @@ def load_library(build_if_missing: bool = True):
         "sph_load_state": [vp, P(StateView)],
         "sph_get_stream": [vp, P(vp)],
         "sph_device_arrays": [vp, P(vp), P(vp), P(vp), P(vp)],
+        "sph_particle_colors": [vp, _c.c_size_t, vp],
+        "sph_render_points": [vp, _c.c_int, _c.c_int, vp],
+        "sph_scenario_count": [P(_c.c_int)],
+        "sph_scenario_describe": [_c.c_int, P(ScenarioDesc)],
+        "sph_load_scenario": [vp, _c.c_int],
         "sph_synchronize": [vp],
         "sph_kernel_launches": [vp, P(_c.c_uint64)],
         "sph_use_graphs": [vp, _c.c_int],
@@ -243,7 +278,9 @@ C_SYMBOLS = (
     "sph_get_particle_count", "sph_set_gravity", "sph_get_params", "sph_get_stats", "sph_set_params",
     "sph_set_multithreading", "sph_is_multithreading_supported", "sph_is_multithreading",
     "sph_get_worker_thread_count", "sph_read_particles", "sph_state_info", "sph_dump_state", "sph_load_state",
-    "sph_get_stream", "sph_device_arrays", "sph_synchronize", "sph_kernel_launches",
+    "sph_get_stream", "sph_device_arrays", "sph_particle_colors", "sph_render_points", "sph_scenario_count",
+    "sph_scenario_describe", "sph_load_scenario", "sph_synchronize",
+    "sph_kernel_launches",
     "sph_use_graphs", "sph_autotune", "sph_get_sweep_shape", "sph_set_sweep_shape", "sph_set_springs", "sph_get_spring_count", "sph_dump_springs", "sph_load_springs",
     "sph_mpnn_create", "sph_mpnn_destroy", "sph_mpnn_param_count", "sph_mpnn_get_params", "sph_mpnn_set_params",
     "sph_mpnn_capture", "sph_mpnn_sample_count", "sph_mpnn_clear_samples", "sph_mpnn_sample_info",
@@ -256,6 +293,20 @@ C_SYMBOLS = (
 def _check(status: int, what: str) -> None:
     if status != SPH_OK:
         raise SphError(status, what)
+
+
+def scenario_count() -> int:
+    """Number of the reference's built-in scenarios (SPHScenarios[], sph.h:315-437)."""
+    n = _c.c_int()
+    _check(load_library().sph_scenario_count(_c.byref(n)), "sph_scenario_count")
+    return n.value
+
+
+def scenario_describe(index: int) -> ScenarioDesc:
+    """The calls LoadScenario (app.cpp:477-534) makes for scenario ``index``."""
+    d = ScenarioDesc()
+    _check(load_library().sph_scenario_describe(int(index), _c.byref(d)), "sph_scenario_describe")
+    return d
 
 
 def reference_domain() -> Domain:
@@ -453,6 +504,26 @@ class Simulation:
         for k, a in arrs.items():
             setattr(v, k, a.ctypes.data)
         self._call("sph_load_state", _c.byref(v))
+
+    def load_scenario(self, index: int):
+        """DemoApplication::LoadScenario (app.cpp:477-534) for built-in
+        scenario ``index``; use the reference domain."""
+        self._call("sph_load_scenario", int(index))
+
+    def particle_colors(self) -> np.ndarray:
+        """RGBA of every particle in AddParticle order: SPHGetParticleColor
+        (sph.h:683-695), as Demo4's Render colours its points."""
+        n = self.get_particle_count()
+        out = np.zeros((n, 4), np.float32)
+        self._call("sph_particle_colors", n, out.ctypes.data)
+        return out
+
+    def render_points(self, width: int, height: int) -> np.ndarray:
+        """Headless point image of the box: (height, width, 4) uint8, row 0 at
+        the top; each particle colours the pixel under it."""
+        out = np.zeros((height, width, 4), np.uint8)
+        self._call("sph_render_points", int(width), int(height), out.ctypes.data)
+        return out
 
     def stream(self) -> int:
         out = _c.c_void_p()

@@ -38,6 +38,9 @@
 #include "demo4.cpp"
 
 #include <stdint.h>
+#include <math.h>
+
+#include "sph_gb300.h"  // sph_scenario_desc, filled below from the reference's table
 
 using Demo4::ParticleSimulation;
 
@@ -255,6 +258,69 @@ void sphref_get_stats(void *p, uint64_t *counts, float *times) {
 	times[6] = st.time.densityAndPressure;
 	times[7] = st.time.deltaPositions;
 	times[8] = st.time.collisions;
+}
+
+// The calls DemoApplication::LoadScenario (app.cpp:477-534) makes for
+// SPHScenarios[index] (sph.h:315-437), written into the C ABI's description
+// struct: bodies as placed by the loader, then the volume loop -- which walks
+// bodyCount entries of the scenario's volume table -- then the emitters.
+int sphref_scenario_count(void) { return (int)(sizeof(SPHScenarios) / sizeof(SPHScenarios[0])); }
+
+int sphref_scenario_describe(int index, sph_scenario_desc *out) {
+	if (index < 0 || index >= sphref_scenario_count()) return -1;
+	const SPHScenario &sc = SPHScenarios[index];
+	memset(out, 0, sizeof(*out));
+	strncpy(out->name, sc.name, sizeof(out->name) - 1);
+	out->gravity = sph_vec2{sc.gravity.x, sc.gravity.y};
+	const SPHParameters &p = sc.parameters;
+	out->params = sph_params{p.kernelHeight,  p.cellSize,      p.particleSpacing,  p.invKernelHeight,   p.restDensity,
+	                         p.stiffness,     p.nearStiffness, p.linearViscosity,  p.quadraticViscosity};
+	out->body_count = (uint32_t)sc.bodyCount;
+	for (size_t b = 0; b < sc.bodyCount; ++b) {
+		const SPHScenarioBody &body = sc.bodies[b];
+		sph_scenario_body &o = out->bodies[b];
+		switch (body.type) {
+			case SPHScenarioBodyType_Plane:
+				o.type = SPH_BODY_PLANE;
+				o.normal = sph_vec2{body.orientation.col1.x, body.orientation.col1.y};
+				o.distance = Vec2Dot(body.orientation.col1, body.position);
+				break;
+			case SPHScenarioBodyType_Circle:
+				o.type = SPH_BODY_CIRCLE;
+				o.center = sph_vec2{body.position.x, body.position.y};
+				o.radius = body.radius;
+				break;
+			case SPHScenarioBodyType_LineSegment:
+			case SPHScenarioBodyType_Polygon: {
+				o.type = body.type == SPHScenarioBodyType_Polygon ? SPH_BODY_POLYGON : SPH_BODY_LINE_SEGMENT;
+				o.vertex_count = (int)body.vertexCount;
+				for (size_t k = 0; k < body.vertexCount; ++k) {
+					const Vec2f v = Vec2MultMat2(body.orientation, body.localVerts[k]) + body.position;
+					o.verts[k] = sph_vec2{v.x, v.y};
+				}
+			} break;
+			default:
+				break;
+		}
+	}
+	const float spacing = sc.parameters.particleSpacing;
+	out->volume_count = (uint32_t)sc.bodyCount;
+	for (size_t v = 0; v < sc.bodyCount; ++v) {
+		const SPHScenarioVolume &vol = sc.volumes[v];
+		sph_scenario_volume &o = out->volumes[v];
+		o.center = sph_vec2{vol.position.x, vol.position.y};
+		o.force = sph_vec2{vol.force.x, vol.force.y};
+		o.count_x = (int)floor(vol.size.x / spacing);
+		o.count_y = (int)floor(vol.size.y / spacing);
+		o.spacing = spacing;
+	}
+	out->emitter_count = (uint32_t)sc.emitterCount;
+	for (size_t e = 0; e < sc.emitterCount; ++e) {
+		const SPHScenarioEmitter &em = sc.emitters[e];
+		out->emitters[e] = sph_scenario_emitter{{em.position.x, em.position.y}, {em.direction.x, em.direction.y},
+		                                        em.radius, em.speed, em.rate, em.duration};
+	}
+	return 0;
 }
 
 }  // extern "C"
