@@ -65,6 +65,24 @@ def dist_env():
     return rank, world, local
 
 
+def job_seconds(local_s, world, device):
+    """Duration of a timed region for the whole job: the maximum over ranks
+    (independent replicas, so the job ends with its slowest one)."""
+    if world <= 1:
+        return float(local_s)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(local_s)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(particles, steps, world, seconds):
+    """Whole-job particle-steps/s: every rank advances its own replica of
+    ``particles`` by ``steps`` updates within ``seconds``."""
+    return particles * steps * world / seconds
+
+
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -358,7 +376,7 @@ def bench_learned(torch, pkg, scenes, device: int, args):
                       "held_out_loss": ev["learned"], "held_out_loss_without_network": ev["without_network"]}}
 
 
-def main():
+def parse_args(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
@@ -376,8 +394,13 @@ def main():
     ap.add_argument("--learned-steps", type=int, default=1500, help="Adam steps")
     ap.add_argument("--learned-eval-frames", type=int, default=20)
     ap.add_argument("--learned-warmup", type=int, default=3)
-    args = ap.parse_args()
+    args = ap.parse_args(argv)
     args.warmup = max(3, args.warmup)
+    return args
+
+
+def main():
+    args = parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
 
@@ -435,12 +458,8 @@ def main():
         dist.barrier()
     clocks = sampler.stop()
     launches = sim.kernel_launches() - launches0 - 0  # get_stats launches nothing
-    total_s = sum(step_ms) / 1e3
-    if world > 1:
-        t = torch.tensor([total_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
-    value = scene.n * args.steps * world / total_s
+    total_s = job_seconds(sum(step_ms) / 1e3, world, "cuda")
+    value = job_rate(scene.n, args.steps, world, total_s)
 
     # density deviation from the rest density at the end of the run
     rd = sim.read_particles(("dens",))
@@ -462,13 +481,15 @@ def main():
     h2d = sum(pinned[k].nbytes for k in ("pos", "prev", "vel", "acc", "dens", "press", "id", "cell",
                                         "cell_start", "cell_count"))
     torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         sim.load_state(pinned)
         sim.update(dt)
         out = sim.dump_state()
-    e2e_s = time.perf_counter() - t0
-    e2e_value = scene.n * e2e_steps * world / e2e_s
+    e2e_s = job_seconds(time.perf_counter() - t0, world, "cuda")
+    e2e_value = job_rate(scene.n, e2e_steps, world, e2e_s)
 
     hbm, peak_kind = measured_peaks()
     mean_delta_s = statistics.mean(delta_ms) / 1e3
