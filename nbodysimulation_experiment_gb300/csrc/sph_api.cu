@@ -96,7 +96,8 @@ struct sph_sim {
 	cudaStream_t stream = nullptr;
 	int numSMs = 0;
 	int viscBlocks = 0, deltaBlocks = 0, densBlocks = 0, gridBlocks = 0;
-	int viscLean = 0, deltaLean = 0;  // sweep shapes: 0 = wide, 1 = lean (sph_kernels.cuh)
+	int viscLean = 0;   // viscosity shape: 0 = wide, 1 = lean (sph_kernels.cuh)
+	int deltaShape = 0;  // delta shape: kDeltaWide, kDeltaLean or kDeltaMid
 	bool batch = false;
 	int multithreading = 0;
 
@@ -538,7 +539,7 @@ int enqueue_step(sph_sim *s, bool capturing) {
 	{
 		SimTables d = T;
 		d.done = s->doneD;
-		launch_delta(s->deltaLean, s->deltaBlocks, st, tt, B.view(), d);
+		launch_delta(s->deltaShape, s->deltaBlocks, st, tt, B.view(), d);
 		SPH_LAUNCHED(s);
 	}
 	SPH_CUDA(mark(kEvDelta));
@@ -737,7 +738,7 @@ int allocate(sph_sim *s) {
 	                         (int)springs_smem_bytes()) != cudaSuccess)
 		return SPH_ERR_CUDA;
 	int occV = 0, occD = 0;
-	if (sweep_occupancy(false, false, &occV, &occD) != cudaSuccess || occV < 1 || occD < 1) return SPH_ERR_CUDA;
+	if (sweep_occupancy(false, kDeltaWide, &occV, &occD) != cudaSuccess || occV < 1 || occD < 1) return SPH_ERR_CUDA;
 	s->viscBlocks = occV * s->numSMs;
 	s->deltaBlocks = occD * s->numSMs;
 	s->densBlocks = std::max(1, std::min(blocks_for(C, kDensWarps), 64 * s->numSMs));
@@ -1782,9 +1783,10 @@ int sph_load_springs(sph_sim *s, size_t count, const int32_t *spring_count, cons
 }
 
 // Launch-shape autotuner: the ordered sweeps are persistent kernels; each
-// has two shapes (wide: short per-particle latency for one scene; lean: more
-// tasks per SM for many scenes) and a resident block count that trades
-// parallel tasks against polling traffic.  Every shape gives the same results
+// has shapes (wide: short per-particle latency for one scene; the delta
+// sweep's mid: the same pipeline with two blocks per SM; lean: more tasks per
+// SM for many scenes) and a resident block count that trades parallel tasks
+// against polling traffic.  Every shape gives the same results
 // (the task order fixes them), so each candidate is timed on the same update
 // from a snapshot and the fastest kept for each sweep.
 int sph_autotune(sph_sim *s, float dt, int *shape) {
@@ -1803,10 +1805,10 @@ int sph_autotune(sph_sim *s, float dt, int *shape) {
 	if (rc) return rc;
 	// Median of three timed updates per shape (after one warm-up update); the
 	// current shape is kept unless another is faster by more than 2%.
-	auto measure = [&](int vLean, int vBlocks, int dLean, int dBlocks, float *tv, float *td) -> int {
+	auto measure = [&](int vLean, int vBlocks, int dShape, int dBlocks, float *tv, float *td) -> int {
 		s->viscLean = vLean;
 		s->viscBlocks = vBlocks;
-		s->deltaLean = dLean;
+		s->deltaShape = dShape;
 		s->deltaBlocks = dBlocks;
 		float v[3], d[3];
 		for (int rep = 0; rep < 4; ++rep) {
@@ -1824,17 +1826,21 @@ int sph_autotune(sph_sim *s, float dt, int *shape) {
 		*td = d[1];
 		return SPH_OK;
 	};
-	int pick[4] = {s->viscLean, s->viscBlocks, s->deltaLean, s->deltaBlocks};
+	int pick[4] = {s->viscLean, s->viscBlocks, s->deltaShape, s->deltaBlocks};
 	float bestV = 0.f, bestD = 0.f;
 	rc = measure(pick[0], pick[1], pick[2], pick[3], &bestV, &bestD);
-	for (int lean = 0; lean < 2 && !rc; ++lean) {
+	// Candidates: every delta shape, each timed with the viscosity shape of
+	// the same kind (lean with lean, wide with both pipelined delta shapes),
+	// at every resident block count per SM.
+	for (int dShape = 0; dShape < kDeltaShapes && !rc; ++dShape) {
+		const int lean = dShape == kDeltaLean ? 1 : 0;
 		int occV = 0, occD = 0;
-		rc = cuda_status(sweep_occupancy(lean != 0, lean != 0, &occV, &occD));
+		rc = cuda_status(sweep_occupancy(lean != 0, dShape, &occV, &occD));
 		const int maxPer = std::max(occV, occD);
 		for (int per = 1; per <= maxPer && !rc; ++per) {
 			const int vb = std::min(per, occV) * s->numSMs, db = std::min(per, occD) * s->numSMs;
 			float tv = 0.f, td = 0.f;
-			rc = measure(lean, vb, lean, db, &tv, &td);
+			rc = measure(lean, vb, dShape, db, &tv, &td);
 			if (rc) break;
 			if (tv < 0.98f * bestV) {
 				bestV = tv;
@@ -1843,7 +1849,7 @@ int sph_autotune(sph_sim *s, float dt, int *shape) {
 			}
 			if (td < 0.98f * bestD) {
 				bestD = td;
-				pick[2] = lean;
+				pick[2] = dShape;
 				pick[3] = db;
 			}
 		}
@@ -1851,7 +1857,7 @@ int sph_autotune(sph_sim *s, float dt, int *shape) {
 	if (!rc) rc = copy_state(s, false);
 	s->viscLean = pick[0];
 	s->viscBlocks = pick[1];
-	s->deltaLean = pick[2];
+	s->deltaShape = pick[2];
 	s->deltaBlocks = pick[3];
 	s->useGraphs = graphs;
 	drop_graphs(s);
@@ -1861,7 +1867,7 @@ int sph_autotune(sph_sim *s, float dt, int *shape) {
 	if (shape) {
 		shape[0] = s->viscLean ? ViscLean::kWarps : ViscWide::kWarps;
 		shape[1] = s->viscBlocks;
-		shape[2] = s->deltaLean ? DeltaLean::kWarps : DeltaWide::kWarps;
+		shape[2] = delta_shape_warps(s->deltaShape);
 		shape[3] = s->deltaBlocks;
 	}
 	return SPH_OK;
@@ -1871,7 +1877,7 @@ int sph_get_sweep_shape(sph_sim *s, int *shape) {
 	if (!s || !shape) return SPH_ERR_INVALID_ARGUMENT;
 	shape[0] = s->viscLean ? ViscLean::kWarps : ViscWide::kWarps;
 	shape[1] = s->viscBlocks;
-	shape[2] = s->deltaLean ? DeltaLean::kWarps : DeltaWide::kWarps;
+	shape[2] = delta_shape_warps(s->deltaShape);
 	shape[3] = s->deltaBlocks;
 	return SPH_OK;
 }
@@ -1879,13 +1885,16 @@ int sph_get_sweep_shape(sph_sim *s, int *shape) {
 int sph_set_sweep_shape(sph_sim *s, const int *shape) {
 	if (!s || !shape) return SPH_ERR_INVALID_ARGUMENT;
 	const bool vOk = shape[0] == ViscLean::kWarps || shape[0] == ViscWide::kWarps;
-	const bool dOk = shape[2] == DeltaLean::kWarps || shape[2] == DeltaWide::kWarps;
+	int dShape = -1;
+	for (int k = 0; k < kDeltaShapes; ++k)
+		if (shape[2] == delta_shape_warps(k)) dShape = k;
+	const bool dOk = dShape >= 0;
 	if (!vOk || !dOk || shape[1] < 1 || shape[3] < 1 || shape[1] > (1 << 20) || shape[3] > (1 << 20))
 		return SPH_ERR_INVALID_ARGUMENT;
 	SPH_CUDA(cudaStreamSynchronize(s->stream));
 	s->viscLean = shape[0] == ViscLean::kWarps;
 	s->viscBlocks = shape[1];
-	s->deltaLean = shape[2] == DeltaLean::kWarps;
+	s->deltaShape = dShape;
 	s->deltaBlocks = shape[3];
 	drop_graphs(s);
 	return SPH_OK;

@@ -1318,10 +1318,10 @@ __global__ void __launch_bounds__(kDensWarps * kWarp, 4) k_density(Totals tt, Pa
 // before reading it.
 // Particles whose lists exceed one pass, and regions staged particle by
 // particle, drain the pipeline and run on the whole block in turn.
-// Two shapes (DeltaWide, DeltaLean in sph_kernels.cuh): wide is pipelined
-// with seven producer warps (short per-particle latency, one scene); lean is
-// two warps without the pipeline and with smaller staging (more tasks per
-// SM, many scenes).
+// Three shapes (sph_kernels.cuh): wide is pipelined with eleven producer
+// warps, one block per SM (short per-particle latency, one scene); mid is
+// pipelined with seven, two blocks per SM; lean is two warps without the
+// pipeline and with smaller staging (more tasks per SM, many scenes).
 template <class C>
 struct DeltaSmemT {
 	static constexpr int kProd = C::kWarps - 1;         // producer warps
@@ -1416,13 +1416,34 @@ __device__ __forceinline__ bool stage_region(DeltaSmemT<C> &S, Region &R, const 
 	return true;
 }
 
+// Write the staged positions of the owned cells back.  Flat: one element
+// per thread, its cell found by binary search over the region's offsets as
+// in staging, so no thread walks the cells one after another.  Otherwise
+// cell by cell, with fewer instructions per element.
 template <class C>
 __device__ __forceinline__ void write_back_owned(DeltaSmemT<C> &S, const Region &R, const Particles &Q, int tid) {
 	constexpr int kDT = C::kWarps * kWarp;
-	for (int q = 0; q < R.ncells; ++q) {
-		if (!S.owned[q]) continue;
-		const int off = S.segOff[q], nn = S.segOff[q + 1] - off, st = S.segStart[q];
-		for (int j = tid; j < nn; j += kDT) __stcg(&Q.pos[st + j], S.pos[off + j]);
+	if (!C::kShortEntry) {
+		for (int q = 0; q < R.ncells; ++q) {
+			if (!S.owned[q]) continue;
+			const int off = S.segOff[q], nn = S.segOff[q + 1] - off, st = S.segStart[q];
+			for (int j = tid; j < nn; j += kDT) __stcg(&Q.pos[st + j], S.pos[off + j]);
+		}
+		return;
+	}
+	for (int b0 = 0; b0 < R.L; b0 += 4 * kDT) {
+#pragma unroll
+		for (int u = 0; u < 4; ++u) {
+			const int e = b0 + u * kDT + tid;
+			if (e < R.L) {
+				int lo = 0, hi = R.ncells;
+				while (hi - lo > 1) {
+					const int mid = (lo + hi) >> 1;
+					if (S.segOff[mid] <= e) lo = mid; else hi = mid;
+				}
+				if (S.owned[lo]) __stcg(&Q.pos[S.segStart[lo] + (e - S.segOff[lo])], S.pos[e]);
+			}
+		}
 	}
 }
 
@@ -1658,12 +1679,14 @@ template <class C>
 __device__ __forceinline__ void summer(DeltaSmemT<C> &S, int b, int4 sl, int4 ln, float2 pk, const StepParams &s,
                                        float2 &hres) {
 	const int prev = S.meta[b ^ 1].z;
+	// Particle k's own slot is written by no warp in this phase (its self
+	// pair is kept aside), so its position is read before the sum.
+	const float2 xk = S.pos[sl.w];
 	const float2 xp = finish_particle<C>(S, b ^ 1, hres);
 	hres = make_float2(0.0f, 0.0f);
 	const bool inList = (prev >= sl.x && prev < sl.x + ln.x) || (prev >= sl.y && prev < sl.y + ln.y) ||
 	                    (prev >= sl.z && prev < sl.z + ln.z);
 	if (!inList) return;
-	const float2 xk = S.pos[sl.w];
 	const float rx = xp.x - xk.x, ry = xp.y - xk.y;
 	const float r2 = rx * rx + ry * ry;
 	if (r2 < s.h2) {
@@ -1689,6 +1712,16 @@ __device__ __forceinline__ void relax_group(DeltaSmemT<C> &S, int p0, int p1, in
 	R.y0 = max(by0 - 1, 0);
 	R.x1 = min(bx1 + 1, s.gx - 1);
 	R.y1 = min(by1 + 1, s.gy - 1);
+	// Per-particle inputs of the first chunk (one particle per thread) do not
+	// depend on the staged positions: their loads can overlap the staging.
+	static_assert(kDT >= C::kPrefetch, "a chunk holds at most one particle per thread");
+	int jk0 = 0, nc0 = 0;
+	float2 pk0 = make_float2(0.0f, 0.0f);
+	if (C::kShortEntry && p0 + tid < min(p1, p0 + C::kPrefetch)) {
+		jk0 = T.newLabel[p0 + tid];
+		nc0 = T.newCell[p0 + tid];
+		pk0 = Q.press[jk0];
+	}
 	const bool staged = stage_region<C>(S, R, Q, T, s, cellBase, tid);
 	bool pending = false;  // the previous particle still needs its sum (buffer ph ^ 1)
 	int ph = 0;
@@ -1696,9 +1729,10 @@ __device__ __forceinline__ void relax_group(DeltaSmemT<C> &S, int p0, int p1, in
 	for (int c0 = p0; c0 < p1; c0 += C::kPrefetch) {
 		const int c1 = min(p1, c0 + C::kPrefetch);
 		for (int k = c0 + tid; k < c1; k += kDT) {
-			const int jk = T.newLabel[k];
-			const int nc = T.newCell[k];
-			S.ppk[k - c0] = Q.press[jk];
+			const bool first = C::kShortEntry && c0 == p0;
+			const int jk = first ? jk0 : T.newLabel[k];
+			const int nc = first ? nc0 : T.newCell[k];
+			S.ppk[k - c0] = first ? pk0 : Q.press[jk];
 			if (staged) {
 				particle_slots<C>(S, R, nc, jk, s, cellBase, T.error, S.pslot[k - c0], S.plen[k - c0]);
 			} else {
@@ -2100,10 +2134,13 @@ cudaError_t sweep_attributes() {
 	if (e == cudaSuccess)
 		e = cudaFuncSetAttribute(k_delta<DeltaLean>, cudaFuncAttributeMaxDynamicSharedMemorySize,
 		                         (int)delta_smem_bytes<DeltaLean>());
+	if (e == cudaSuccess)
+		e = cudaFuncSetAttribute(k_delta<DeltaMid>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                         (int)delta_smem_bytes<DeltaMid>());
 	return e;
 }
 
-cudaError_t sweep_occupancy(bool viscLean, bool deltaLean, int *occV, int *occD) {
+cudaError_t sweep_occupancy(bool viscLean, int deltaShape, int *occV, int *occD) {
 	cudaError_t e = viscLean ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(occV, k_viscosity_multi<ViscLean>,
 	                                                                         ViscLean::kWarps * kWarp,
 	                                                                         sizeof(ViscMultiSmemT<ViscLean>))
@@ -2111,10 +2148,14 @@ cudaError_t sweep_occupancy(bool viscLean, bool deltaLean, int *occV, int *occD)
 	                                                                         ViscWide::kWarps * kWarp,
 	                                                                         visc_smem_bytes<ViscWide>());
 	if (e != cudaSuccess) return e;
-	return deltaLean ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(occD, k_delta<DeltaLean>, DeltaLean::kWarps * kWarp,
-	                                                                 delta_smem_bytes<DeltaLean>())
-	                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(occD, k_delta<DeltaWide>, DeltaWide::kWarps * kWarp,
-	                                                                 delta_smem_bytes<DeltaWide>());
+	if (deltaShape == kDeltaLean)
+		return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occD, k_delta<DeltaLean>, DeltaLean::kWarps * kWarp,
+		                                                     delta_smem_bytes<DeltaLean>());
+	if (deltaShape == kDeltaMid)
+		return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occD, k_delta<DeltaMid>, DeltaMid::kWarps * kWarp,
+		                                                     delta_smem_bytes<DeltaMid>());
+	return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occD, k_delta<DeltaWide>, DeltaWide::kWarps * kWarp,
+	                                                     delta_smem_bytes<DeltaWide>());
 }
 
 void launch_viscosity(bool lean, int blocks, cudaStream_t st, Totals tt, Particles P, SimTables T) {
@@ -2125,9 +2166,11 @@ void launch_viscosity(bool lean, int blocks, cudaStream_t st, Totals tt, Particl
 		k_viscosity<ViscWide><<<blocks, ViscWide::kWarps * kWarp, visc_smem_bytes<ViscWide>(), st>>>(tt, P, T);
 }
 
-void launch_delta(bool lean, int blocks, cudaStream_t st, Totals tt, Particles Q, SimTables T) {
-	if (lean)
+void launch_delta(int shape, int blocks, cudaStream_t st, Totals tt, Particles Q, SimTables T) {
+	if (shape == kDeltaLean)
 		k_delta<DeltaLean><<<blocks, DeltaLean::kWarps * kWarp, delta_smem_bytes<DeltaLean>(), st>>>(tt, Q, T);
+	else if (shape == kDeltaMid)
+		k_delta<DeltaMid><<<blocks, DeltaMid::kWarps * kWarp, delta_smem_bytes<DeltaMid>(), st>>>(tt, Q, T);
 	else
 		k_delta<DeltaWide><<<blocks, DeltaWide::kWarps * kWarp, delta_smem_bytes<DeltaWide>(), st>>>(tt, Q, T);
 }

@@ -22,17 +22,32 @@ struct ViscLean {
 // summer warp per task; the others relax one particle at a time on the
 // whole block.  kChainW in-range pairs are buffered per warp; a particle's
 // list is relaxed in the pipeline when it has at most (kWarps - 1) * kChainW
-// entries.  Wide: pipelined, eight warps (short per-particle latency for one
-// scene).  Lean: two warps, not pipelined, smaller staging (more tasks per SM
-// for many scenes).
+// entries.  Wide: pipelined, twelve warps, one block per SM (short
+// per-particle latency for one scene).  Lean: two warps, not pipelined,
+// smaller staging (more tasks per SM for many scenes).  kShortEntry: a
+// task's entry and exit take the fewest cycles (first chunk's inputs loaded
+// during the staging, region written back one element per thread) rather
+// than the fewest instructions.
 struct DeltaWide {
-	static constexpr int kWarps = 8, kStage = kDeltaStageCap, kChainW = 128, kPrefetch = 128, kMinBlocks = 2;
-	static constexpr bool kPipelined = true;
+	static constexpr int kWarps = 12, kStage = kDeltaStageCap, kChainW = 96, kPrefetch = 128, kMinBlocks = 1;
+	static constexpr bool kPipelined = true, kShortEntry = true;
 };
 struct DeltaLean {
 	static constexpr int kWarps = 2, kStage = 1536, kChainW = 192, kPrefetch = 64, kMinBlocks = 8;
-	static constexpr bool kPipelined = false;
+	static constexpr bool kPipelined = false, kShortEntry = false;
 };
+// Mid: pipelined, eight warps, two blocks per SM (mid-size scenes, where
+// more tasks run at once than one block per SM holds).
+struct DeltaMid {
+	static constexpr int kWarps = 8, kStage = kDeltaStageCap, kChainW = 128, kPrefetch = 128, kMinBlocks = 2;
+	static constexpr bool kPipelined = true, kShortEntry = true;
+};
+// Delta shapes by index (sph_set_sweep_shape names them by warp count).
+constexpr int kDeltaShapes = 3;
+constexpr int kDeltaWide = 0, kDeltaLean = 1, kDeltaMid = 2;
+constexpr int delta_shape_warps(int shape) {
+	return shape == kDeltaLean ? DeltaLean::kWarps : (shape == kDeltaMid ? DeltaMid::kWarps : DeltaWide::kWarps);
+}
 constexpr int kDensWarps = 8;
 constexpr int kGridWarps = 4;
 constexpr int kScanThreads = 1024;
@@ -45,9 +60,9 @@ struct DensWarp;
 
 // The two ordered sweeps in a chosen shape (lean or wide), and their set-up.
 cudaError_t sweep_attributes();
-cudaError_t sweep_occupancy(bool viscLean, bool deltaLean, int *occV, int *occD);
+cudaError_t sweep_occupancy(bool viscLean, int deltaShape, int *occV, int *occD);
 void launch_viscosity(bool lean, int blocks, cudaStream_t st, Totals tt, Particles P, SimTables T);
-void launch_delta(bool lean, int blocks, cudaStream_t st, Totals tt, Particles Q, SimTables T);
+void launch_delta(int shape, int blocks, cudaStream_t st, Totals tt, Particles Q, SimTables T);
 size_t dens_smem_bytes();
 size_t springs_smem_bytes();
 

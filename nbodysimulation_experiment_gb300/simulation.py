@@ -125,10 +125,11 @@ class SpringParams(ctypes.Structure):
 
 
 SPRING_SLOTS = 16
-#: Warps per task of the ordered sweeps' two launch shapes, (wide, lean):
-#: the values ``sph_set_sweep_shape`` accepts (csrc/sph_kernels.cuh).
+#: Warps per task of the ordered sweeps' launch shapes, (wide, lean) and for
+#: the delta sweep (wide, lean, mid): the values ``sph_set_sweep_shape``
+#: accepts (csrc/sph_kernels.cuh).
 VISC_WARPS = (4, 5)
-DELTA_WARPS = (8, 2)
+DELTA_WARPS = (12, 2, 8)
 
 
 class BodyDesc(ctypes.Structure):
