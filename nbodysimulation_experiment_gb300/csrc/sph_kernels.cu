@@ -1679,14 +1679,12 @@ template <class C>
 __device__ __forceinline__ void summer(DeltaSmemT<C> &S, int b, int4 sl, int4 ln, float2 pk, const StepParams &s,
                                        float2 &hres) {
 	const int prev = S.meta[b ^ 1].z;
-	// Particle k's own slot is written by no warp in this phase (its self
-	// pair is kept aside), so its position is read before the sum.
-	const float2 xk = S.pos[sl.w];
 	const float2 xp = finish_particle<C>(S, b ^ 1, hres);
 	hres = make_float2(0.0f, 0.0f);
 	const bool inList = (prev >= sl.x && prev < sl.x + ln.x) || (prev >= sl.y && prev < sl.y + ln.y) ||
 	                    (prev >= sl.z && prev < sl.z + ln.z);
 	if (!inList) return;
+	const float2 xk = S.pos[sl.w];
 	const float rx = xp.x - xk.x, ry = xp.y - xk.y;
 	const float r2 = rx * rx + ry * ry;
 	if (r2 < s.h2) {

@@ -2,6 +2,7 @@
 profiler such as Nsight Compute (each runs a few launches of its kernels on
 inputs larger than L2 but a few hundred MB on the device at most).
 
+    python -m nbodysimulation_experiment_gb300.profile_cases plain
     python -m nbodysimulation_experiment_gb300.profile_cases springs
     python -m nbodysimulation_experiment_gb300.profile_cases mpnn
     python -m nbodysimulation_experiment_gb300.profile_cases batched
@@ -15,6 +16,21 @@ import numpy as np
 
 from . import learned, scenes
 from .simulation import DELTA_WARPS, VISC_WARPS, BatchSimulation, Mpnn, Simulation
+
+
+def plain(updates: int = 3, warm: int = 20) -> None:
+    """The 65,536-particle obstacle scene (the benchmark's workload) with the
+    default (wide) sweep shapes: the scene's first update, `warm` updates,
+    then `updates` more, so each sweep kernel's launches after the first
+    1 + warm are steady-state ones."""
+    scene = scenes.obstacles_65536()
+    sim = Simulation(scene.domain())
+    scene.apply(sim)
+    for _ in range(1 + warm + updates):
+        sim.update(float(scenes.DT))
+    sim.synchronize()
+    print("shape", sim.sweep_shape())
+    sim.close()
 
 
 def springs(updates: int = 3) -> None:
@@ -71,7 +87,7 @@ def learned_frame(frames: int = 3) -> None:
     sim.close()
 
 
-CASES = {"springs": springs, "mpnn": mpnn, "batched": batched, "learned_frame": learned_frame}
+CASES = {"plain": plain, "springs": springs, "mpnn": mpnn, "batched": batched, "learned_frame": learned_frame}
 
 if __name__ == "__main__":
     CASES[sys.argv[1]]()
