@@ -154,10 +154,20 @@ __global__ void k_integrate(Totals tt, Particles P, SimTables T) {
 // block's velocities are written back.  Two tasks conflict iff they belong to
 // one scene and their cells are at most two apart; every task waits for the
 // earlier conflicting ones.
-// One task per block: warp 0 runs the ordered velocity chain of particle k
-// while warps 1..3 compute the compacted pair geometry of particle k+1
-// (positions do not change during this pass, so the geometry of every
-// particle of the task is known in advance).
+// One task per block: lanes 0 and 1 of warp 0 run the ordered velocity
+// chains while warps 1..3 compute the compacted pair geometry of the next
+// particle (positions do not change during this pass, so the geometry of
+// every particle of the task is known in advance).
+// The task's particles k = 0, 1, ... sit at consecutive list slots own + k
+// of one shared list.  Particle k's pairs before slot own + k - 1 (its head)
+// need only what particles < k did at those slots, and particle k - 1 has
+// passed them once it is past slot own + k + 1.  So the head of k runs in
+// lockstep with the tail of k - 1 (its pairs after slot own + k), on the
+// other lane: the two touch disjoint slots.  The middle of k (its pairs with
+// k - 1, itself and k + 1) follows once k - 1 is finished, and k's tail runs
+// beside the head of k + 1.  Each particle costs about the longer of its head
+// and tail instead of its whole list, with every pair in the reference's
+// order for each particle it touches.
 // This is the wide shape (ViscWide); the lean one, k_viscosity_multi below,
 // runs several tasks per block for throughput.  Both run the geometry inline
 // in the chain for particles with more in-range pairs than their geometry
@@ -165,10 +175,12 @@ __global__ void k_integrate(Totals tt, Particles P, SimTables T) {
 template <class C>
 struct ViscSmemT {
 	float2 pos[kStageCap];
-	float2 vel[kStageCap];
-	float4 geo[2][C::kGeom];  // in-range pairs of a particle, list order: slot, unit vector, 1 - q
-	int m[2];
+	float2 vel[kStageCap + 2];  // + a scratch slot (kStageCap) for the chains' idle steps
+	float4 geo[3][C::kGeom];  // in-range pairs of a particle, list order: slot, unit vector, 1 - q
+	int m[3];
+	int2 split[3];            // first pair of the middle, first pair of the tail
 	int warpCnt[2][C::kWarps];
+	int headCnt[C::kWarps], midCnt[C::kWarps];
 	int task;
 };
 
@@ -192,14 +204,15 @@ __device__ __forceinline__ void producers_sync() {
 
 // Geometry of the particle at staged slot `slot` over the L staged entries
 // (its whole list): in-range pairs in list order with their unit vectors
-// and 1 - q (sph.h:497-505).  Run by the producer warps only, in two passes:
-// the in-range entries are compacted first (slot, r, r^2), then the square
-// roots and divisions run over the dense compacted list.
+// and 1 - q (sph.h:497-505), and where its middle (slots slot-1..slot+1)
+// and tail begin.  Run by the producer warps only, in two passes: the
+// in-range entries are compacted first (slot, r, r^2), then the square roots
+// and divisions run over the dense compacted list.
 template <class C>
 __device__ __forceinline__ void visc_geometry(ViscSmemT<C> &S, int buf, int slot, int L, const StepParams &s, int p) {
 	const int lane = p & (kWarp - 1), w = p / kWarp;
 	const float2 xi = S.pos[slot];
-	int m = 0, parity = 0;
+	int m = 0, parity = 0, nHead = 0, nToTail = 0;
 	for (int base = 0; base < L; base += C::kProducers) {
 		const int e = base + p;
 		bool in = false;
@@ -211,6 +224,8 @@ __device__ __forceinline__ void visc_geometry(ViscSmemT<C> &S, int buf, int slot
 			r2 = rx * rx + ry * ry;
 			in = r2 < s.h2;
 		}
+		nHead += (in && e < slot - 1) ? 1 : 0;
+		nToTail += (in && e <= slot + 1) ? 1 : 0;
 		const unsigned mask = __ballot_sync(kFull, in);
 		int before = m, total = __popc(mask);
 		if (C::kProducers > kWarp) {
@@ -229,7 +244,22 @@ __device__ __forceinline__ void visc_geometry(ViscSmemT<C> &S, int buf, int slot
 		if (in && at < C::kGeom) S.geo[buf][at] = make_float4(__int_as_float(e), rx, ry, r2);
 		m += total;
 	}
+	nHead = __reduce_add_sync(kFull, nHead);
+	nToTail = __reduce_add_sync(kFull, nToTail);
+	if (lane == 0) {
+		S.headCnt[w] = nHead;
+		S.midCnt[w] = nToTail;
+	}
 	if (C::kProducers > kWarp) producers_sync<C>(); else __syncwarp();
+	if (p == 0) {
+		int h = 0, t = 0;
+#pragma unroll
+		for (int q = 0; q < C::kProducers / kWarp; ++q) {
+			h += S.headCnt[q];
+			t += S.midCnt[q];
+		}
+		S.split[buf] = make_int2(h, t);
+	}
 	const int mm = min(m, C::kGeom);
 	for (int q = p; q < mm; q += C::kProducers) {
 		const float4 g = S.geo[buf][q];
@@ -331,15 +361,78 @@ __device__ __forceinline__ void visc_run(float2 *vel, const float4 *G, int m, fl
 			                    beta, hdt);
 }
 
+// The chain over pairs [start, start + len) of G, in lockstep with the
+// other chain lane: both run n >= len steps (the longer of the two).  This
+// lane's steps past len take an idle pair: the scratch slot kStageCap with a
+// zero unit vector, so u = 0 is not approaching and neither velocity
+// changes; the steps stay branch-free.  The same four-pair software pipeline
+// as visc_run; the two lanes touch disjoint slots, so a prefetched velocity
+// is never one the other lane changes.
+template <bool kBranchy>
+__device__ __forceinline__ void visc_run_range(float2 *vel, const float4 *G, int start, int len, int n, float2 &vi,
+                                               float sigma, float beta, float hdt) {
+	const float4 idle = make_float4(__int_as_float(kStageCap), 0.f, 0.f, 0.f);
+	float4 g[4];
+	float2 vj[4];
+#pragma unroll
+	for (int u = 0; u < 4; ++u) g[u] = u < len ? G[start + u] : idle;
+#pragma unroll
+	for (int u = 0; u < 4; ++u) vj[u] = vel[__float_as_int(g[u].x)];
+	for (int q = 0; q < n; q += 4) {
+		float4 gn[4];
+		float2 vn[4];
+#pragma unroll
+		for (int u = 0; u < 4; ++u) gn[u] = q + 4 + u < len ? G[start + q + 4 + u] : idle;
+#pragma unroll
+		for (int u = 0; u < 4; ++u) vn[u] = vel[__float_as_int(gn[u].x)];
+#pragma unroll
+		for (int u = 0; u < 4; ++u)
+			visc_pair<kBranchy>(vel, __float_as_int(g[u].x), make_float2(g[u].y, g[u].z), g[u].w, vj[u], vi, sigma,
+			                    beta, hdt);
+#pragma unroll
+		for (int u = 0; u < 4; ++u) {
+			g[u] = gn[u];
+			vj[u] = vn[u];
+		}
+	}
+}
+
+// Phase k of a task's chains (lanes 0 and 1 of warp 0; cnt particles at
+// slots own..own+cnt-1, particle j's geometry in buffer j % 3).  Lane k & 1
+// starts particle k: its head beside the tail of particle k - 1 on the other
+// lane, then (once k - 1 is finished and stored) its middle.  vi is the
+// lane's particle velocity, carried from the head to the tail.  A particle
+// with more in-range pairs than the geometry buffer holds runs its whole
+// chain in the middle, in list order, computing the geometry there.
 template <class C>
-__device__ __forceinline__ void visc_chain(ViscSmemT<C> &S, int buf, int slot, int L, const StepParams &s) {
+__device__ __forceinline__ void visc_wave(ViscSmemT<C> &S, int k, int cnt, int own, int L, const StepParams &s,
+                                          float2 &vi) {
+	const int lane = threadIdx.x & (kWarp - 1);
 	const float hdt = 0.5f * s.dt;
-	const int m = S.m[buf];
-	float2 vi = S.vel[slot];
+	const bool head = (k & 1) == lane;  // head and middle of particle k; else the tail of particle k - 1
+	const bool has = head ? k < cnt : k >= 1;
+	const int buf = has ? (head ? k : k - 1) % 3 : 0;
+	int start = 0, len = 0, m = 0;
+	int2 sp = make_int2(0, 0);
+	if (has) {
+		m = S.m[buf];
+		sp = S.split[buf];
+		const bool inl = m > C::kGeom;
+		if (head) {
+			vi = S.vel[own + k];
+			len = inl ? 0 : sp.x;
+		} else {
+			start = sp.y;
+			len = inl ? 0 : m - sp.y;
+		}
+	}
+	const int n = max(len, __shfl_xor_sync(0x3u, len, 1));
+	visc_run_range<C::kBranchy>(S.vel, S.geo[buf], start, len, n, vi, s.sigma, s.beta, hdt);
+	if (has && !head) S.vel[own + k - 1] = vi;  // particle k - 1 is finished
+	__syncwarp(0x3u);
+	if (!(has && head)) return;
 	if (m > C::kGeom) {
-		// More in-range pairs than the geometry buffer holds: the same pair
-		// geometry (sph.h:497-505), computed here in list order.
-		const float2 xi = S.pos[slot];
+		const float2 xi = S.pos[own + k];
 		for (int e = 0; e < L; ++e) {
 			const float2 xj = S.pos[e];
 			const float rx = xj.x - xi.x, ry = xj.y - xi.y;
@@ -347,17 +440,20 @@ __device__ __forceinline__ void visc_chain(ViscSmemT<C> &S, int buf, int slot, i
 			if (!(r2 < s.h2)) continue;
 			const float r = sqrtf(r2);
 			const float qq = r * s.invH;
-			float len = r;
-			if (len == 0.0f) len = 1.0f;
-			const float inv = 1.0f / len;
+			float lenr = r;
+			if (lenr == 0.0f) lenr = 1.0f;
+			const float inv = 1.0f / lenr;
 			visc_pair<C::kBranchy>(S.vel, e, make_float2(rx * inv, ry * inv), 1.0f - qq, S.vel[e], vi, s.sigma,
 			                       s.beta, hdt);
 		}
-		S.vel[slot] = vi;
 		return;
 	}
-	visc_run<C::kBranchy>(S.vel, S.geo[buf], m, vi, s.sigma, s.beta, hdt);
-	S.vel[slot] = vi;
+	const float4 *G = S.geo[buf];
+	for (int q = sp.x; q < sp.y; ++q) {
+		const float4 g = G[q];
+		const int j = __float_as_int(g.x);
+		visc_pair<C::kBranchy>(S.vel, j, make_float2(g.y, g.z), g.w, S.vel[j], vi, s.sigma, s.beta, hdt);
+	}
 }
 
 }  // namespace
@@ -442,11 +538,12 @@ __global__ void __launch_bounds__(C::kWarps * kWarp, C::kMinBlocks) k_viscosity(
 				stamp(T, 0, t, 2, tid);
 				if (warp > 0) visc_geometry<C>(S, 0, own, L, s, tid - kWarp);
 				__syncthreads();
-				for (int k = 0; k < cnt; ++k) {
+				float2 vi = make_float2(0.0f, 0.0f);
+				for (int k = 0; k <= cnt; ++k) {
 					if (warp == 0) {
-						if (tid == 0) visc_chain<C>(S, k & 1, own + k, L, s);
+						if (tid < 2) visc_wave<C>(S, k, cnt, own, L, s, vi);
 					} else if (k + 1 < cnt) {
-						visc_geometry<C>(S, (k + 1) & 1, own + k + 1, L, s, tid - kWarp);
+						visc_geometry<C>(S, (k + 1) % 3, own + k + 1, L, s, tid - kWarp);
 					}
 					__syncthreads();
 				}
@@ -1423,25 +1520,25 @@ __device__ __forceinline__ bool stage_region(DeltaSmemT<C> &S, Region &R, const 
 template <class C>
 __device__ __forceinline__ void write_back_owned(DeltaSmemT<C> &S, const Region &R, const Particles &Q, int tid) {
 	constexpr int kDT = C::kWarps * kWarp;
-	if (!C::kShortEntry) {
+	if constexpr (!C::kShortEntry) {
 		for (int q = 0; q < R.ncells; ++q) {
 			if (!S.owned[q]) continue;
 			const int off = S.segOff[q], nn = S.segOff[q + 1] - off, st = S.segStart[q];
 			for (int j = tid; j < nn; j += kDT) __stcg(&Q.pos[st + j], S.pos[off + j]);
 		}
-		return;
-	}
-	for (int b0 = 0; b0 < R.L; b0 += 4 * kDT) {
+	} else {
+		for (int b0 = 0; b0 < R.L; b0 += 4 * kDT) {
 #pragma unroll
-		for (int u = 0; u < 4; ++u) {
-			const int e = b0 + u * kDT + tid;
-			if (e < R.L) {
-				int lo = 0, hi = R.ncells;
-				while (hi - lo > 1) {
-					const int mid = (lo + hi) >> 1;
-					if (S.segOff[mid] <= e) lo = mid; else hi = mid;
+			for (int u = 0; u < 4; ++u) {
+				const int e = b0 + u * kDT + tid;
+				if (e < R.L) {
+					int lo = 0, hi = R.ncells;
+					while (hi - lo > 1) {
+						const int mid = (lo + hi) >> 1;
+						if (S.segOff[mid] <= e) lo = mid; else hi = mid;
+					}
+					if (S.owned[lo]) __stcg(&Q.pos[S.segStart[lo] + (e - S.segOff[lo])], S.pos[e]);
 				}
-				if (S.owned[lo]) __stcg(&Q.pos[S.segStart[lo] + (e - S.segOff[lo])], S.pos[e]);
 			}
 		}
 	}

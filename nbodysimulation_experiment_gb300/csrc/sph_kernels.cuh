@@ -10,7 +10,7 @@ namespace sphgb {
 // critical path for one scene).  Lean: fewer warps and smaller buffers (more
 // tasks per SM for many scenes).  Results do not depend on the shape.
 struct ViscWide {
-	static constexpr int kWarps = 4, kProducers = 3 * kWarp, kGeom = kStageCap, kMinBlocks = 4;
+	static constexpr int kWarps = 4, kProducers = 3 * kWarp, kGeom = 512, kMinBlocks = 4;
 	static constexpr bool kBranchy = false;
 };
 // Lean viscosity: kSlots tasks per block; warp 0's lanes run their chains,
