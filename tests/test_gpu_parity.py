@@ -196,6 +196,41 @@ def test_dense_cluster_and_bodies():
         _assert_step(res)
 
 
+@pytest.mark.parametrize("lean", [False, True])
+def test_cluster_beyond_the_pair_buffers(lean):
+    """700 particles within 0.1 of one point, without pressure so that they
+    stay together: ~700 in-range pairs each, more than either viscosity
+    shape buffers (the chain computes the geometry inline), and delta lists
+    of 700 entries."""
+    from nbodysimulation_experiment_gb300.simulation import DELTA_WARPS, VISC_WARPS, Params
+    params = scenes.scenario_params()
+    params[5] = 0.0  # stiffness
+    params[6] = 0.0  # near stiffness
+    rng = np.random.default_rng(5)
+    ang = rng.uniform(0, 2 * np.pi, 700)
+    rad = 0.1 * np.sqrt(rng.uniform(0, 1, 700))
+    # Centred on a cell corner (cells of 0.3 from (-5, -2.8125)): ~175 per cell.
+    pts = np.stack([rad * np.cos(ang) + 0.1, rad * np.sin(ang) - 1.0125], 1).astype(np.float32)
+    d = pkg.reference_domain()
+    sim = pkg.Simulation(d)
+    orc = OracleSim()
+    for s in (sim, orc):
+        gpu = s is sim
+        s.set_params(Params.from_array(params)) if gpu else s.set_params(params)
+        s.set_gravity((0.0, -10.0)) if gpu else s.set_gravity(0.0, -10.0)
+        for nx, ny, dist in scenes.box_planes(scenes.REF_WIDTH, scenes.REF_HEIGHT):
+            s.add_plane((nx, ny), dist) if gpu else s.add_plane(nx, ny, dist)
+        s.add_particles(pts)
+    sim.update(float(scenes.DT))
+    orc.update(float(scenes.DT))
+    if lean:
+        base = sim.sweep_shape()
+        sim.set_sweep_shape((VISC_WARPS[1], base[1], DELTA_WARPS[1], base[3]))
+    for _ in range(3):
+        res, _, _ = _teacher_step(sim, orc)
+        _assert_step(res)
+
+
 def test_emitter_matches_reference():
     """Emitters add particles during the update (demo4.cpp:257-284); the
     jitter comes from the C library's rand() in both."""
