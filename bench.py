@@ -10,7 +10,7 @@ segments, gravity (0, -10), the reference's sph.h constants, FP32.
   (a 256 MiB write) between steps, outside the events.
 * ``e2e``: the same metric through the C ABI with host buffers: every step
   loads the full state from pinned host memory (``sph_load_state``), updates
-  and reads the full state back (``sph_dump_state``).
+  and reads the full state back into pinned host memory (``sph_dump_state``).
 * ``roofline``: the dominant kernel (the ordered delta sweep) against the
   measured HBM copy bandwidth; achieved = algorithmic bytes (24 B per
   particle: read position and pressure, write position) / its event-timed
@@ -477,6 +477,12 @@ def main():
         pinned[k] = arr
     pinned["canonical_count"] = st["canonical_count"]
     pinned["grid"] = st["grid"]
+    # The step's result is read back into pinned host memory as well.
+    pinned_out = {}
+    for k in ("pos", "prev", "vel", "acc", "dens", "press", "id", "cell", "cell_start", "cell_count"):
+        a = st[k]
+        pinned_out[k] = torch.empty(a.shape, dtype=torch.float32 if a.dtype == np.float32 else torch.int32,
+                                    pin_memory=True).numpy()
     e2e_steps = max(10, args.steps // 4)
     h2d = sum(pinned[k].nbytes for k in ("pos", "prev", "vel", "acc", "dens", "press", "id", "cell",
                                         "cell_start", "cell_count"))
@@ -487,7 +493,7 @@ def main():
     for _ in range(e2e_steps):
         sim.load_state(pinned)
         sim.update(dt)
-        out = sim.dump_state()
+        out = sim.dump_state(out=pinned_out)
     e2e_s = job_seconds(time.perf_counter() - t0, world, "cuda")
     e2e_value = job_rate(scene.n, e2e_steps, world, e2e_s)
 

@@ -345,6 +345,24 @@ def _state_arrays(n: int, n0: int, gx: int, gy: int):
     return st, v
 
 
+def _state_view_of(out: Dict[str, np.ndarray], n: int, n0: int, gx: int, gy: int):
+    """The ``StateView`` of caller-given host arrays for one dump (checked
+    against the state's sizes)."""
+    shapes = {k: ((n, 2), np.float32) for k in ("pos", "prev", "vel", "acc", "dens", "press")}
+    shapes.update(id=((n,), np.int32), cell=((n,), np.int32), cell_start=((gx * gy,), np.int32),
+                  cell_count=((gx * gy,), np.int32))
+    v = StateView(count=n, canonical_count=n0, grid_x=gx, grid_y=gy)
+    for k, (shape, dtype) in shapes.items():
+        a = out[k]
+        if a.shape != shape or a.dtype != dtype or not a.flags["C_CONTIGUOUS"] or not a.flags["WRITEABLE"]:
+            raise ValueError("dump_state out[%r]: want a writeable contiguous %s array of shape %s"
+                             % (k, np.dtype(dtype).name, shape))
+        setattr(v, k, a.ctypes.data)
+    out["canonical_count"] = n0
+    out["grid"] = (gx, gy)
+    return out, v
+
+
 class Simulation:
     """GB300 Demo4 particle simulation (``BaseSimulation``, base.h:8-38)."""
 
@@ -487,10 +505,12 @@ class Simulation:
         self._call("sph_state_info", _c.byref(n), _c.byref(n0), _c.byref(gx), _c.byref(gy))
         return n.value, n0.value, gx.value, gy.value
 
-    def dump_state(self) -> Dict[str, np.ndarray]:
-        """Full state in the internal numbering (see sph_dump_state)."""
+    def dump_state(self, out: Optional[Dict[str, np.ndarray]] = None) -> Dict[str, np.ndarray]:
+        """Full state in the internal numbering (see sph_dump_state).  With
+        ``out`` (arrays of a previous dump's keys, shapes and types, e.g. in
+        pinned host memory) the state is copied into those arrays."""
         n, n0, gx, gy = self.state_info()
-        st, v = _state_arrays(n, n0, gx, gy)
+        st, v = _state_arrays(n, n0, gx, gy) if out is None else _state_view_of(out, n, n0, gx, gy)
         self._call("sph_dump_state", _c.byref(v))
         return st
 

@@ -55,3 +55,21 @@ def test_create_without_gpu_fails_loudly():
     with pytest.raises(pkg.SphError) as e:
         pkg.Simulation()
     assert e.value.status == simulation.SPH_ERR_NO_DEVICE
+
+
+def test_dump_target_arrays_are_checked():
+    """Caller-given dump arrays must match the state's sizes and types; the
+    view then points at them (no device needed)."""
+    import numpy as np
+    n, n0, gx, gy = 5, 4, 3, 2
+    out = {k: np.zeros((n, 2), np.float32) for k in ("pos", "prev", "vel", "acc", "dens", "press")}
+    out.update(id=np.zeros(n, np.int32), cell=np.zeros(n, np.int32), cell_start=np.zeros(gx * gy, np.int32),
+               cell_count=np.zeros(gx * gy, np.int32))
+    st, v = simulation._state_view_of(out, n, n0, gx, gy)
+    assert st is out and st["canonical_count"] == n0 and st["grid"] == (gx, gy)
+    assert v.pos == out["pos"].ctypes.data and v.cell_count == out["cell_count"].ctypes.data
+    assert v.count == n and v.canonical_count == n0
+    for bad in ({"pos": np.zeros((n + 1, 2), np.float32)}, {"id": np.zeros(n, np.int64)},
+                {"vel": np.zeros((2, n), np.float32).T}):
+        with pytest.raises(ValueError):
+            simulation._state_view_of({**out, **bad}, n, n0, gx, gy)

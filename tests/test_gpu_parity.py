@@ -231,6 +231,25 @@ def test_cluster_beyond_the_pair_buffers(lean):
         _assert_step(res)
 
 
+def test_dump_into_given_arrays():
+    """sph_dump_state into caller-given arrays (the end-to-end benchmark's
+    pinned buffers) gives the same state as a fresh dump."""
+    scene = scenes.dam_break_4096()
+    sim = pkg.Simulation(scene.domain())
+    scene.apply(sim)
+    for _ in range(3):
+        sim.update(float(scenes.DT))
+    want = sim.dump_state()
+    out = {k: np.full_like(v, 7) for k, v in want.items() if isinstance(v, np.ndarray)}
+    got = sim.dump_state(out=out)
+    assert got is out
+    for k, v in want.items():
+        if isinstance(v, np.ndarray):
+            assert np.array_equal(got[k], v), k
+    assert got["canonical_count"] == want["canonical_count"] and got["grid"] == want["grid"]
+    sim.close()
+
+
 def test_emitter_matches_reference():
     """Emitters add particles during the update (demo4.cpp:257-284); the
     jitter comes from the C library's rand() in both."""
