@@ -33,7 +33,29 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
-REFERENCE_TREE = "/root/reference"
+
+
+def _reference_tree() -> str:
+    """The reference's source tree: $SPH_REFERENCE_TREE, else the Makefile's
+    REF default (the one recipe that names where the tree lies)."""
+    env = os.environ.get("SPH_REFERENCE_TREE")
+    if env:
+        return env
+    try:
+        with open(os.path.join(HERE, "Makefile")) as f:
+            for line in f:
+                if line.startswith("REF ?="):
+                    return line.split("?=", 1)[1].strip()
+    except OSError:
+        pass
+    return ""
+
+
+REFERENCE_TREE = _reference_tree()
+
+
+def reference_tree_present() -> bool:
+    return bool(REFERENCE_TREE) and os.path.isdir(os.path.join(REFERENCE_TREE, "NBodySimulation"))
 
 _c = ctypes
 _vp = _c.c_void_p
@@ -58,9 +80,9 @@ class DomainStruct(ctypes.Structure):
 def build(reference: bool = True) -> None:
     """Build the restatement, and the reference harness where the tree exists."""
     targets = ["all"]
-    if reference and os.path.isdir(os.path.join(REFERENCE_TREE, "NBodySimulation")):
+    if reference and reference_tree_present():
         targets.append("reference")
-    subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
+    subprocess.run(["make", "-s", "-C", HERE, "REF=" + (REFERENCE_TREE or ".")] + targets, check=True)
 
 
 def reference_available() -> bool:

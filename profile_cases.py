@@ -2,20 +2,24 @@
 profiler such as Nsight Compute (each runs a few launches of its kernels on
 inputs larger than L2 but a few hundred MB on the device at most).
 
-    python -m nbodysimulation_experiment_gb300.profile_cases plain
-    python -m nbodysimulation_experiment_gb300.profile_cases springs
-    python -m nbodysimulation_experiment_gb300.profile_cases mpnn
-    python -m nbodysimulation_experiment_gb300.profile_cases batched
-    python -m nbodysimulation_experiment_gb300.profile_cases learned_frame
+    python profile_cases.py plain
+    python profile_cases.py springs
+    python profile_cases.py mpnn
+    python profile_cases.py batched
+    python profile_cases.py learned_frame
 """
 from __future__ import annotations
 
+import os
 import sys
 
-import numpy as np
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
 
-from . import learned, scenes
-from .simulation import DELTA_WARPS, VISC_WARPS, BatchSimulation, Mpnn, Simulation
+from nbodysimulation_experiment_gb300 import learned, scenes  # noqa: E402
+from nbodysimulation_experiment_gb300.simulation import (  # noqa: E402
+    DELTA_WARPS, VISC_WARPS, BatchSimulation, Mpnn, Simulation)
 
 
 def plain(updates: int = 3, warm: int = 20) -> None:

@@ -67,7 +67,7 @@ def test_params_ctor8_quirk():
         assert np.array_equal(mine, stored)
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/NBodySimulation"), reason="reference tree not present")
+@pytest.mark.skipif(not oracle.reference_tree_present(), reason="reference tree not present")
 def test_restatement_matches_reference_build_step_by_step():
     from oracle.oracle import ReferenceSim
     assert oracle.reference_available()
@@ -89,7 +89,7 @@ def test_restatement_matches_reference_build_step_by_step():
         assert np.array_equal(ref.get_stats()[0], orc.get_stats()[0])
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/NBodySimulation"), reason="reference tree not present")
+@pytest.mark.skipif(not oracle.reference_tree_present(), reason="reference tree not present")
 def test_reference_multithreading_is_racy_but_single_worker_deterministic():
     """The reference's threaded scatter races (demo4.cpp:233-234, 250); only
     its single-worker order is a reproducible oracle."""
