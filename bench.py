@@ -1,38 +1,47 @@
 """Benchmark of the GB300 Demo4 SPH step (one JSON line on rank 0).
 
-Workload (one "step" = one ``Update`` of the whole scene): ``obstacles_65536``
--- a 256x256 jittered block (65,536 particles, spacing h/6) in a 51.2 x 28.8
-box with four walls, eight seeded circles (radii 2h..6h) and four seeded line
-segments, gravity (0, -10), the reference's sph.h constants, FP32.
+Headline workload (one "step" = one ``Update`` of the whole scene):
+``block_1m_springs`` -- a 1024x1024 jittered lattice (1,048,576 particles,
+spacing h/6, uniform jitter +-0.1h) in a 204.8 x 115.2 box with four walls,
+gravity (0, -10), the reference's sph.h constants, FP32, with viscoelastic
+springs on (yield ratio 0.1, plasticity 0.3, spring stiffness 0.3, at most 16
+springs per particle in fixed-capacity int32/float tables).
 
 * ``value``: particle-steps/s with the scene resident in HBM; each timed step
   is bracketed by CUDA events on the simulation's stream, and L2 is flushed
   (a 256 MiB write) between steps, outside the events.
 * ``e2e``: the same metric through the C ABI with host buffers: every step
-  loads the full state from pinned host memory (``sph_load_state``), updates
-  and reads the full state back into pinned host memory (``sph_dump_state``).
-* ``roofline``: the dominant kernel (the ordered delta sweep) against the
-  measured HBM copy bandwidth; achieved = algorithmic bytes (24 B per
-  particle: read position and pressure, write position) / its event-timed
-  duration.
+  loads the full state and the spring tables from pinned host memory
+  (``sph_load_state``, ``sph_load_springs``), updates, and reads the state
+  and the spring tables back into pinned host memory (``sph_dump_state``,
+  ``sph_dump_springs``).
+* ``roofline``: the dominant kernel of the step (the slower of the two ordered
+  sweeps) against the measured HBM copy bandwidth; achieved = its algorithmic
+  bytes (24 B per particle: read position and velocity or pressure, write
+  velocity or position) / its event-timed duration.  ``roofline.step`` puts
+  the whole step's algorithmic bytes (480 B per particle-step with springs)
+  over the step time.
 * ``cpu_baseline``: the CPU restatement of the reference step (oracle/),
   multithreaded like the reference's ThreadPool on all host cores, on a
   bounded sample of the same workload.
 
-Further objects in the same line (forms of the step beyond the reference):
+Further objects in the same line (other configurations and forms of the step):
 
+* ``obstacles_65536``: the 65,536-particle scene (256x256 block, 51.2 x 28.8
+  box, walls, 8 circles, 4 segments), plain step, with its own e2e and
+  roofline.
+* ``block_1m_plain``: the 1,048,576-particle block without springs.
 * ``batched``: 512 independent scenes (log-uniform 1,024..65,536 particles,
   ~8.1M in all) advanced by one update per step from the per-step CUDA graph,
   sweep shapes chosen by the autotuner.
-* ``block_1m``: the 1,048,576-particle block, plain and with viscoelastic
-  springs.
 * ``learned``: the message-passing network trained on the GPU on plain
   frames of seeded 65,536-particle scenes, then learned frames on a
   262,144-particle dam break with obstacles against plain frames (four
   updates of dt/4), under the density-deviation judge.
 
-``--impl reference`` times that CPU implementation alone (rank 0 only).
-Multi-GPU runs are independent replicas (the step does not shard).
+``--impl reference`` times that CPU implementation alone on the headline
+workload (rank 0 only).  Multi-GPU runs are independent replicas (the step
+does not shard).
 """
 from __future__ import annotations
 
@@ -53,9 +62,28 @@ if ROOT not in sys.path:
 
 METRIC = "particle-steps/s (1 GB300) plain vs batched vs learned at stated density error"
 UNIT = "particle-steps/s"
-DELTA_BYTES_PER_PARTICLE = 24  # read pos 8 + pressure 8, write pos 8
-WORKLOAD = ("obstacles_65536: 65,536-particle jittered block (spacing h/6) in a 51.2 x 28.8 box, "
-            "4 walls + 8 circles + 4 segments, plain Demo4 step (viscosity on, springs off), FP32")
+SWEEP_BYTES_PER_PARTICLE = 24  # viscosity: read pos + vel, write vel; delta: read pos + pressure, write pos
+STEP_BYTES_PLAIN = 224         # whole plain step, compulsory HBM bytes per particle-step
+STEP_BYTES_SPRINGS = 480       # with 16 spring slots (int32 partner + float rest length), read and written
+SPRINGS = dict(yield_ratio=0.1, plasticity=0.3, stiffness=0.3, max_per_particle=16)
+
+WORKLOADS = {
+    "block_1m_springs": ("block_1m", True,
+                         "block_1m_springs: 1,048,576-particle 1024x1024 jittered lattice (spacing h/6) in a "
+                         "204.8 x 115.2 box, 4 walls, viscoelastic springs on (yield 0.1, plasticity 0.3, "
+                         "stiffness 0.3, <= 16 per particle), FP32"),
+    "obstacles_65536": ("obstacles_65536", False,
+                        "obstacles_65536: 65,536-particle jittered block (spacing h/6) in a 51.2 x 28.8 box, "
+                        "4 walls + 8 circles + 4 segments, plain Demo4 step (viscosity on, springs off), FP32"),
+    "block_1m_plain": ("block_1m", False,
+                       "block_1m_plain: 1,048,576-particle 1024x1024 jittered lattice (spacing h/6) in a "
+                       "204.8 x 115.2 box, 4 walls, plain Demo4 step (springs off), FP32"),
+}
+HEADLINE = "block_1m_springs"
+
+STAGES = ("time_integration", "time_viscosity_forces", "time_predict", "time_update_grid",
+          "time_neighbor_search", "time_density_and_pressure", "time_delta_positions", "time_collisions")
+STAGE_KEYS = {"time_neighbor_search": "springs"}
 
 
 def dist_env():
@@ -93,14 +121,15 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def profile_traffic(n_particles: int):
-    """DRAM bytes per launch of the delta sweep from the committed ncu
-    summary (captured on a smaller case, scaled by particle count)."""
-    path = os.path.join(ROOT, "profiles", "k_delta_traffic.json")
+def profile_traffic(kernel: str, n_particles: int):
+    """DRAM bytes per launch of `kernel` from the committed ncu summaries
+    (captured on a smaller case of the same kernel and shape, scaled by
+    particle count), or None."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic.json")
     try:
         with open(path) as f:
             d = json.load(f)
-        return float(d["dram_bytes_per_particle"]) * n_particles
+        return float(d[kernel]["dram_bytes_per_particle"]) * n_particles
     except Exception:
         return None
 
@@ -157,26 +186,55 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(scene, state_gpu, steps: int, workers: int):
-    """Time the CPU restatement (multithreaded like the reference) on a
-    bounded sample: `steps` updates from the GPU's mid-run state."""
+def host_memory_gb() -> float:
+    """Memory this process may use, in GB (host availability, capped by the
+    control group's limit where one is set)."""
+    avail = os.sysconf("SC_AVPHYS_PAGES") * os.sysconf("SC_PAGE_SIZE")
+    for path in ("/sys/fs/cgroup/memory.max", "/sys/fs/cgroup/memory/memory.limit_in_bytes"):
+        try:
+            with open(path) as f:
+                v = f.read().strip()
+            if v.isdigit():
+                avail = min(avail, int(v))
+        except OSError:
+            pass
+    return avail / 1e9
+
+
+# Host memory the CPU restatement needs per particle: the reference's layout
+# (1,000 neighbour slots of 8 bytes per particle, 500 per cell).
+ORACLE_BYTES_PER_PARTICLE = 9000
+
+
+def make_scene(workload: str):
+    from nbodysimulation_experiment_gb300 import scenes
+    name, springs, desc = WORKLOADS[workload]
+    return getattr(scenes, name)(), springs, desc
+
+
+def cpu_port_rate(scene, springs: bool, workers: int, min_updates: int, budget_s: float, warm_updates: int = 1):
+    """Time the CPU restatement of the reference step (multithreaded like the
+    reference's ThreadPool) on the scene from its start: the first update
+    (AddParticle order) and `warm_updates` more untimed, then updates until
+    `min_updates` ran and `budget_s` passed.  Returns (particle-steps/s,
+    updates timed, seconds)."""
+    from nbodysimulation_experiment_gb300 import scenes
     from oracle.oracle import OracleSim
-    from oracle import state as ostate
     orc = OracleSim(scene.oracle_domain(OracleSim), fp64=False, workers=workers)
     scene.apply(orc)
-    orc.set_state(ostate.to_reference_state(state_gpu))
-    orc.update(float(scene_dt()))  # warm the pool and caches
+    if springs:
+        orc.set_springs(True, **SPRINGS)
+    dt = float(scenes.DT)
+    for _ in range(1 + warm_updates):
+        orc.update(dt)
     t0 = time.perf_counter()
-    for _ in range(steps):
-        orc.update(float(scene_dt()))
-    dt = time.perf_counter() - t0
+    k = 0
+    while k < min_updates or time.perf_counter() - t0 < budget_s:
+        orc.update(dt)
+        k += 1
+    sec = time.perf_counter() - t0
     orc.close()
-    return scene.n * steps / dt, dt
-
-
-def scene_dt():
-    from nbodysimulation_experiment_gb300 import scenes
-    return scenes.DT
+    return scene.n * k / sec, k, sec
 
 
 def run_reference_arm(args):
@@ -185,35 +243,182 @@ def run_reference_arm(args):
         return 0
     from nbodysimulation_experiment_gb300 import scenes
     from oracle.oracle import OracleSim, build as build_oracle
-    build_oracle(reference=True)
-    scene = scenes.obstacles_65536()
+    build_oracle(reference=False)
+    scene, springs, desc = make_scene(args.workload)
+    need = 2.0 * ORACLE_BYTES_PER_PARTICLE * scene.n / 1e9
+    if host_memory_gb() < need:
+        print(json.dumps({"impl": "reference", "unavailable": "the CPU step at %d particles needs ~%.0f GB of host "
+                          "memory; %.0f GB available" % (scene.n, need, host_memory_gb())}), flush=True)
+        return 0
     workers = OracleSim.hardware_threads()
     orc = OracleSim(scene.oracle_domain(OracleSim), fp64=False, workers=workers)
     scene.apply(orc)
-    orc.update(float(scenes.DT))  # first update (AddParticle order)
-    per = max(1, args.cpu_steps // max(1, args.steps))
+    if springs:
+        orc.set_springs(True, **SPRINGS)
+    dt = float(scenes.DT)
+    orc.update(dt)  # first update (AddParticle order)
+    per = max(1, args.cpu_steps // max(1, args.steps)) if args.workload != HEADLINE else 1
     for _ in range(args.warmup):
-        orc.update(float(scenes.DT))
+        orc.update(dt)
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
         for _ in range(per):
-            orc.update(float(scenes.DT))
+            orc.update(dt)
         times.append(time.perf_counter() - t0)
+    orc.close()
     total = sum(times)
     value = scene.n * per * args.steps / total
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / (per * args.steps),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded)", "config": {"workload": WORKLOAD, "particles": scene.n},
+        "data": "synthetic (seeded)", "config": {"workload": desc, "particles": scene.n, "springs": springs},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": workers, "kind": "port",
-                         "sample": "%d updates of the %d-particle scene per step, %d steps, after %d warm-up "
-                                   "updates" % (per, scene.n, args.steps, args.warmup + 1)},
+                         "sample": "%d update(s) of the %d-particle scene per step, %d steps, after %d warm-up "
+                                   "updates from the scene's start" % (per, scene.n, args.steps, args.warmup + 1)},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def sweep_kernels(shape):
+    """Kernel names of the two ordered sweeps for a launch shape
+    (viscosity warps, blocks, delta warps, blocks)."""
+    visc = "k_viscosity_multi<ViscLean>" if shape[0] == 5 else "k_viscosity<ViscWide>"
+    delta = {12: "k_delta<DeltaWide>", 8: "k_delta<DeltaMid>", 2: "k_delta<DeltaLean>"}.get(shape[2], "k_delta")
+    return visc, delta
+
+
+def pinned_like(torch, arrays):
+    out = {}
+    for k, a in arrays.items():
+        t = torch.empty(a.shape, dtype=torch.float32 if a.dtype == np.float32 else torch.int32, pin_memory=True)
+        out[k] = t.numpy()
+        out[k][...] = a
+    return out
+
+
+STATE_KEYS = ("pos", "prev", "vel", "acc", "dens", "press", "id", "cell", "cell_start", "cell_count")
+
+
+def measure_scene(torch, pkg, workload: str, device: int, steps: int, warmup: int, world: int, flush,
+                  e2e_steps: int, clocks: bool = False):
+    """One configuration of the plain (or springs) step: device-resident
+    event-timed updates with L2 flushed between them, per-stage times, the
+    dominant sweep's roofline, and the end-to-end rate through the C ABI with
+    pinned host buffers."""
+    from nbodysimulation_experiment_gb300 import scenes
+    scene, springs, desc = make_scene(workload)
+    sim = pkg.Simulation(scene.domain(), device=device)
+    scene.apply(sim)
+    if springs:
+        sim.set_springs(True, **SPRINGS)
+    dt = float(scenes.DT)
+    stream = torch.cuda.ExternalStream(sim.stream())
+    for _ in range(warmup):
+        sim.update(dt)
+    sim.synchronize()
+    tuned = sim.autotune(dt)
+
+    launches0 = sim.kernel_launches()
+    sampler = ClockSampler(device) if clocks else None
+    if sampler:
+        sampler.start()
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    step_ms = []
+    stage_sum = dict.fromkeys(STAGES, 0.0)
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        sim.update(dt)
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        stats = sim.get_stats()
+        for k in STAGES:
+            stage_sum[k] += getattr(stats, k)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clock_rec = sampler.stop() if sampler else None
+    launches = sim.kernel_launches() - launches0
+    total_s = job_seconds(sum(step_ms) / 1e3, world, "cuda")
+    value = job_rate(scene.n, steps, world, total_s)
+    stage_ms = {STAGE_KEYS.get(k, k[5:]): v / steps for k, v in stage_sum.items()}
+
+    rd = sim.read_particles(("dens",))
+    rho0 = float(scene.params[4])
+    dens_err = float(np.mean(np.abs(rd["dens"][:, 0] - rho0)) / rho0)
+    spring_count = sim.spring_count() if springs else None
+
+    # --- end to end through the C ABI with host buffers ---------------------
+    st = sim.dump_state()
+    pinned = pinned_like(torch, {k: st[k] for k in STATE_KEYS})
+    pinned["canonical_count"] = st["canonical_count"]
+    pinned["grid"] = st["grid"]
+    pinned_out = pinned_like(torch, {k: st[k] for k in STATE_KEYS})
+    h2d = sum(pinned[k].nbytes for k in STATE_KEYS)
+    spr_in = spr_out = None
+    if springs:
+        cnt, part, rest = sim.dump_springs()
+        spr_in = pinned_like(torch, {"count": cnt, "partner": part, "rest": rest})
+        spr_out = pinned_like(torch, {"count": cnt, "partner": part, "rest": rest})
+        h2d += sum(a.nbytes for a in spr_in.values())
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sim.load_state(pinned)
+        if springs:
+            sim.load_springs(spr_in["count"], spr_in["partner"], spr_in["rest"])
+        sim.update(dt)
+        sim.dump_state(out=pinned_out)
+        if springs:
+            sim.dump_springs(out=spr_out)
+    e2e_s = job_seconds(time.perf_counter() - t0, world, "cuda")
+    e2e_value = job_rate(scene.n, e2e_steps, world, e2e_s)
+    sim.close()
+
+    hbm, peak_kind = measured_peaks()
+    visc_k, delta_k = sweep_kernels(tuned)
+    if stage_ms["delta_positions"] >= stage_ms["viscosity_forces"]:
+        kern, kms = delta_k, stage_ms["delta_positions"]
+    else:
+        kern, kms = visc_k, stage_ms["viscosity_forces"]
+    alg = SWEEP_BYTES_PER_PARTICLE * scene.n
+    achieved = alg / (kms / 1e3) / 1e9
+    step_bytes = STEP_BYTES_SPRINGS if springs else STEP_BYTES_PLAIN
+    mean_ms = statistics.mean(step_ms)
+    step_gbs = step_bytes * scene.n / (mean_ms / 1e3) / 1e9
+    out = {
+        "workload": desc, "value": value, "unit": UNIT, "ms_per_step": mean_ms, "steps": steps, "warmup": warmup,
+        "particles": scene.n, "springs": springs, "gpu_launches": int(launches),
+        "sweep_shape": {"viscosity_warps": tuned[0], "viscosity_blocks": tuned[1], "delta_warps": tuned[2],
+                        "delta_blocks": tuned[3]},
+        "stage_ms": stage_ms, "density_error": dens_err,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(h2d),
+                "steps": e2e_steps},
+        "roofline": {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": profile_traffic(kern, scene.n),
+                     "algorithmic_bytes": alg, "kernel_ms": kms,
+                     "step": {"bytes_per_particle_step": step_bytes, "achieved": step_gbs,
+                              "frac": step_gbs / hbm}},
+    }
+    if springs:
+        out["spring_count"] = spring_count
+    if clock_rec is not None:
+        out["clocks"] = clock_rec
+    return out
 
 
 def bench_batched(torch, pkg, scenes, device: int, steps: int, warmup: int):
@@ -264,45 +469,6 @@ def bench_batched(torch, pkg, scenes, device: int, steps: int, warmup: int):
             "density_error": float(np.mean(errs)),
             "workload": "512 independent box scenes, particle counts log-uniform in [1024, 65536] (seeded), "
                         "each a jittered block + 0-4 circles, 4 walls, plain step, FP32; inputs > L2"}
-
-
-def bench_block_1m(torch, pkg, scenes, device: int, steps: int, warmup: int, springs: bool):
-    """The 1,048,576-particle block (1024x1024 jittered lattice in a
-    204.8 x 115.2 box, four walls), plain or with viscoelastic springs
-    (yield ratio 0.1, plasticity 0.3, stiffness 0.3, at most 16 per
-    particle); event-timed updates on the simulation's stream."""
-    scene = scenes.block_1m()
-    sim = pkg.Simulation(scene.domain(), device=device)
-    scene.apply(sim)
-    if springs:
-        sim.set_springs(True, yield_ratio=0.1, plasticity=0.3, stiffness=0.3, max_per_particle=16)
-    dt = float(scenes.DT)
-    stream = torch.cuda.ExternalStream(sim.stream())
-    for _ in range(warmup):
-        sim.update(dt)
-    sim.synchronize()
-    tuned = sim.autotune(dt)
-    ms, spring_ms = [], []
-    for _ in range(steps):
-        with torch.cuda.stream(stream):
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-        sim.update(dt)
-        with torch.cuda.stream(stream):
-            e1.record(stream)
-        e1.synchronize()
-        ms.append(e0.elapsed_time(e1))
-        spring_ms.append(sim.get_stats().time_neighbor_search)
-    out = {"value": scene.n * steps / (sum(ms) / 1e3), "unit": UNIT, "ms_per_step": statistics.mean(ms),
-           "steps": steps, "warmup": warmup, "particles": scene.n, "springs": springs,
-           "autotuned_shape": {"viscosity_warps": tuned[0], "viscosity_blocks": tuned[1],
-                               "delta_warps": tuned[2], "delta_blocks": tuned[3]}}
-    if springs:
-        out["spring_phase_ms"] = statistics.mean(spring_ms)
-        out["spring_count"] = sim.spring_count()
-    sim.close()
-    return out
 
 
 def bench_learned(torch, pkg, scenes, device: int, args):
@@ -379,15 +545,18 @@ def bench_learned(torch, pkg, scenes, device: int, args):
 def parse_args(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--cpu-steps", type=int, default=60, help="CPU-baseline sample size in updates")
+    ap.add_argument("--workload", default=HEADLINE, choices=sorted(WORKLOADS),
+                    help="the headline line's workload (the others are extra objects)")
+    ap.add_argument("--cpu-steps", type=int, default=4, help="CPU-baseline sample: at least this many updates")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample: at least this long")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the other configurations' objects")
+    ap.add_argument("--extra-steps", type=int, default=20, help="timed updates of the other configurations")
     ap.add_argument("--batch-steps", type=int, default=20, help="timed updates of the 512-scene batch")
     ap.add_argument("--no-batch", action="store_true")
-    ap.add_argument("--block-steps", type=int, default=10, help="timed updates of the 1M-particle block")
-    ap.add_argument("--no-block", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--learned-scenes", type=int, default=100, help="seeded 65,536-particle training scenes")
     ap.add_argument("--learned-frames", type=int, default=20, help="training frames captured per scene")
@@ -414,143 +583,60 @@ def main():
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     pkg.build()
-
-    scene = scenes.obstacles_65536()
-    sim = pkg.Simulation(scene.domain(), device=local)
-    scene.apply(sim)
-    dt = float(scenes.DT)
-    stream = torch.cuda.ExternalStream(sim.stream())
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
-    for _ in range(args.warmup):
-        sim.update(dt)
-    sim.synchronize()
-    tuned = sim.autotune(dt)
+    head = measure_scene(torch, pkg, args.workload, local, args.steps, args.warmup, world, flush,
+                         max(10, args.steps // 4), clocks=True)
 
-    # --- device-resident timed region -------------------------------------
-    launches0 = sim.kernel_launches()
-    sampler = ClockSampler(local)
-    sampler.start()
-    if world > 1:
-        dist.barrier()
-    torch.cuda.synchronize()
-    step_ms, delta_ms = [], []
-    stage_names = ("time_integration", "time_viscosity_forces", "time_predict", "time_update_grid",
-                   "time_neighbor_search", "time_density_and_pressure", "time_delta_positions", "time_collisions")
-    stage_sum = dict.fromkeys(stage_names, 0.0)
-    for _ in range(args.steps):
-        with torch.cuda.stream(stream):
-            flush.zero_()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-        sim.update(dt)
-        with torch.cuda.stream(stream):
-            e1.record(stream)
-        e1.synchronize()
-        step_ms.append(e0.elapsed_time(e1))
-        stats = sim.get_stats()
-        delta_ms.append(stats.time_delta_positions)
-        for k in stage_names:
-            stage_sum[k] += getattr(stats, k)
-    torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
-    clocks = sampler.stop()
-    launches = sim.kernel_launches() - launches0 - 0  # get_stats launches nothing
-    total_s = job_seconds(sum(step_ms) / 1e3, world, "cuda")
-    value = job_rate(scene.n, args.steps, world, total_s)
-
-    # density deviation from the rest density at the end of the run
-    rd = sim.read_particles(("dens",))
-    rho0 = float(scene.params[4])
-    dens_err = float(np.mean(np.abs(rd["dens"][:, 0] - rho0)) / rho0)
-
-    # --- end to end through the C ABI with host buffers --------------------
-    st = sim.dump_state()
-    pinned = {}
-    for k in ("pos", "prev", "vel", "acc", "dens", "press", "id", "cell", "cell_start", "cell_count"):
-        a = st[k]
-        t = torch.empty(a.shape, dtype=torch.float32 if a.dtype == np.float32 else torch.int32, pin_memory=True)
-        arr = t.numpy()
-        arr[...] = a
-        pinned[k] = arr
-    pinned["canonical_count"] = st["canonical_count"]
-    pinned["grid"] = st["grid"]
-    # The step's result is read back into pinned host memory as well.
-    pinned_out = {}
-    for k in ("pos", "prev", "vel", "acc", "dens", "press", "id", "cell", "cell_start", "cell_count"):
-        a = st[k]
-        pinned_out[k] = torch.empty(a.shape, dtype=torch.float32 if a.dtype == np.float32 else torch.int32,
-                                    pin_memory=True).numpy()
-    e2e_steps = max(10, args.steps // 4)
-    h2d = sum(pinned[k].nbytes for k in ("pos", "prev", "vel", "acc", "dens", "press", "id", "cell",
-                                        "cell_start", "cell_count"))
-    torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        sim.load_state(pinned)
-        sim.update(dt)
-        out = sim.dump_state(out=pinned_out)
-    e2e_s = job_seconds(time.perf_counter() - t0, world, "cuda")
-    e2e_value = job_rate(scene.n, e2e_steps, world, e2e_s)
-
-    hbm, peak_kind = measured_peaks()
-    mean_delta_s = statistics.mean(delta_ms) / 1e3
-    achieved = DELTA_BYTES_PER_PARTICLE * scene.n / mean_delta_s / 1e9
-    traffic = profile_traffic(scene.n)
+    extras = {}
+    if not args.no_extra:
+        for w in WORKLOADS:
+            if w != args.workload:
+                extras[w] = measure_scene(torch, pkg, w, local, args.extra_steps, 5, world, flush, 10)
 
     batched = None
     if not args.no_batch:
         batched = bench_batched(torch, pkg, scenes, local, args.batch_steps, 3)
-        batched["vs_plain"] = batched["value"] / value
-
-    block = None
-    if not args.no_block:
-        block = {"plain": bench_block_1m(torch, pkg, scenes, local, args.block_steps, 3, False),
-                 "springs": bench_block_1m(torch, pkg, scenes, local, args.block_steps, 3, True)}
+        batched["vs_plain_1m"] = batched["value"] / extras["block_1m_plain"]["value"] \
+            if "block_1m_plain" in extras else None
 
     learned_line = None
     if not args.no_learned:
         learned_line = bench_learned(torch, pkg, scenes, local, args)
 
     cpu = None
-    if rank == 0 and not args.no_cpu:
+    if rank == 0 and not args.no_cpu and host_memory_gb() >= 2.0 * ORACLE_BYTES_PER_PARTICLE * head["particles"] / 1e9:
         from oracle.oracle import OracleSim, build as build_oracle
         build_oracle(reference=False)
         workers = OracleSim.hardware_threads()
-        cval, csec = cpu_baseline(scene, st, args.cpu_steps, workers)
+        scene, springs, _ = make_scene(args.workload)
+        cval, k, csec = cpu_port_rate(scene, springs, workers, args.cpu_steps, args.cpu_seconds)
         cpu = {"value": cval, "unit": UNIT, "cores": workers, "kind": "port",
-               "sample": "%d updates of the %d-particle scene from the GPU's state after %d updates "
-                         "(%.1f s)" % (args.cpu_steps, scene.n, args.warmup, csec)}
+               "sample": "%d updates of the %d-particle scene%s after its first 2 updates (%.1f s)"
+                         % (k, scene.n, " with springs" if springs else "", csec)}
 
     if rank == 0:
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms), "higher_is_better": True,
+            "metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": {"workload": WORKLOAD, "particles": scene.n, "l2": "flushed between steps (256 MiB write)",
-                       "sweep_shape": {"viscosity_warps": tuned[0], "viscosity_blocks": tuned[1],
-                                       "delta_warps": tuned[2], "delta_blocks": tuned[3]},
+            "config": {"workload": head["workload"], "particles": head["particles"], "springs": head["springs"],
+                       "l2": "flushed between steps (256 MiB write); inputs also exceed L2",
+                       "sweep_shape": head["sweep_shape"],
                        "parallelism": "replicas" if world > 1 else "single GPU",
-                       "density_error": dens_err},
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(h2d)},
-            "gpu_launches": int(launches),
-            "stage_ms": {k[5:]: v / args.steps for k, v in stage_sum.items()},
-            "roofline": {"bound": "hbm", "kernel": "k_delta", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": traffic,
-                         "algorithmic_bytes": DELTA_BYTES_PER_PARTICLE * scene.n,
-                         "kernel_ms": 1e3 * mean_delta_s},
+                       "density_error": head["density_error"], "spring_count": head.get("spring_count")},
+            "e2e": head["e2e"],
+            "gpu_launches": head["gpu_launches"],
+            "stage_ms": head["stage_ms"],
+            "roofline": head["roofline"],
             "cpu_baseline": cpu,
-            "batched": batched,
-            "block_1m": block,
-            "learned": learned_line,
-            "clocks": clocks,
+            "clocks": head.get("clocks"),
         }
+        for w, d in extras.items():
+            line[w] = d
+        line["batched"] = batched
+        line["learned"] = learned_line
         print(json.dumps(line), flush=True)
-    sim.close()
     if world > 1:
         dist.destroy_process_group()
     return 0

@@ -294,6 +294,20 @@ int sph_use_graphs(sph_sim *sim, int enable);
  * block count per SM, keeps the fastest for each sweep, restores the state
  * and reports the choice; it needs a state after an update. */
 int sph_autotune(sph_sim *sim, float dt, int *shape);
+/* No counterpart in the reference (which waits on its worker threads without
+ * a limit, threading.h:101-109).  Every device-side wait of the ordered
+ * sweeps (a task waiting for an earlier task whose neighbourhood overlaps
+ * its own) gives up after `seconds` (default 2): the sweep then stops
+ * waiting, the update's results are not meaningful, and the next call that
+ * synchronises returns SPH_ERR_TIMEOUT.  The simulation stays usable; load a
+ * state (sph_load_state) to continue from known data. */
+int sph_set_wait_limit(sph_sim *sim, double seconds);
+/* No counterpart in the reference; for tests of the timeout path only.  In
+ * the next updates the task claimed at position `claim` of sweep `sweep`
+ * (0 = viscosity, 1 = delta) does its work but never publishes that it is
+ * done, so the tasks that depend on it wait until the wait limit.  -1 turns
+ * it off (the default). */
+int sph_test_hold_task(sph_sim *sim, int sweep, int claim);
 int sph_get_sweep_shape(sph_sim *sim, int *shape);
 int sph_set_sweep_shape(sph_sim *sim, const int *shape);
 

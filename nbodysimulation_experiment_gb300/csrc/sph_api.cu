@@ -158,7 +158,7 @@ struct sph_sim {
 
 namespace {
 
-
+constexpr unsigned long long kDefaultWaitLimitNs = 2000000000ull;  // 2 s per bounded wait
 
 // Text of the last failing CUDA call on this thread (sph_last_error).
 thread_local char g_last_error[256] = "";
@@ -680,6 +680,8 @@ int allocate(sph_sim *s) {
 	    (rc = dalloc(&T.appRun, appCap)) || (rc = dalloc(&T.appBox, 4 * appCap)))
 		return rc;
 	T.moverList = nullptr;
+	T.waitLimitNs = kDefaultWaitLimitNs;
+	T.hold[0] = T.hold[1] = -1;
 
 	// Per scene: colour-major cell rank -- colour (y%3, x%3), then sub-colour
 	// ((y/3)%2, (x/3)%2), then row-major.  Cells of one colour are >= 3
@@ -1896,6 +1898,21 @@ int sph_set_sweep_shape(sph_sim *s, const int *shape) {
 	s->viscBlocks = shape[1];
 	s->deltaShape = dShape;
 	s->deltaBlocks = shape[3];
+	drop_graphs(s);
+	return SPH_OK;
+}
+
+int sph_set_wait_limit(sph_sim *s, double seconds) {
+	if (!s || !(seconds > 0.0) || !(seconds <= 3600.0)) return SPH_ERR_INVALID_ARGUMENT;
+	const double ns = seconds * 1e9;
+	s->T.waitLimitNs = ns < 1.0 ? 1ull : (unsigned long long)ns;
+	drop_graphs(s);  // graphs hold the tables by value
+	return SPH_OK;
+}
+
+int sph_test_hold_task(sph_sim *s, int sweep, int claim) {
+	if (!s || sweep < 0 || sweep > 1 || claim < -1) return SPH_ERR_INVALID_ARGUMENT;
+	s->T.hold[sweep] = claim;
 	drop_graphs(s);
 	return SPH_OK;
 }

@@ -138,6 +138,13 @@ struct SimTables {
 	uint32_t *stats;                   // per scene: minNb, maxNb, minCell, maxCell
 	uint32_t *error;
 	uint32_t *abort;
+	// Bounded waits of the ordered sweeps give up after this many
+	// nanoseconds (sph_set_wait_limit; 2 s by default).
+	unsigned long long waitLimitNs;
+	// Tests of the timeout path only (sph_test_hold_task): the sweep task
+	// claimed at position hold[sweep] (0 = viscosity, 1 = delta) does its
+	// work but never publishes its done flag; -1 = off.
+	int hold[2];
 	Body *bodies;
 	// Spring phase scratch (null when off): chosen candidates per particle
 	// (count, kSprings new numbers), positions after the phase, springs per scene.

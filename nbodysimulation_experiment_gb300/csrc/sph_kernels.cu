@@ -42,7 +42,6 @@ namespace sphgb {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s per wait
 constexpr uint32_t kWaitLimitIter = 1u << 24;
 
 __device__ __forceinline__ uint64_t global_ns() {
@@ -73,9 +72,11 @@ __device__ __forceinline__ void stamp(const SimTables &T, int sweep, int task, i
 
 // Converged bounded wait of a whole warp: each lane names one done flag (or
 // none) and the warp polls until every named flag is set.  All lanes run the
-// same loop, so a wait never leaves a warp diverged.  Gives up after 2 s or
-// 2^24 polls, raising kErrTimeout and the abort flag that ends every wait.
-__device__ __forceinline__ void warp_wait(const uint32_t *flag, uint32_t *abortFlag, uint32_t *err) {
+// same loop, so a wait never leaves a warp diverged.  Gives up after
+// `limitNs` (SimTables::waitLimitNs, 2 s by default) or 2^24 polls, raising
+// kErrTimeout and the abort flag that ends every wait.
+__device__ __forceinline__ void warp_wait(const uint32_t *flag, uint32_t *abortFlag, uint32_t *err,
+                                          unsigned long long limitNs) {
 	if (!__any_sync(kFull, flag != nullptr && ld_acquire(flag) == 0u)) return;
 	const uint64_t t0 = global_ns();
 	unsigned ns = 32;
@@ -83,7 +84,7 @@ __device__ __forceinline__ void warp_wait(const uint32_t *flag, uint32_t *abortF
 		const bool pending = flag != nullptr && ld_acquire(flag) == 0u;
 		if (!__any_sync(kFull, pending)) return;
 		if (__any_sync(kFull, ld_acquire(abortFlag) != 0u)) return;
-		if (__any_sync(kFull, global_ns() - t0 > kWaitLimitNs)) break;
+		if (__any_sync(kFull, global_ns() - t0 > limitNs)) break;
 		__nanosleep(ns);
 		if (ns < 256) ns <<= 1;
 	}
@@ -493,7 +494,7 @@ __global__ void __launch_bounds__(C::kWarps * kWarp, C::kMinBlocks) k_viscosity(
 					const int r2 = T.taskOfCell[c2];
 					if (r2 < t && T.cellCount[c2] > 0) flag = &T.done[r2];
 				}
-				warp_wait(flag, T.abort, T.error);
+				warp_wait(flag, T.abort, T.error, T.waitLimitNs);
 			}
 			__syncthreads();
 			stamp(T, 0, t, 1, tid);
@@ -557,7 +558,7 @@ __global__ void __launch_bounds__(C::kWarps * kWarp, C::kMinBlocks) k_viscosity(
 		}
 		__syncthreads();
 		stamp(T, 0, t, 3, tid);
-		if (tid == 0) st_release(&T.done[t], 1u);
+		if (tid == 0 && i != T.hold[0]) st_release(&T.done[t], 1u);
 	}
 }
 
@@ -584,7 +585,7 @@ struct ViscMultiSmemT {
 	ViscSlotT<C> slot[C::kSlots];
 	int segStart[C::kSlots][9], segOff[C::kSlots][9];
 	int state[C::kSlots], task[C::kSlots], first[C::kSlots], cnt[C::kSlots], own[C::kSlots], L[C::kSlots],
-	    k[C::kSlots], cell[C::kSlots];
+	    k[C::kSlots], cell[C::kSlots], claim[C::kSlots];
 	int m[C::kSlots][2];
 	float h2[C::kSlots], invH[C::kSlots], sigma[C::kSlots], beta[C::kSlots], hdt[C::kSlots];
 	unsigned long long waitSince[C::kSlots];
@@ -683,6 +684,7 @@ __device__ __forceinline__ bool slot_claim(ViscMultiSmemT<C> &S, int s, const Si
 	const int own = __shfl_sync(kFull, incl - nn, 4);
 	if (lane == 0) {
 		S.task[s] = t;
+		S.claim[s] = i;
 		S.cell[s] = c;
 		S.first[s] = T.cellStart[c];
 		S.cnt[s] = T.cellCount[c];
@@ -762,7 +764,7 @@ __device__ __forceinline__ void slot_produce(ViscMultiSmemT<C> &S, int s, const 
 		__threadfence();
 		__syncwarp();
 		if (lane == 0) {
-			st_release(&T.done[S.task[s]], 1u);
+			if (S.claim[s] != T.hold[0]) st_release(&T.done[S.task[s]], 1u);
 			S.state[s] = kSlotFree;
 		}
 		__syncwarp();
@@ -778,7 +780,7 @@ __device__ __forceinline__ void slot_produce(ViscMultiSmemT<C> &S, int s, const 
 	}
 	if (state == kSlotWait) {
 		if (!slot_ready<C>(S, s, T, lane)) {
-			if (lane == 0 && global_ns() - S.waitSince[s] > kWaitLimitNs) {
+			if (lane == 0 && global_ns() - S.waitSince[s] > T.waitLimitNs) {
 				atomicOr(T.error, kErrTimeout);
 				atomicExch(T.abort, 1u);
 			}
@@ -1911,7 +1913,7 @@ __device__ __forceinline__ void wait_canonical(int bx0, int by0, int bx1, int by
 				if (rect_dist(b.x, b.y, b.z, b.w, bx0, by0, bx1, by1) <= 2) flag = &T.done[r2];
 			}
 		}
-		warp_wait(flag, T.abort, T.error);
+		warp_wait(flag, T.abort, T.error, T.waitLimitNs);
 	}
 	__syncthreads();
 }
@@ -1970,7 +1972,7 @@ __global__ void __launch_bounds__(C::kWarps * kWarp, C::kMinBlocks) k_delta(Tota
 					const int4 o = *reinterpret_cast<const int4 *>(&T.appBox[4 * q]);
 					if (rect_dist(o.x, o.y, o.z, o.w, bx0, by0, bx1, by1) <= 2) flag = &T.done[tt.ncell + q];
 				}
-				warp_wait(flag, T.abort, T.error);
+				warp_wait(flag, T.abort, T.error, T.waitLimitNs);
 			}
 			__syncthreads();
 			relax_group<C>(S, p0, p1, bx0, by0, bx1, by1, Q, T, s, base, tid);
@@ -1979,7 +1981,7 @@ __global__ void __launch_bounds__(C::kWarps * kWarp, C::kMinBlocks) k_delta(Tota
 		}
 		__syncthreads();
 		stamp(T, 1, t, 3, tid);
-		if (tid == 0) st_release(&T.done[t], 1u);
+		if (tid == 0 && i != T.hold[1]) st_release(&T.done[t], 1u);
 	}
 }
 

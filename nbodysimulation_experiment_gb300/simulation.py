@@ -229,6 +229,8 @@ def load_library(build_if_missing: bool = True):
         "sph_synchronize": [vp],
         "sph_kernel_launches": [vp, P(_c.c_uint64)],
         "sph_use_graphs": [vp, _c.c_int],
+        "sph_set_wait_limit": [vp, _c.c_double],
+        "sph_test_hold_task": [vp, _c.c_int, _c.c_int],
         "sph_autotune": [vp, _c.c_float, vp],
         "sph_get_sweep_shape": [vp, vp],
         "sph_set_sweep_shape": [vp, vp],
@@ -282,7 +284,7 @@ C_SYMBOLS = (
     "sph_get_stream", "sph_device_arrays", "sph_particle_colors", "sph_render_points", "sph_scenario_count",
     "sph_scenario_describe", "sph_load_scenario", "sph_synchronize",
     "sph_kernel_launches",
-    "sph_use_graphs", "sph_autotune", "sph_get_sweep_shape", "sph_set_sweep_shape", "sph_set_springs", "sph_get_spring_count", "sph_dump_springs", "sph_load_springs",
+    "sph_use_graphs", "sph_autotune", "sph_set_wait_limit", "sph_test_hold_task", "sph_get_sweep_shape", "sph_set_sweep_shape", "sph_set_springs", "sph_get_spring_count", "sph_dump_springs", "sph_load_springs",
     "sph_mpnn_create", "sph_mpnn_destroy", "sph_mpnn_param_count", "sph_mpnn_get_params", "sph_mpnn_set_params",
     "sph_mpnn_capture", "sph_mpnn_sample_count", "sph_mpnn_clear_samples", "sph_mpnn_sample_info",
     "sph_mpnn_read_sample", "sph_mpnn_eval", "sph_mpnn_gradient", "sph_mpnn_train_step", "sph_learned_frame",
@@ -563,6 +565,18 @@ class Simulation:
         """Replay repeated updates from a per-step CUDA graph (default on)."""
         self._call("sph_use_graphs", 1 if enable else 0)
 
+    def set_wait_limit(self, seconds: float) -> None:
+        """Device-side waits of the ordered sweeps give up after ``seconds``
+        (default 2); a wait that runs out makes the next synchronising call
+        raise with SPH_ERR_TIMEOUT (see sph_set_wait_limit)."""
+        self._call("sph_set_wait_limit", float(seconds))
+
+    def test_hold_task(self, sweep: int, claim: int) -> None:
+        """Tests of the timeout path only: the task claimed at position
+        ``claim`` of sweep ``sweep`` (0 viscosity, 1 delta) never publishes
+        that it is done; -1 turns it off (sph_test_hold_task)."""
+        self._call("sph_test_hold_task", int(sweep), int(claim))
+
     def autotune(self, delta_time: float) -> Tuple[int, int, int, int]:
         """Pick the sweeps' launch shapes by timing (state kept); returns
         (viscosity warps, viscosity blocks, delta warps, delta blocks)."""
@@ -593,12 +607,22 @@ class Simulation:
         self._call("sph_get_spring_count", _c.byref(out))
         return out.value
 
-    def dump_springs(self):
-        """(count (n,), partner (n, 16) internal numbers or -1, rest (n, 16))."""
+    def dump_springs(self, out: Optional[Dict[str, np.ndarray]] = None):
+        """(count (n,), partner (n, 16) internal numbers or -1, rest (n, 16)).
+        With ``out`` (keys count, partner, rest of those shapes and types,
+        e.g. in pinned host memory) the tables are copied into those arrays."""
         n = self.get_particle_count()
-        count = np.zeros(n, np.int32)
-        partner = np.zeros((n, SPRING_SLOTS), np.int32)
-        rest = np.zeros((n, SPRING_SLOTS), np.float32)
+        if out is not None:
+            count, partner, rest = out["count"], out["partner"], out["rest"]
+            for a, shape, dtype in ((count, (n,), np.int32), (partner, (n, SPRING_SLOTS), np.int32),
+                                    (rest, (n, SPRING_SLOTS), np.float32)):
+                if a.shape != shape or a.dtype != dtype or not a.flags["C_CONTIGUOUS"] or not a.flags["WRITEABLE"]:
+                    raise ValueError("dump_springs out: want writeable contiguous %s arrays of shape %s"
+                                     % (np.dtype(dtype).name, shape))
+        else:
+            count = np.zeros(n, np.int32)
+            partner = np.zeros((n, SPRING_SLOTS), np.int32)
+            rest = np.zeros((n, SPRING_SLOTS), np.float32)
         self._call("sph_dump_springs", n, count.ctypes.data, partner.ctypes.data, rest.ctypes.data)
         return count, partner, rest
 

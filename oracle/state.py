@@ -151,3 +151,39 @@ def compare_step(gpu_before: Dict[str, np.ndarray], gpu_after: Dict[str, np.ndar
     out["cells_equal"] = float(all(np.array_equal(a, b) for a, b in zip(ref_cells, gpu_cells)))
     out["cell_sets_equal"] = float(all(np.array_equal(np.sort(a), np.sort(b)) for a, b in zip(ref_cells, gpu_cells)))
     return out
+
+
+def colour_rank_order(gx: int, gy: int) -> np.ndarray:
+    """Cells in the library's numbering order: colour (y%3, x%3), then
+    sub-colour ((y/3)%2, (x/3)%2), then row-major."""
+    c = np.arange(gx * gy, dtype=np.int64)
+    x, y = c % gx, c // gx
+    key = (((y % 3) * 3 + (x % 3)) * 4 + ((y // 3) % 2) * 2 + ((x // 3) % 2)) * (1 << 26) + c
+    return c[np.argsort(key, kind="stable")]
+
+
+def from_reference_state(ref: Dict[str, np.ndarray], gx: int, gy: int) -> Dict[str, np.ndarray]:
+    """A library state (``sph_load_state`` dict) holding the reference solver
+    state ``ref`` (oracle ``get_state``), every particle canonical: particles
+    are numbered cell by cell in the library's cell order, each cell's members
+    in the reference's cell-array order; ``id`` keeps the reference's index.
+    Valid where every particle has the list NeighborSearch builds from the
+    current cell arrays, i.e. after an update without added particles."""
+    n = len(ref["pos"])
+    cnt = np.asarray(ref["cell_count"], np.int64)
+    flat = np.asarray(ref["cell_flat"], np.int64)
+    off = np.concatenate([[0], np.cumsum(cnt)])
+    order = colour_rank_order(gx, gy)
+    numbered = np.concatenate([flat[off[c]:off[c + 1]] for c in order]) if n else np.zeros(0, np.int64)
+    start = np.zeros(gx * gy, np.int32)
+    run = 0
+    for c in order:
+        start[c] = run
+        run += int(cnt[c])
+    cell = np.asarray(ref["cell"], np.int64)
+    lin = (cell[:, 1] * gx + cell[:, 0]).astype(np.int32)
+    st = {k: np.ascontiguousarray(np.asarray(ref[k], np.float32)[numbered]) for k in
+          ("pos", "prev", "vel", "acc", "dens", "press")}
+    st.update(id=numbered.astype(np.int32), cell=lin[numbered], cell_start=start,
+              cell_count=cnt.astype(np.int32), canonical_count=n, grid=(gx, gy))
+    return st

@@ -7,6 +7,8 @@ inputs larger than L2 but a few hundred MB on the device at most).
     python profile_cases.py mpnn
     python profile_cases.py batched
     python profile_cases.py learned_frame
+    python profile_cases.py block [side]   # side x side block, springs on, lean sweep shapes
+    python profile_cases.py all            # every kernel of the library, small sizes
 """
 from __future__ import annotations
 
@@ -91,7 +93,48 @@ def learned_frame(frames: int = 3) -> None:
     sim.close()
 
 
-CASES = {"plain": plain, "springs": springs, "mpnn": mpnn, "batched": batched, "learned_frame": learned_frame}
+def block(side: int = 512, updates: int = 3) -> None:
+    """A side x side jittered block with springs on (yield 0.1, plasticity
+    0.3, stiffness 0.3, at most 16), in the lean sweep shapes the autotuner
+    picks for the 1,048,576-particle block (5-warp viscosity at 3 blocks per
+    SM, 2-warp delta at 5 per SM): 3 + `updates` updates."""
+    scene = scenes.block_1m() if side == 1024 else scenes.scaled_block(side, seed=3, obstacles=False)
+    sim = Simulation(scene.domain())
+    scene.apply(sim)
+    sim.set_springs(True, yield_ratio=0.1, plasticity=0.3, stiffness=0.3, max_per_particle=16)
+    for _ in range(3):
+        sim.update(float(scenes.DT))
+    sms = sim.sweep_shape()[3]  # the default delta shape runs one block per SM
+    sim.set_sweep_shape((VISC_WARPS[1], 3 * sms, DELTA_WARPS[1], 5 * sms))
+    for _ in range(updates):
+        sim.update(float(scenes.DT))
+    sim.synchronize()
+    print("particles", scene.n, "springs", sim.spring_count())
+    sim.close()
+
+
+def everything() -> None:
+    """Every kernel the library launches, on small cases: the plain step
+    (wide shapes), the springs block (lean shapes), training steps, learned
+    frames, a small batch and the host-facing reads."""
+    plain(updates=2, warm=4)
+    block(side=512, updates=2)
+    mpnn(steps=2)
+    learned_frame(frames=2)
+    batched(updates=2)
+    scene = scenes.dam_break_4096()
+    sim = Simulation(scene.domain())
+    scene.apply(sim)
+    sim.update(float(scenes.DT))
+    sim.read_particles(("pos", "vel"))
+    sim.particle_colors()
+    sim.render_points(320, 180)
+    sim.close()
+    print("all cases ran")
+
+
+CASES = {"plain": plain, "springs": springs, "mpnn": mpnn, "batched": batched, "learned_frame": learned_frame,
+         "block": block, "all": everything}
 
 if __name__ == "__main__":
-    CASES[sys.argv[1]]()
+    CASES[sys.argv[1]](*[int(a) for a in sys.argv[2:]])

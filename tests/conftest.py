@@ -25,3 +25,18 @@ def oracle_built():
     from oracle import oracle
     oracle.build(reference=True)
     return oracle
+
+
+def host_memory_gb() -> float:
+    """Memory this process may use, in GB: the smaller of the host's
+    available memory and the control group's limit (where one is set)."""
+    avail = os.sysconf("SC_AVPHYS_PAGES") * os.sysconf("SC_PAGE_SIZE")
+    for path in ("/sys/fs/cgroup/memory.max", "/sys/fs/cgroup/memory/memory.limit_in_bytes"):
+        try:
+            with open(path) as f:
+                v = f.read().strip()
+            if v.isdigit():
+                avail = min(avail, int(v))
+        except OSError:
+            pass
+    return avail / 1e9

@@ -10,7 +10,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def test_reference_arm_prints_one_contract_line():
     out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
-                          "--warmup", "3", "--cpu-steps", "1"], cwd=ROOT, capture_output=True, text=True,
+                          "--warmup", "3", "--cpu-steps", "1", "--workload", "obstacles_65536"], cwd=ROOT, capture_output=True, text=True,
                          timeout=600, check=True)
     lines = [ln for ln in out.stdout.splitlines() if ln.startswith("{")]
     assert len(lines) == 1

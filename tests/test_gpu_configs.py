@@ -1,0 +1,107 @@
+"""GPU parity at the benchmark's full sizes, through the C ABI.
+
+* The 1,048,576-particle block with viscoelastic springs on (yield ratio
+  0.1, plasticity 0.3, stiffness 0.3, at most 16 per particle), in the
+  launch shapes the autotuner picks for it: after a few free updates, one
+  update from the GPU's state is taken by both the GPU and the oracle
+  (teacher forcing) and compared particle by particle and spring by spring.
+* The 262,144-particle dam break with obstacles (the learned frame's scene),
+  plain update, the same way.
+
+Gates as in the smaller parity tests: cell arrays identical as ordered id
+sequences, positions and velocities bit-identical (the 1e-5 relative gate is
+the stated tolerance), spring tables identical.
+"""
+import numpy as np
+import pytest
+
+import nbodysimulation_experiment_gb300 as pkg
+from nbodysimulation_experiment_gb300 import scenes
+from oracle import state as ostate
+from oracle.oracle import OracleSim
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-5
+DT = float(scenes.DT)
+SPRINGS = dict(yield_ratio=0.1, plasticity=0.3, stiffness=0.3, max_per_particle=16)
+
+
+def springs_by_id(count, partner, rest, ids):
+    """Spring tables re-indexed by AddParticle index: rows in id order,
+    partners as ids (-1 past the count), rest lengths (0 past the count)."""
+    n = len(count)
+    ids = np.asarray(ids, np.int64)
+    slot = np.arange(partner.shape[1])[None, :]
+    live = slot < np.asarray(count)[:, None]
+    pid = np.where(live, ids[np.where(live, partner, 0)], -1)
+    rl = np.where(live, rest, 0.0).astype(np.float32)
+    out_p = np.empty_like(pid)
+    out_r = np.empty_like(rl)
+    out_c = np.empty(n, np.int64)
+    out_p[ids] = pid
+    out_r[ids] = rl
+    out_c[ids] = count
+    return out_c, out_p, out_r
+
+
+def _check(res):
+    assert res["cell_sets_equal"] == 1.0, res
+    assert res["cells_equal"] == 1.0, res
+    for k in ("pos", "prev", "vel", "dens", "press"):
+        assert res[k + "_rel"] <= REL_TOL, (k, res)
+    assert res["pos_ulp"] == 0 and res["vel_ulp"] == 0, res
+
+
+def test_block_1m_springs_teacher_forced():
+    from conftest import host_memory_gb
+    if host_memory_gb() < 40:
+        pytest.skip("the oracle at 1M particles needs ~15 GB of host memory; %.0f GB available" % host_memory_gb())
+    scene = scenes.block_1m()
+    sim = pkg.Simulation(scene.domain())
+    scene.apply(sim)
+    sim.set_springs(True, **SPRINGS)
+    for _ in range(4):
+        sim.update(DT)
+    sim.autotune(DT)
+    for _ in range(2):
+        sim.update(DT)
+    before = sim.dump_state()
+    cnt, part, rest = sim.dump_springs()
+    assert cnt.sum() > 0
+    orc = OracleSim(scene.oracle_domain(OracleSim))
+    scene.apply(orc)  # bodies, gravity, parameters
+    orc.set_springs(True, **SPRINGS)
+    orc.set_state(ostate.to_reference_state(before))
+    orc.set_spring_state(cnt, np.where(part < 0, 0, part), rest, tag=before["id"])
+    orc.update(DT)
+    sim.update(DT)
+    after = sim.dump_state()
+    ref = orc.get_state(lists=False)
+    _check(ostate.compare_step(before, after, ref))
+    g = springs_by_id(*sim.dump_springs(), after["id"])
+    o = springs_by_id(*orc.get_spring_state(), before["id"])
+    for a, b in zip(g, o):
+        assert np.array_equal(a, b)
+    assert sim.spring_count() * 2 == int(g[0].sum())
+    orc.close()
+    sim.close()
+
+
+def test_dam_break_262144_plain_teacher_forced():
+    scene = scenes.dam_break_262144()
+    sim = pkg.Simulation(scene.domain())
+    scene.apply(sim)
+    for _ in range(6):
+        sim.update(DT)
+    sim.autotune(DT)
+    orc = OracleSim(scene.oracle_domain(OracleSim))
+    scene.apply(orc)
+    for _ in range(2):
+        before = sim.dump_state()
+        orc.set_state(ostate.to_reference_state(before))
+        orc.update(DT)
+        sim.update(DT)
+        _check(ostate.compare_step(before, sim.dump_state(), orc.get_state(lists=False)))
+    orc.close()
+    sim.close()
