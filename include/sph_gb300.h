@@ -294,6 +294,24 @@ int sph_use_graphs(sph_sim *sim, int enable);
  * block count per SM, keeps the fastest for each sweep, restores the state
  * and reports the choice; it needs a state after an update. */
 int sph_autotune(sph_sim *sim, float dt, int *shape);
+/* Particle order of the update (single-scene simulations).  By default the
+ * library renumbers particles cell by cell after every update (colour-major
+ * cells, each cell's array in the reference's order) and runs the two
+ * ordered passes (viscosity, delta) and the grid update in that numbering:
+ * one update from a given state equals the reference's Update on the same
+ * numbered state, but a run of many updates visits particles in a different
+ * order from the reference's own run (demo4.cpp:223-255, 344-352 loop over
+ * the reference's index order, which is AddParticle order), so its
+ * trajectory drifts from the reference's by rounding from the second update
+ * on.  enable = 1 selects reference order: both passes and the grid update
+ * visit particles in AddParticle order, so every update equals the
+ * reference's single-worker Update on the reference's own numbering, and a
+ * free run reproduces the reference's trajectory bit for bit.  The storage
+ * numbering (sph_dump_state) is unchanged; reference order costs speed (its
+ * tasks follow AddParticle order, not the cell colouring) and is meant for
+ * validation and reproduction.  Default 0. */
+int sph_set_reference_order(sph_sim *sim, int enable);
+int sph_get_reference_order(sph_sim *sim, int *out);
 /* No counterpart in the reference (which waits on its worker threads without
  * a limit, threading.h:101-109).  Every device-side wait of the ordered
  * sweeps (a task waiting for an earlier task whose neighbourhood overlaps
@@ -390,19 +408,28 @@ int sph_batch_dump_state(sph_sim *sim, size_t scene, const sph_state_view *out);
  * (code running inside another component's memory budget or allocator, or a
  * real-time loop that must not allocate): density and pressure
  * (SPHComputeDensity/SPHComputePressure semantics, what one update computes
- * for freshly added particles) of `count` particles whose positions are on
- * the current device at `pos`, written to `dens` (density, near density) and
- * `press` (pressure, near pressure), enqueued on `stream` (a cudaStream_t;
- * NULL = legacy default stream).  It allocates nothing: its working memory is
- * one fixed device array inside the library, sized for at most
+ * for freshly added, motionless particles without gravity) of `count`
+ * particles whose positions are on the current device at `pos`, written to
+ * `dens` (density, near density) and `press` (pressure, near pressure).  The
+ * work runs on `stream` (a cudaStream_t; NULL = legacy default stream) and
+ * the call returns once it is done.  It allocates nothing: its working
+ * memory is one fixed device array inside the library, sized for at most
  * SPH_NOALLOC_MAX_PARTICLES particles and SPH_NOALLOC_MAX_CELLS grid cells
- * (about 5 MiB, held by every GPU that loads the library until the process
- * exits); larger inputs return SPH_ERR_CAPACITY.  The first call on a device
- * looks up that array's device address; make it before any stream capture.
- * All calls share the array: calls whose work overlaps on the GPU (other
- * streams, other threads) race and must be serialised by the caller. */
+ * (about 6.3 MiB, held by every GPU that loads the library until the process
+ * exits); larger inputs, and domains allowing more than
+ * SPH_NOALLOC_MAX_NEIGHBORS neighbours, return SPH_ERR_CAPACITY before any
+ * work.  The domain's capacities hold as in the update: a cell with more
+ * than max_cell_particles particles, or a 3x3 block listing more than
+ * max_neighbors, is skipped and the call returns SPH_ERR_CAPACITY (the
+ * reference asserts there).  The first call on a device looks up that
+ * array's device address and keeps it for the life of the process; make it
+ * before any stream capture, and do not call this entry point on a device
+ * after cudaDeviceReset.  All calls share the array: calls whose work
+ * overlaps on the GPU (other streams, other threads) race and must be
+ * serialised by the caller. */
 #define SPH_NOALLOC_MAX_PARTICLES 262144
 #define SPH_NOALLOC_MAX_CELLS 262144
+#define SPH_NOALLOC_MAX_NEIGHBORS 4096
 int sph_density_pressure_noalloc(const sph_domain *domain, const sph_params *params, const sph_vec2 *pos,
                                  size_t count, sph_vec2 *dens, sph_vec2 *press, void *stream);
 

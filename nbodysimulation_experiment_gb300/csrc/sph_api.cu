@@ -97,6 +97,8 @@ struct sph_sim {
 	int numSMs = 0;
 	int viscBlocks = 0, deltaBlocks = 0, densBlocks = 0, gridBlocks = 0;
 	int viscLean = 0;   // viscosity shape: 0 = wide, 1 = lean (sph_kernels.cuh)
+	bool refOrder = false;  // sweeps and grid events in AddParticle order (sph_set_reference_order)
+	int viscRefBlocks = 0;
 	int deltaShape = 0;  // delta shape: kDeltaWide, kDeltaLean or kDeltaMid
 	bool batch = false;
 	int multithreading = 0;
@@ -245,6 +247,8 @@ Totals totals(const sph_sim *s) {
 	tt.ncell = s->ncellTotal;
 	tt.nApp = s->nApp;
 	tt.nscenes = (int)s->scenes.size();
+	tt.refOrder = s->refOrder ? 1 : 0;
+	tt.nViscRuns = s->refOrder ? (int)((s->scenes[0].n0 + kAppendixRun - 1) / kAppendixRun) : 0;
 	return tt;
 }
 
@@ -421,7 +425,8 @@ int check_device_errors(sph_sim *s) {
 
 // Appendix runs (particles added since the last update, kAppendixRun at a
 // time) of every scene as delta-sweep tasks after the canonical ones,
-// interleaved across scenes.  A run waits for the earlier runs of its scene
+// interleaved across scenes; in reference order, runs of the whole scene in
+// AddParticle order are the only delta-sweep tasks.  A run waits for the earlier runs of its scene
 // whose particles' new cells come within two cells of its own, so a scene's
 // appendix is relaxed as in AddParticle order.
 int upload_appendix_tasks(sph_sim *s) {
@@ -430,7 +435,9 @@ int upload_appendix_tasks(sph_sim *s) {
 	int maxRuns = 0;
 	for (size_t k = 0; k < S; ++k) {
 		const Scene &sc = s->scenes[k];
-		runs[k] = (int)((sc.nDev - sc.n0 + kAppendixRun - 1) / kAppendixRun);
+		// In reference order the delta sweep runs over the whole scene.
+		const size_t first = s->refOrder ? 0 : sc.n0;
+		runs[k] = (int)((sc.nDev - first + kAppendixRun - 1) / kAppendixRun);
 		maxRuns = std::max(maxRuns, runs[k]);
 	}
 	s->nApp = 0;
@@ -483,7 +490,21 @@ int enqueue_step(sph_sim *s, bool capturing) {
 	}
 	SPH_CUDA(mark(kEvIntegrate));
 
-	if (anyCanonical) {
+	if (tt.refOrder) {
+		k_ref_order<<<blocks_for(tt.n, kElemThreads), kElemThreads, 0, st>>>(tt, A.view(), T);
+		SPH_LAUNCHED(s);
+	}
+	if (anyCanonical && tt.refOrder) {
+		SPH_CUDA(cudaMemsetAsync(s->doneV, 0, sizeof(uint32_t) * std::max(tt.nViscRuns, 1), st));
+		SPH_CUDA(cudaMemsetAsync(T.taskCounter, 0, sizeof(int), st));
+		SimTables v = T;
+		v.done = s->doneV;
+		k_visc_boxes<<<blocks_for((size_t)tt.nViscRuns * kWarp, kElemThreads), kElemThreads, 0, st>>>(tt, A.view(),
+		                                                                                          v);
+		SPH_LAUNCHED(s);
+		k_viscosity_ref<<<s->viscRefBlocks, kViscRefWarps * kWarp, 0, st>>>(tt, A.view(), v);
+		SPH_LAUNCHED(s);
+	} else if (anyCanonical) {
 		SPH_CUDA(cudaMemsetAsync(s->doneV, 0, sizeof(uint32_t) * s->ncellTotal, st));
 		SPH_CUDA(cudaMemsetAsync(T.taskCounter, 0, sizeof(int), st));
 		SimTables v = T;
@@ -671,13 +692,16 @@ int allocate(sph_sim *s) {
 	    (rc = dalloc(&T.scanTiles, 3 * ((C + kScanTile - 1) / kScanTile))) ||
 	    (rc = dalloc(&T.liveTask, C)) || (rc = dalloc(&T.liveTiles, (C + kScanTile - 1) / kScanTile)) ||
 	    (rc = dalloc(&T.nLive, 1)) ||
-	    (rc = dalloc(&T.abort, 1)) || (rc = dalloc(&T.bodies, s->bodyCap)) || (rc = dalloc(&s->doneV, C)))
+	    (rc = dalloc(&T.abort, 1)) || (rc = dalloc(&T.bodies, s->bodyCap)))
 		return rc;
 	// Appendix runs: at most one partial run per scene beyond N / kAppendixRun.
 	const size_t appCap = (N + kAppendixRun - 1) / kAppendixRun + S + 1;
 	s->doneDCap = C + appCap;
+	// Viscosity done flags: one per cell, or per run in reference order.
 	if ((rc = dalloc(&s->doneD, s->doneDCap)) || (rc = dalloc(&T.appScene, appCap)) ||
-	    (rc = dalloc(&T.appRun, appCap)) || (rc = dalloc(&T.appBox, 4 * appCap)))
+	    (rc = dalloc(&T.appRun, appCap)) || (rc = dalloc(&T.appBox, 4 * appCap)) ||
+	    (rc = dalloc(&s->doneV, std::max(C, appCap))) || (rc = dalloc(&T.refOrd, N)) ||
+	    (rc = dalloc(&T.viscBox, 4 * appCap)))
 		return rc;
 	T.moverList = nullptr;
 	T.waitLimitNs = kDefaultWaitLimitNs;
@@ -746,6 +770,7 @@ int allocate(sph_sim *s) {
 	s->densBlocks = std::max(1, std::min(blocks_for(C, kDensWarps), 64 * s->numSMs));
 	s->springBlocks = std::max(1, std::min(blocks_for(C, kSpringWarps), 64 * s->numSMs));
 	s->gridBlocks = std::max(1, std::min(blocks_for(C, kGridWarps), 64 * s->numSMs));
+	s->viscRefBlocks = 8 * s->numSMs;
 	return SPH_OK;
 }
 
@@ -1899,6 +1924,21 @@ int sph_set_sweep_shape(sph_sim *s, const int *shape) {
 	s->deltaShape = dShape;
 	s->deltaBlocks = shape[3];
 	drop_graphs(s);
+	return SPH_OK;
+}
+
+int sph_set_reference_order(sph_sim *s, int enable) {
+	Scene *sc = single(s);
+	if (!sc) return not_single(s);
+	if (s->refOrder != (enable != 0)) drop_graphs(s);
+	s->refOrder = enable != 0;
+	s->sceneTableDirty = true;
+	return SPH_OK;
+}
+
+int sph_get_reference_order(sph_sim *s, int *out) {
+	if (!s || !out) return SPH_ERR_INVALID_ARGUMENT;
+	*out = s->refOrder ? 1 : 0;
 	return SPH_OK;
 }
 

@@ -98,6 +98,12 @@ struct Totals {
 	int ncell;      // cells (= canonical sweep tasks)
 	int nApp;       // appendix runs (delta-sweep tasks after the canonical ones)
 	int nscenes;
+	// Reference order (single scene): both sweeps and the grid update run in
+	// AddParticle order, as the reference's Update does on its own numbering;
+	// the delta sweep's tasks are then nApp runs over all particles, and the
+	// viscosity sweep's nViscRuns runs over the canonical ones.
+	int refOrder;
+	int nViscRuns;
 };
 
 // Particle arrays of one buffer set, in the internal numbering.
@@ -123,6 +129,11 @@ struct SimTables {
 	SceneDev *scenes;
 	int *appScene, *appRun;            // appendix run tasks: scene, run within the scene
 	int *appBox;                       // per appendix run: x0, y0, x1, y1 of its particles' new cells
+	// Reference order: refOrd[pBase + id] = number of the particle with
+	// AddParticle index id; viscBox per viscosity run: x0, y0, x1, y1 of its
+	// particles' old cells.
+	int *refOrd;
+	int *viscBox;
 	int *appCount, *appStart, *appIdx, *appCursor;  // appendix members per cell
 	int *newCell;                      // cell after predict, per particle
 	int *enterCount, *leaveCount, *enterOffset, *enterCursor, *enterList;

@@ -894,6 +894,150 @@ __global__ void __launch_bounds__(C::kWarps * kWarp, C::kMinBlocks) k_viscosity_
 }
 
 // ---------------------------------------------------------------------------
+// Reference order (single scene).  The reference's Update visits particles
+// in its own index order, which is AddParticle order for a scene that was
+// built and then stepped (demo4.cpp:223-255, 344-352).  In reference order
+// the library does the same: refOrd lists the particles' numbers in
+// AddParticle order; the viscosity sweep runs as tasks of kAppendixRun
+// consecutive AddParticle indices (k_viscosity_ref), the delta sweep as the
+// same runs over the whole scene (k_delta's run path), and the grid update
+// applies each cell's events in AddParticle order.
+
+__global__ void k_ref_order(Totals tt, Particles P, SimTables T) {
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= tt.n) return;
+	const SceneDev &sc = T.scenes[T.sceneOf[i]];
+	const int id = P.id[i];
+	if (id < 0 || id >= sc.n) {
+		atomicOr(T.error, kErrIndex);
+		return;
+	}
+	T.refOrd[sc.pBase + id] = i;
+}
+
+// Bounding box (cell coordinates) of the old cells of each viscosity run:
+// the cells whose canonical arrays made its particles' neighbour lists.  One
+// warp per run.
+__global__ void k_visc_boxes(Totals tt, Particles P, SimTables T) {
+	const int a = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+	const int lane = threadIdx.x & (kWarp - 1);
+	if (a >= tt.nViscRuns) return;
+	const SceneDev &sc = T.scenes[0];
+	const int gx = sc.p.gx;
+	const int p0 = sc.pBase + a * kAppendixRun;
+	const int p1 = min(sc.pBase + sc.n0, p0 + kAppendixRun);
+	int bx0 = sc.p.gx, by0 = sc.p.gy, bx1 = -1, by1 = -1;
+	for (int k = p0 + lane; k < p1; k += kWarp) {
+		const int lc = P.cellOf[T.refOrd[k]] - sc.cellBase;
+		bx0 = min(bx0, lc % gx);
+		bx1 = max(bx1, lc % gx);
+		by0 = min(by0, lc / gx);
+		by1 = max(by1, lc / gx);
+	}
+	for (int o = 16; o > 0; o >>= 1) {
+		bx0 = min(bx0, __shfl_xor_sync(kFull, bx0, o));
+		by0 = min(by0, __shfl_xor_sync(kFull, by0, o));
+		bx1 = max(bx1, __shfl_xor_sync(kFull, bx1, o));
+		by1 = max(by1, __shfl_xor_sync(kFull, by1, o));
+	}
+	if (lane == 0) *reinterpret_cast<int4 *>(&T.viscBox[4 * a]) = make_int4(bx0, by0, bx1, by1);
+}
+
+// Viscosity sweep in reference order: one warp per task (run a: the
+// canonical particles with AddParticle indices a*kAppendixRun onwards), each
+// task waiting for the earlier runs whose old cells come within two cells of
+// its own.  For each particle, in order, the warp walks its stale list (the
+// 3x3 block of canonical cell arrays around its old cell, demo4.cpp:188-201)
+// 32 entries at a time, computing the pair geometry of the in-range entries
+// (sph.h:497-505), and lane 0 runs the ordered velocity chain over them
+// (demo4.cpp:231-234), velocities in global memory.
+__global__ void __launch_bounds__(kViscRefWarps * kWarp) k_viscosity_ref(Totals tt, Particles P, SimTables T) {
+	__shared__ float4 geo[kViscRefWarps][kWarp];
+	const int lane = threadIdx.x & (kWarp - 1), w = threadIdx.x / kWarp;
+	const SceneDev &sc = T.scenes[0];
+	const StepParams s = sc.p;
+	const int base = sc.cellBase, gx = s.gx, gy = s.gy;
+	const float hdt = 0.5f * s.dt;
+	for (;;) {
+		int a = 0;
+		if (lane == 0) a = atomicAdd(&T.taskCounter[0], 1);
+		a = __shfl_sync(kFull, a, 0);
+		if (a >= tt.nViscRuns) break;
+		const int4 box = *reinterpret_cast<const int4 *>(&T.viscBox[4 * a]);
+		for (int q0 = 0; q0 < a; q0 += kWarp) {
+			const int q = q0 + lane;
+			const uint32_t *flag = nullptr;
+			if (q < a) {
+				const int4 o = *reinterpret_cast<const int4 *>(&T.viscBox[4 * q]);
+				if (rect_dist(o.x, o.y, o.z, o.w, box.x, box.y, box.z, box.w) <= 2) flag = &T.done[q];
+			}
+			warp_wait(flag, T.abort, T.error, T.waitLimitNs);
+		}
+		const int p0 = sc.pBase + a * kAppendixRun;
+		const int p1 = min(sc.pBase + sc.n0, p0 + kAppendixRun);
+		for (int k = p0; k < p1; ++k) {
+			const int i = T.refOrd[k];
+			const int lc = P.cellOf[i] - base;
+			const int cx = lc % gx, cy = lc / gx;
+			const float2 xi = P.pos[i];
+			float2 vi = __ldcg(&P.vel[i]);
+			for (int q = 0; q < 9; ++q) {
+				const int x = cx + q % 3 - 1, y = cy + q / 3 - 1;
+				if (x < 0 || x >= gx || y < 0 || y >= gy) continue;
+				const int c2 = base + y * gx + x;
+				const int st = T.cellStart[c2], nn = T.cellCount[c2];
+				for (int b0 = 0; b0 < nn; b0 += kWarp) {
+					const int e = b0 + lane;
+					bool in = false;
+					if (e < nn) {
+						const int j = st + e;
+						const float2 xj = P.pos[j];
+						const float rx = xj.x - xi.x, ry = xj.y - xi.y;
+						const float r2 = rx * rx + ry * ry;
+						in = r2 < s.h2;
+						if (in) {
+							const float r = sqrtf(r2);
+							const float qq = r * s.invH;
+							float len = r;  // Vec2Length(Rij) == rij
+							if (len == 0.0f) len = 1.0f;
+							const float inv = 1.0f / len;
+							geo[w][lane] = make_float4(__int_as_float(j), rx * inv, ry * inv, 1.0f - qq);
+						}
+					}
+					unsigned mask = __ballot_sync(kFull, in);
+					__syncwarp();
+					if (lane == 0) {
+						while (mask) {
+							const int t = __ffs(mask) - 1;
+							mask &= mask - 1;
+							const float4 g = geo[w][t];
+							const int j = __float_as_int(g.x);
+							const float2 vj = __ldcg(&P.vel[j]);
+							const float2 n = make_float2(g.y, g.z);
+							const float uu = (vi.x - vj.x) * n.x + (vi.y - vj.y) * n.y;
+							if (uu > 0.0f) {
+								const float f = g.w * (s.sigma * uu + s.beta * (uu * uu));
+								const float ix = (f * n.x) * hdt;
+								const float iy = (f * n.y) * hdt;
+								vi.x = vi.x - ix;
+								vi.y = vi.y - iy;
+								__stcg(&P.vel[j], make_float2(ix + vj.x, iy + vj.y));
+							}
+						}
+					}
+					__syncwarp();
+				}
+			}
+			if (lane == 0) __stcg(&P.vel[i], vi);
+			__syncwarp();
+		}
+		__threadfence();
+		__syncwarp();
+		if (lane == 0 && a != T.hold[0]) st_release(&T.done[a], 1u);
+	}
+}
+
+// ---------------------------------------------------------------------------
 // Predict (demo4.cpp:329-337) and the new cell (demo4.cpp:347).  Movers
 // extend the bounding box of new cells of their old cell, count as leaving
 // their old cell and entering their new cell.
@@ -1141,6 +1285,20 @@ struct GridWarp {
 	int enter[kCellCap];
 };
 
+// Numbers sorted by their particles' AddParticle index (reference order).
+__device__ void insertion_sort_by_id(int *a, int n, const int *id) {
+	for (int i = 1; i < n; ++i) {
+		const int v = a[i];
+		const int key = id[v];
+		int j = i - 1;
+		while (j >= 0 && id[a[j]] > key) {
+			a[j + 1] = a[j];
+			--j;
+		}
+		a[j + 1] = v;
+	}
+}
+
 __device__ void insertion_sort(int *a, int n) {
 	for (int i = 1; i < n; ++i) {
 		const int v = a[i];
@@ -1193,13 +1351,15 @@ __global__ void __launch_bounds__(kGridWarps * kWarp) k_grid_update(Totals tt, P
 		for (int j = lane; j < ec; j += kWarp) S.enter[j] = T.enterList[eo + j];
 		__syncwarp();
 		if (lane == 0) {
-			// Appendix members joined in number order; entering particles
-			// are applied in number order.
+			// Appendix members joined in number order (their AddParticle
+			// order); entering particles are applied in number order, or in
+			// AddParticle order in reference order.
 			insertion_sort(S.arr + cc, ac);
-			insertion_sort(S.enter, ec);
+			if (tt.refOrder) insertion_sort_by_id(S.enter, ec, P.id); else insertion_sort(S.enter, ec);
 		}
 		__syncwarp();
-		// Leaving particles, in number order (the array is sorted here).
+		// Leaving particles, in number order (the array is sorted here); in
+		// reference order they are sorted by AddParticle index below.
 		int nl = 0;
 		for (int base = 0; base < init; base += kWarp) {
 			const int j = base + lane;
@@ -1215,11 +1375,15 @@ __global__ void __launch_bounds__(kGridWarps * kWarp) k_grid_update(Totals tt, P
 		}
 		__syncwarp();
 		if (lane == 0) {
+			if (tt.refOrder) insertion_sort_by_id(S.leave, nl, P.id);
 			int cnt = init;
 			int lo = 0x7fffffff, hi = 0;
 			int a = 0, b = 0;
 			while (a < nl || b < ec) {
-				if (b >= ec || (a < nl && S.leave[a] < S.enter[b])) {
+				bool leaveFirst = b >= ec;
+				if (a < nl && b < ec)
+					leaveFirst = tt.refOrder ? P.id[S.leave[a]] < P.id[S.enter[b]] : S.leave[a] < S.enter[b];
+				if (leaveFirst) {
 					const int p = S.leave[a++];
 					int at = 0;
 					while (at < cnt && S.arr[at] != p) ++at;
@@ -1260,18 +1424,19 @@ __global__ void __launch_bounds__(kGridWarps * kWarp) k_grid_update(Totals tt, P
 }
 
 // Bounding box (scene-local cell coordinates) of the new cells of each
-// appendix run; one warp per run.
+// appendix run (in reference order: of each run of the whole scene in
+// AddParticle order); one warp per run.
 __global__ void k_app_boxes(Totals tt, SimTables T) {
 	const int a = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
 	const int lane = threadIdx.x & (kWarp - 1);
 	if (a >= tt.nApp) return;
 	const SceneDev &sc = T.scenes[T.appScene[a]];
 	const int gx = sc.p.gx;
-	const int p0 = sc.pBase + sc.n0 + T.appRun[a] * kAppendixRun;
+	const int p0 = sc.pBase + (tt.refOrder ? 0 : sc.n0) + T.appRun[a] * kAppendixRun;
 	const int p1 = min(sc.pBase + sc.n, p0 + kAppendixRun);
 	int bx0 = sc.p.gx, by0 = sc.p.gy, bx1 = -1, by1 = -1;
 	for (int k = p0 + lane; k < p1; k += kWarp) {
-		const int lc = T.newCell[k] - sc.cellBase;
+		const int lc = T.newCell[tt.refOrder ? T.refOrd[k] : k] - sc.cellBase;
 		bx0 = min(bx0, lc % gx);
 		bx1 = max(bx1, lc % gx);
 		by0 = min(by0, lc / gx);
@@ -1796,14 +1961,15 @@ __device__ __forceinline__ void summer(DeltaSmemT<C> &S, int b, int4 sl, int4 ln
 	}
 }
 
-// Process particles [p0, p1) (old numbers) in order: one staged region if
-// it fits (pipelined), otherwise one 3x3 region per particle.  Per-particle
+// Process particles [p0, p1) (old numbers, or positions in AddParticle order
+// mapped to old numbers by `ord`) in order: one staged region if it fits
+// (pipelined), otherwise one 3x3 region per particle.  Per-particle
 // inputs (new cell, new number, pressure, list slots) are prefetched in
 // chunks, off the serial path.
 template <class C>
-__device__ __forceinline__ void relax_group(DeltaSmemT<C> &S, int p0, int p1, int bx0, int by0, int bx1, int by1,
-                                            const Particles &Q, const SimTables &T, const StepParams &s,
-                                            int cellBase, int tid) {
+__device__ __forceinline__ void relax_group(DeltaSmemT<C> &S, int p0, int p1, const int *ord, int bx0, int by0,
+                                            int bx1, int by1, const Particles &Q, const SimTables &T,
+                                            const StepParams &s, int cellBase, int tid) {
 	constexpr int kDT = C::kWarps * kWarp;
 	constexpr int kP = DeltaSmemT<C>::kProd;
 	const int warp = tid / kWarp, lane = tid & (kWarp - 1);
@@ -1818,8 +1984,9 @@ __device__ __forceinline__ void relax_group(DeltaSmemT<C> &S, int p0, int p1, in
 	int jk0 = 0, nc0 = 0;
 	float2 pk0 = make_float2(0.0f, 0.0f);
 	if (C::kShortEntry && p0 + tid < min(p1, p0 + C::kPrefetch)) {
-		jk0 = T.newLabel[p0 + tid];
-		nc0 = T.newCell[p0 + tid];
+		const int q = ord ? ord[p0 + tid] : p0 + tid;
+		jk0 = T.newLabel[q];
+		nc0 = T.newCell[q];
 		pk0 = Q.press[jk0];
 	}
 	const bool staged = stage_region<C>(S, R, Q, T, s, cellBase, tid);
@@ -1830,8 +1997,9 @@ __device__ __forceinline__ void relax_group(DeltaSmemT<C> &S, int p0, int p1, in
 		const int c1 = min(p1, c0 + C::kPrefetch);
 		for (int k = c0 + tid; k < c1; k += kDT) {
 			const bool first = C::kShortEntry && c0 == p0;
-			const int jk = first ? jk0 : T.newLabel[k];
-			const int nc = first ? nc0 : T.newCell[k];
+			const int q = ord ? ord[k] : k;
+			const int jk = first ? jk0 : T.newLabel[q];
+			const int nc = first ? nc0 : T.newCell[q];
 			S.ppk[k - c0] = first ? pk0 : Q.press[jk];
 			if (staged) {
 				particle_slots<C>(S, R, nc, jk, s, cellBase, T.error, S.pslot[k - c0], S.plen[k - c0]);
@@ -1926,9 +2094,10 @@ __global__ void __launch_bounds__(C::kWarps * kWarp, C::kMinBlocks) k_delta(Tota
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	DeltaSmemT<C> &S = *reinterpret_cast<DeltaSmemT<C> *>(smem_raw);
 	const int tid = threadIdx.x;
-	const int nLive = *T.nLive;
+	const int nLive = tt.refOrder ? 0 : *T.nLive;
 	const int ntask = nLive + tt.nApp;
 	const int moveMax = T.moverCount[1];
+	const int *ord = tt.refOrder ? T.refOrd : nullptr;
 	for (;;) {
 		if (tid == 0) S.task = atomicAdd(&T.taskCounter[1], 1);
 		__syncthreads();
@@ -1947,24 +2116,26 @@ __global__ void __launch_bounds__(C::kWarps * kWarp, C::kMinBlocks) k_delta(Tota
 				const int4 b = *reinterpret_cast<const int4 *>(&T.bbox[4 * c]);
 				wait_canonical<kDT>(b.x, b.y, b.z, b.w, moveMax, t, c, T, s, sc.cellBase, tid);
 				stamp(T, 1, t, 1, tid);
-				relax_group<C>(S, p0, p0 + cnt, b.x, b.y, b.z, b.w, Q, T, s, sc.cellBase, tid);
+				relax_group<C>(S, p0, p0 + cnt, nullptr, b.x, b.y, b.z, b.w, Q, T, s, sc.cellBase, tid);
 				__syncthreads();
 				__threadfence();
 			}
 		} else {
 			// Appendix run: particles added since the last update, after all
 			// canonical tasks; it waits for the earlier runs of its scene
-			// whose new cells come within two cells of its own.
+			// whose new cells come within two cells of its own.  In reference
+			// order every task is such a run, over the whole scene in
+			// AddParticle order.
 			const int a = t - tt.ncell;
 			const int scene = T.appScene[a];
 			const SceneDev &sc = T.scenes[scene];
 			const StepParams s = sc.p;
 			const int base = sc.cellBase;
-			const int p0 = sc.pBase + sc.n0 + T.appRun[a] * kAppendixRun;
+			const int p0 = sc.pBase + (tt.refOrder ? 0 : sc.n0) + T.appRun[a] * kAppendixRun;
 			const int p1 = min(sc.pBase + sc.n, p0 + kAppendixRun);
 			const int4 box = *reinterpret_cast<const int4 *>(&T.appBox[4 * a]);
 			const int bx0 = box.x, by0 = box.y, bx1 = box.z, by1 = box.w;
-			wait_canonical<kDT>(bx0, by0, bx1, by1, moveMax, tt.ncell, -1, T, s, base, tid);
+			if (!tt.refOrder) wait_canonical<kDT>(bx0, by0, bx1, by1, moveMax, tt.ncell, -1, T, s, base, tid);
 			for (int q0 = 0; q0 < a; q0 += kDT) {
 				const int q = q0 + tid;
 				const uint32_t *flag = nullptr;
@@ -1975,7 +2146,7 @@ __global__ void __launch_bounds__(C::kWarps * kWarp, C::kMinBlocks) k_delta(Tota
 				warp_wait(flag, T.abort, T.error, T.waitLimitNs);
 			}
 			__syncthreads();
-			relax_group<C>(S, p0, p1, bx0, by0, bx1, by1, Q, T, s, base, tid);
+			relax_group<C>(S, p0, p1, ord, bx0, by0, bx1, by1, Q, T, s, base, tid);
 			__syncthreads();
 			__threadfence();
 		}

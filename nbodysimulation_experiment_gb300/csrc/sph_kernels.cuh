@@ -49,6 +49,7 @@ constexpr int delta_shape_warps(int shape) {
 	return shape == kDeltaLean ? DeltaLean::kWarps : (shape == kDeltaMid ? DeltaMid::kWarps : DeltaWide::kWarps);
 }
 constexpr int kDensWarps = 8;
+constexpr int kViscRefWarps = 4;  // reference-order viscosity sweep: one task per warp
 constexpr int kGridWarps = 4;
 constexpr int kScanThreads = 1024;
 constexpr int kScanTile = 4 * kScanThreads;  // scan positions per block
@@ -67,6 +68,9 @@ size_t dens_smem_bytes();
 size_t springs_smem_bytes();
 
 __global__ void k_integrate(Totals tt, Particles P, SimTables T);
+__global__ void k_ref_order(Totals tt, Particles P, SimTables T);
+__global__ void k_visc_boxes(Totals tt, Particles P, SimTables T);
+__global__ void k_viscosity_ref(Totals tt, Particles P, SimTables T);
 __global__ void k_predict(Totals tt, Particles P, SimTables T);
 __global__ void k_live_reduce(Totals tt, SimTables T);
 __global__ void k_live_tiles(SimTables T, int ntiles);

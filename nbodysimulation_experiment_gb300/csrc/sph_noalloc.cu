@@ -5,16 +5,27 @@
 // device memory, a plugin host that forbids the runtime's allocator), a
 // real-time loop that must not hit allocation latency or fragmentation.
 // They hand in device pointers for the inputs and outputs; the working
-// memory (cell counts, offsets, per-particle lists) lives in one fixed
-// device array of this file, which every GPU that loads the library holds
-// until the process exits.
+// memory (cell keys, sort buffers, per-cell counts and offsets, a status
+// word) lives in one fixed device array of this file, which every GPU that
+// loads the library holds until the process exits.
 //
 // What it computes: SPHComputeDensity / SPHComputePressure
 // (NBodySimulation/sph.h:465-481) for every particle over the reference's
 // unfiltered 3x3-cell neighbour list (demo4.cpp:183-206), with each cell's
 // array in particle order -- what one Update computes for particles that
-// have just been added with zero velocity.  Same FP32 operation order as the
-// update; sums run in list order.
+// have just been added with zero velocity and no gravity.  Same FP32
+// operation order as the update; sums run in list order.
+//
+// How: every particle gets its cell key (sph.h:450-463, clamped into the
+// grid); a stable least-significant-digit radix sort of the particle indices
+// by cell key (two passes of 9 bits: keys are below 2^18) puts each cell's
+// members in particle order, which is the order AddParticle appends them
+// (demo4.cpp:37-54); per-cell counts and offsets come from a count pass and
+// a scan.  The domain's capacities are enforced: a cell holding more than
+// max_cell_particles, or a 3x3 block listing more than max_neighbors
+// particles, sets a status word and is skipped, and the call then returns
+// SPH_ERR_CAPACITY -- where the reference would assert (demo4.cpp:45, 199).
+// All work is O(particles x max_neighbors).
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -26,22 +37,37 @@ namespace {
 constexpr int kNaThreads = 256;
 constexpr int kNaWarps = 4;
 constexpr int kNaMaxDevices = 64;
+// Radix sort: digits of 9 bits, tiles of kTile particles (8 per thread).
+constexpr int kRadixBits = 9;
+constexpr int kRadix = 1 << kRadixBits;
+constexpr int kItems = 8;
+constexpr int kTile = kNaThreads * kItems;
+constexpr int kMaxTiles = (SPH_NOALLOC_MAX_PARTICLES + kTile - 1) / kTile;
+static_assert(SPH_NOALLOC_MAX_CELLS <= (1 << (2 * kRadixBits)), "cell keys must fit two radix digits");
 
-// Scratch layout (int32): count, start, cursor per cell; unsorted and sorted
-// particle lists.
+// Scratch layout (int32): per cell count and start; per particle the cell
+// key, and the index and key arrays of the two sort passes; per digit and
+// tile the histogram / offset table; the status word.
 constexpr size_t kCountOff = 0;
 constexpr size_t kStartOff = kCountOff + SPH_NOALLOC_MAX_CELLS;
-constexpr size_t kCursorOff = kStartOff + SPH_NOALLOC_MAX_CELLS;
-constexpr size_t kUnsortedOff = kCursorOff + SPH_NOALLOC_MAX_CELLS;
-constexpr size_t kSortedOff = kUnsortedOff + SPH_NOALLOC_MAX_PARTICLES;
-constexpr size_t kScratchInts = kSortedOff + SPH_NOALLOC_MAX_PARTICLES;
+constexpr size_t kKeyOff = kStartOff + SPH_NOALLOC_MAX_CELLS;
+constexpr size_t kIdxAOff = kKeyOff + SPH_NOALLOC_MAX_PARTICLES;
+constexpr size_t kKeyBOff = kIdxAOff + SPH_NOALLOC_MAX_PARTICLES;
+constexpr size_t kIdxBOff = kKeyBOff + SPH_NOALLOC_MAX_PARTICLES;
+constexpr size_t kHistOff = kIdxBOff + SPH_NOALLOC_MAX_PARTICLES;
+constexpr size_t kStatusOff = kHistOff + (size_t)kRadix * kMaxTiles;
+constexpr size_t kScratchInts = kStatusOff + 64;
 
 static __device__ __align__(256) int g_noalloc_scratch[kScratchInts];
+
+enum : int { kStatusCapacity = 1 };
 
 struct NaParams {
 	float halfW, halfH, cellSize;
 	int gx, gy, ncell;
 	float h2, invH, rho0, k, kNear;
+	int maxCell, maxNeighbors;
+	int n, tiles;
 };
 
 __device__ __forceinline__ int na_cell(float2 p, const NaParams &s) {
@@ -52,19 +78,29 @@ __device__ __forceinline__ int na_cell(float2 p, const NaParams &s) {
 	return y * s.gx + x;
 }
 
-__global__ void k_na_count(int n, const float2 *pos, int *scratch, NaParams s) {
+// Cell key and per-cell count of every particle.
+__global__ void k_na_keys(const float2 *pos, int *scratch, NaParams s) {
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i < n) atomicAdd(&scratch[kCountOff + na_cell(pos[i], s)], 1);
+	if (i >= s.n) return;
+	const int c = na_cell(pos[i], s);
+	scratch[kKeyOff + i] = c;
+	atomicAdd(&scratch[kCountOff + c], 1);
 }
 
-// Exclusive scan of the cell counts (one block, contiguous runs per thread).
+// Per-cell exclusive scan (one block, contiguous runs per thread), and the
+// cell-capacity check.
 __global__ void k_na_scan(int *scratch, NaParams s) {
 	__shared__ int sums[kNaThreads];
 	const int tid = threadIdx.x;
 	const int per = (s.ncell + kNaThreads - 1) / kNaThreads;
 	const int b = tid * per, e = min(s.ncell, b + per);
-	int acc = 0;
-	for (int c = b; c < e; ++c) acc += scratch[kCountOff + c];
+	int acc = 0, over = 0;
+	for (int c = b; c < e; ++c) {
+		const int v = scratch[kCountOff + c];
+		acc += v;
+		over |= v > s.maxCell;
+	}
+	if (over) atomicOr(&scratch[kStatusOff], kStatusCapacity);
 	sums[tid] = acc;
 	__syncthreads();
 	for (int off = 1; off < kNaThreads; off <<= 1) {
@@ -80,42 +116,129 @@ __global__ void k_na_scan(int *scratch, NaParams s) {
 	}
 }
 
-__global__ void k_na_scatter(int n, const float2 *pos, int *scratch, NaParams s) {
-	const int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i >= n) return;
-	const int c = na_cell(pos[i], s);
-	const int slot = scratch[kStartOff + c] + atomicAdd(&scratch[kCursorOff + c], 1);
-	scratch[kUnsortedOff + slot] = i;
+// Radix pass, step 1: digit histogram of each tile, stored digit-major
+// (hist[digit * tiles + tile]) so that one exclusive scan gives every
+// (digit, tile) its output offset.  The first pass reads the keys in
+// particle order (the index is the particle itself).
+__global__ void k_na_hist(const int *keys, int *scratch, NaParams s, int shift) {
+	__shared__ int h[kRadix];
+	for (int d = threadIdx.x; d < kRadix; d += kNaThreads) h[d] = 0;
+	__syncthreads();
+	const int t = blockIdx.x;
+	for (int k = 0; k < kItems; ++k) {
+		const int i = t * kTile + k * kNaThreads + threadIdx.x;
+		if (i < s.n) atomicAdd(&h[(keys[i] >> shift) & (kRadix - 1)], 1);
+	}
+	__syncthreads();
+	for (int d = threadIdx.x; d < kRadix; d += kNaThreads) scratch[kHistOff + (size_t)d * s.tiles + t] = h[d];
 }
 
-// Each cell's array in particle order (AddParticle appends in that order,
-// demo4.cpp:37-54): rank of every member among the cell's members.
-__global__ void k_na_order(int *scratch, NaParams s) {
-	const int lane = threadIdx.x & 31;
-	const int warps = gridDim.x * (blockDim.x / 32);
-	for (int c = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; c < s.ncell; c += warps) {
-		const int st = scratch[kStartOff + c], cnt = scratch[kCountOff + c];
-		for (int a = lane; a < cnt; a += 32) {
-			const int v = scratch[kUnsortedOff + st + a];
-			int rank = 0;
-			for (int b = 0; b < cnt; ++b) rank += scratch[kUnsortedOff + st + b] < v ? 1 : 0;
-			scratch[kSortedOff + st + rank] = v;
+// Radix pass, step 2: exclusive scan of the digit-major histogram (one block).
+__global__ void k_na_hist_scan(int *scratch, NaParams s) {
+	__shared__ int sums[kNaThreads];
+	const int tid = threadIdx.x;
+	const int total = kRadix * s.tiles;
+	const int per = (total + kNaThreads - 1) / kNaThreads;
+	const int b = tid * per, e = min(total, b + per);
+	int *h = scratch + kHistOff;
+	int acc = 0;
+	for (int q = b; q < e; ++q) acc += h[q];
+	sums[tid] = acc;
+	__syncthreads();
+	for (int off = 1; off < kNaThreads; off <<= 1) {
+		const int v = tid >= off ? sums[tid - off] : 0;
+		__syncthreads();
+		sums[tid] += v;
+		__syncthreads();
+	}
+	int run = tid > 0 ? sums[tid - 1] : 0;
+	for (int q = b; q < e; ++q) {
+		const int v = h[q];
+		h[q] = run;
+		run += v;
+	}
+}
+
+// Radix pass, step 3: stable scatter.  Warp w of a tile owns the tile's
+// items [w * 8 * 32, (w + 1) * 8 * 32) in order; per-warp digit counts
+// (then their exclusive scan across the warps) give each warp its first
+// position per digit, and within a warp the items are placed round by round
+// in lane order, equal digits ranked by __match_any_sync.  Input position q
+// holds (inIdx[q], keys[q]); inIdx == nullptr means the identity (the first
+// pass, over particle order).
+__global__ void k_na_scatter(const int *keys, const int *inIdx, int *outKeys, int *outIdx, int *scratch, NaParams s,
+                             int shift) {
+	constexpr int kW = kNaThreads / 32;
+	constexpr int kPerWarp = kTile / kW;  // 256 items per warp
+	__shared__ int cnt[kW][kRadix];
+	const int lane = threadIdx.x & 31, w = threadIdx.x / 32;
+	const int t = blockIdx.x;
+	for (int d = lane; d < kRadix; d += 32) cnt[w][d] = 0;
+	__syncwarp();
+	const int base = t * kTile + w * kPerWarp;
+	// Per-warp digit counts.
+	for (int r = 0; r < kPerWarp / 32; ++r) {
+		const int q = base + r * 32 + lane;
+		const bool in = q < s.n;
+		const int d = in ? (keys[q] >> shift) & (kRadix - 1) : -1;
+		const unsigned peers = __match_any_sync(0xffffffffu, d);
+		if (in && lane == __ffs(peers) - 1) cnt[w][d] += __popc(peers);
+	}
+	__syncthreads();
+	// Exclusive scan over the warps per digit, plus the tile's global offset.
+	for (int d = threadIdx.x; d < kRadix; d += kNaThreads) {
+		int run = scratch[kHistOff + (size_t)d * s.tiles + t];
+		for (int q = 0; q < kW; ++q) {
+			const int v = cnt[q][d];
+			cnt[q][d] = run;
+			run += v;
+		}
+	}
+	__syncthreads();
+	for (int r = 0; r < kPerWarp / 32; ++r) {
+		const int q = base + r * 32 + lane;
+		const bool in = q < s.n;
+		const int key = in ? keys[q] : 0;
+		const int d = in ? (key >> shift) & (kRadix - 1) : -1;
+		const unsigned peers = __match_any_sync(0xffffffffu, d);
+		const unsigned lt = peers & ((1u << lane) - 1u);
+		const int leader = __ffs(peers) - 1;
+		int at = 0;
+		if (in) at = cnt[w][d] + __popc(lt);
+		__syncwarp();
+		if (in && lane == leader) cnt[w][d] += __popc(peers);
+		__syncwarp();
+		if (in) {
+			outKeys[at] = key;
+			outIdx[at] = inIdx ? inIdx[q] : q;
 		}
 	}
 }
 
-// One warp per cell; each lane sums one particle's list in order.
-__global__ void k_na_density(const float2 *pos, float2 *dens, float2 *press, const int *scratch, NaParams s) {
+// One warp per cell; each lane sums one particle's list in order.  Blocks
+// whose list exceeds the domain's neighbour capacity, and cells beyond its
+// cell capacity, are flagged and skipped.
+__global__ void k_na_density(const float2 *pos, float2 *dens, float2 *press, int *scratch, NaParams s) {
 	const int lane = threadIdx.x & 31;
 	const int warps = gridDim.x * (blockDim.x / 32);
+	const int *sorted = scratch + kIdxAOff;
 	for (int c = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; c < s.ncell; c += warps) {
 		const int cnt = scratch[kCountOff + c];
 		if (cnt == 0) continue;
 		const int cx = c % s.gx, cy = c / s.gx;
+		int L = 0;
+		for (int q = 0; q < 9; ++q) {
+			const int x = cx + q % 3 - 1, y = cy + q / 3 - 1;
+			if (x >= 0 && x < s.gx && y >= 0 && y < s.gy) L += scratch[kCountOff + y * s.gx + x];
+		}
+		if (cnt > s.maxCell || L > s.maxNeighbors) {
+			if (lane == 0) atomicOr(&scratch[kStatusOff], kStatusCapacity);
+			continue;
+		}
 		const int st = scratch[kStartOff + c];
 		for (int g = 0; g < cnt; g += 32) {
 			const bool active = g + lane < cnt;
-			const int i = active ? scratch[kSortedOff + st + g + lane] : 0;
+			const int i = active ? sorted[st + g + lane] : 0;
 			const float2 xi = pos[i];
 			float d0 = 0.0f, d1 = 0.0f;
 			for (int q = 0; q < 9; ++q) {
@@ -124,7 +247,7 @@ __global__ void k_na_density(const float2 *pos, float2 *dens, float2 *press, con
 				const int c2 = y * s.gx + x;
 				const int st2 = scratch[kStartOff + c2], cnt2 = scratch[kCountOff + c2];
 				for (int j = 0; j < cnt2; ++j) {
-					const float2 xj = pos[scratch[kSortedOff + st2 + j]];
+					const float2 xj = pos[sorted[st2 + j]];
 					const float rx = xj.x - xi.x, ry = xj.y - xi.y;
 					const float r2 = rx * rx + ry * ry;
 					if (r2 < s.h2) {
@@ -143,7 +266,9 @@ __global__ void k_na_density(const float2 *pos, float2 *dens, float2 *press, con
 	}
 }
 
-// Device address of the scratch array, looked up once per device.
+// Device address of the scratch array, looked up once per device on the
+// first call made with that device current, and kept for the life of the
+// process.
 std::mutex g_mutex;
 int *g_ptr[kNaMaxDevices] = {};
 
@@ -174,6 +299,8 @@ extern "C" int sph_density_pressure_noalloc(const sph_domain *domain, const sph_
 	if (s.gx <= 0 || s.gy <= 0) return SPH_ERR_INVALID_ARGUMENT;
 	if (count > (size_t)SPH_NOALLOC_MAX_PARTICLES) return SPH_ERR_CAPACITY;
 	if ((int64_t)s.gx * s.gy > (int64_t)SPH_NOALLOC_MAX_CELLS) return SPH_ERR_CAPACITY;
+	if (domain->max_neighbors > (uint32_t)SPH_NOALLOC_MAX_NEIGHBORS) return SPH_ERR_CAPACITY;
+	if (count > (size_t)domain->max_particles) return SPH_ERR_CAPACITY;
 	if (count == 0) return SPH_OK;
 	s.ncell = s.gx * s.gy;
 	s.halfW = domain->width * 0.5f;
@@ -184,23 +311,42 @@ extern "C" int sph_density_pressure_noalloc(const sph_domain *domain, const sph_
 	s.rho0 = params->rest_density;
 	s.k = params->stiffness;
 	s.kNear = params->near_stiffness;
+	s.maxCell = (int)domain->max_cell_particles;
+	s.maxNeighbors = (int)domain->max_neighbors;
+	s.n = (int)count;
+	s.tiles = (s.n + kTile - 1) / kTile;
 	int *scratch = nullptr;
 	int rc = scratch_for_current_device(&scratch);
 	if (rc != SPH_OK) return rc;
 	cudaStream_t st = static_cast<cudaStream_t>(stream);
-	const int n = (int)count;
 	const float2 *p = reinterpret_cast<const float2 *>(pos);
-	// Counts and cursors must start at zero; the rest is fully rewritten.
+	// The array keeps the previous call's contents: the counts and the status
+	// word start at zero; everything else is fully rewritten before it is read.
 	if (cudaMemsetAsync(scratch + kCountOff, 0, sizeof(int) * s.ncell, st) != cudaSuccess ||
-	    cudaMemsetAsync(scratch + kCursorOff, 0, sizeof(int) * s.ncell, st) != cudaSuccess)
+	    cudaMemsetAsync(scratch + kStatusOff, 0, sizeof(int), st) != cudaSuccess)
 		return SPH_ERR_CUDA;
-	const int blocks = (n + kNaThreads - 1) / kNaThreads;
+	const int blocks = (s.n + kNaThreads - 1) / kNaThreads;
 	const int cellBlocks = (s.ncell + kNaWarps - 1) / kNaWarps;
-	k_na_count<<<blocks, kNaThreads, 0, st>>>(n, p, scratch, s);
+	k_na_keys<<<blocks, kNaThreads, 0, st>>>(p, scratch, s);
 	k_na_scan<<<1, kNaThreads, 0, st>>>(scratch, s);
-	k_na_scatter<<<blocks, kNaThreads, 0, st>>>(n, p, scratch, s);
-	k_na_order<<<cellBlocks, kNaWarps * 32, 0, st>>>(scratch, s);
+	// Pass 1 (low digit) from particle order into B; pass 2 (high digit) from
+	// B into A: A then lists each cell's members in particle order.
+	k_na_hist<<<s.tiles, kNaThreads, 0, st>>>(scratch + kKeyOff, scratch, s, 0);
+	k_na_hist_scan<<<1, kNaThreads, 0, st>>>(scratch, s);
+	k_na_scatter<<<s.tiles, kNaThreads, 0, st>>>(scratch + kKeyOff, nullptr, scratch + kKeyBOff, scratch + kIdxBOff,
+	                                             scratch, s, 0);
+	k_na_hist<<<s.tiles, kNaThreads, 0, st>>>(scratch + kKeyBOff, scratch, s, kRadixBits);
+	k_na_hist_scan<<<1, kNaThreads, 0, st>>>(scratch, s);
+	k_na_scatter<<<s.tiles, kNaThreads, 0, st>>>(scratch + kKeyBOff, scratch + kIdxBOff, scratch + kKeyOff,
+	                                             scratch + kIdxAOff, scratch, s, kRadixBits);
 	k_na_density<<<cellBlocks, kNaWarps * 32, 0, st>>>(p, reinterpret_cast<float2 *>(dens),
 	                                                    reinterpret_cast<float2 *>(press), scratch, s);
-	return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+	if (cudaGetLastError() != cudaSuccess) return SPH_ERR_CUDA;
+	// The capacity verdict needs the device's status word: wait for this
+	// call's work (a copy into a host variable; nothing is allocated).
+	int status = 0;
+	if (cudaMemcpyAsync(&status, scratch + kStatusOff, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+	    cudaStreamSynchronize(st) != cudaSuccess)
+		return SPH_ERR_CUDA;
+	return (status & kStatusCapacity) ? SPH_ERR_CAPACITY : SPH_OK;
 }

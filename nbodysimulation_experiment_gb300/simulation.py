@@ -229,6 +229,8 @@ def load_library(build_if_missing: bool = True):
         "sph_synchronize": [vp],
         "sph_kernel_launches": [vp, P(_c.c_uint64)],
         "sph_use_graphs": [vp, _c.c_int],
+        "sph_set_reference_order": [vp, _c.c_int],
+        "sph_get_reference_order": [vp, P(_c.c_int)],
         "sph_set_wait_limit": [vp, _c.c_double],
         "sph_test_hold_task": [vp, _c.c_int, _c.c_int],
         "sph_autotune": [vp, _c.c_float, vp],
@@ -284,7 +286,8 @@ C_SYMBOLS = (
     "sph_get_stream", "sph_device_arrays", "sph_particle_colors", "sph_render_points", "sph_scenario_count",
     "sph_scenario_describe", "sph_load_scenario", "sph_synchronize",
     "sph_kernel_launches",
-    "sph_use_graphs", "sph_autotune", "sph_set_wait_limit", "sph_test_hold_task", "sph_get_sweep_shape", "sph_set_sweep_shape", "sph_set_springs", "sph_get_spring_count", "sph_dump_springs", "sph_load_springs",
+    "sph_use_graphs", "sph_autotune", "sph_set_reference_order", "sph_get_reference_order",
+    "sph_set_wait_limit", "sph_test_hold_task", "sph_get_sweep_shape", "sph_set_sweep_shape", "sph_set_springs", "sph_get_spring_count", "sph_dump_springs", "sph_load_springs",
     "sph_mpnn_create", "sph_mpnn_destroy", "sph_mpnn_param_count", "sph_mpnn_get_params", "sph_mpnn_set_params",
     "sph_mpnn_capture", "sph_mpnn_sample_count", "sph_mpnn_clear_samples", "sph_mpnn_sample_info",
     "sph_mpnn_read_sample", "sph_mpnn_eval", "sph_mpnn_gradient", "sph_mpnn_train_step", "sph_learned_frame",
@@ -564,6 +567,17 @@ class Simulation:
     def use_graphs(self, enable: bool = True):
         """Replay repeated updates from a per-step CUDA graph (default on)."""
         self._call("sph_use_graphs", 1 if enable else 0)
+
+    def set_reference_order(self, enable: bool = True) -> None:
+        """Visit particles in AddParticle order in both ordered passes and the
+        grid update, as the reference's own Update does, so that free runs
+        reproduce the reference's trajectory (see sph_set_reference_order)."""
+        self._call("sph_set_reference_order", 1 if enable else 0)
+
+    def reference_order(self) -> bool:
+        out = _c.c_int()
+        self._call("sph_get_reference_order", _c.byref(out))
+        return bool(out.value)
 
     def set_wait_limit(self, seconds: float) -> None:
         """Device-side waits of the ordered sweeps give up after ``seconds``
