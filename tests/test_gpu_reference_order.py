@@ -174,9 +174,14 @@ def test_reference_order_with_springs_free_run():
 
 
 def test_default_order_free_run_difference_is_reported():
-    """The default order equals the reference on update 1 and then drifts by
-    rounding; the size of the drift against the reference's own updates 2
-    and 10 is printed (INTEGRATION.md quotes it)."""
+    """The default order equals the reference on update 1 (every particle is
+    then visited in AddParticle order); from update 2 on it visits the
+    particles in its cell-colour numbering, a different Gauss-Seidel order of
+    the same passes, so its trajectory departs from the reference's own.  The
+    size of that departure against the reference's updates 2 and 10 is
+    printed; measured on GB300: after update 2 the median position differs
+    by 0.031 h and the largest by 0.27 h, after update 10 by 0.28 h and 2.4 h
+    (the dam break is chaotic)."""
     g = np.load(os.path.join(GOLDEN, "dam_break_4096.npz"))
     scene = scenes.dam_break_4096()
     sim = pkg.Simulation(scene.domain())
@@ -194,5 +199,5 @@ def test_default_order_free_run_difference_is_reported():
                             "pos_ulp": ostate.ulp_diff(got["pos"], g["step%d_pos" % step])}
     print("default order vs the reference's own trajectory:", report)
     assert report[1]["pos_ulp"] == 0
-    assert report[2]["pos_max_over_h"] < 1e-3
+    assert 0.0 < report[2]["pos_median_over_h"] < 0.2 and report[2]["pos_max_over_h"] < 1.0
     sim.close()
