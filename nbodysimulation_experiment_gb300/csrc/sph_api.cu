@@ -150,6 +150,7 @@ struct sph_sim {
 	float emitterMs = 0.0f;
 	uint64_t launches = 0;
 	unsigned long long *prof = nullptr;
+	int *check = nullptr;  // verdicts of device-side input checks
 
 	size_t totalParticles() const {
 		size_t t = 0;
@@ -701,7 +702,7 @@ int allocate(sph_sim *s) {
 	if ((rc = dalloc(&s->doneD, s->doneDCap)) || (rc = dalloc(&T.appScene, appCap)) ||
 	    (rc = dalloc(&T.appRun, appCap)) || (rc = dalloc(&T.appBox, 4 * appCap)) ||
 	    (rc = dalloc(&s->doneV, std::max(C, appCap))) || (rc = dalloc(&T.refOrd, N)) ||
-	    (rc = dalloc(&T.viscBox, 4 * appCap)))
+	    (rc = dalloc(&T.viscBox, 4 * appCap)) || (rc = dalloc(&s->check, 4)))
 		return rc;
 	T.moverList = nullptr;
 	T.waitLimitNs = kDefaultWaitLimitNs;
@@ -1253,7 +1254,7 @@ int sph_destroy(sph_sim *s) {
 	                s->snap.pos,   s->snap.prev,  s->snap.vel,   s->snap.acc,   s->snap.dens,  s->snap.press,
 	                s->snap.id,    s->snap.cellOf, s->snapCellStart, s->snapCellCount, s->lz0, s->lu,
 	                s->lbyId,      s->ldens,      s->lerr,       s->lstats,     s->colorBuf,   s->imgKeys,
-	                s->imgRgba};
+	                s->imgRgba,    T.refOrd,      T.viscBox,     s->check};
 	for (void *p : ptrs)
 		if (p) cudaFree(p);
 	if (s->hostPos) cudaFreeHost(s->hostPos);
@@ -1618,46 +1619,51 @@ int sph_load_state(sph_sim *s, const sph_state_view *v) {
 		return SPH_ERR_INVALID_ARGUMENT;
 	if (v->count > sc.cap || v->canonical_count > v->count) return SPH_ERR_INVALID_ARGUMENT;
 	if (v->grid_x != sc.gx || v->grid_y != sc.gy) return SPH_ERR_INVALID_ARGUMENT;
+	SPH_CUDA(cudaSetDevice(s->device));
 	const size_t n = v->count;
-	// Validate the cell tables so that no kernel can index out of range.
-	size_t total = 0;
-	for (int c = 0; c < sc.ncell; ++c) {
-		if (v->cell_count[c] < 0 || v->cell_start[c] < 0) return SPH_ERR_INVALID_ARGUMENT;
-		if ((size_t)v->cell_start[c] + (size_t)v->cell_count[c] > v->canonical_count) return SPH_ERR_INVALID_ARGUMENT;
-		total += (size_t)v->cell_count[c];
-	}
-	if (total != v->canonical_count) return SPH_ERR_INVALID_ARGUMENT;
-	std::vector<int> app(sc.ncell, 0);
-	for (size_t k = 0; k < n; ++k) {
-		if (v->cell[k] < 0 || v->cell[k] >= sc.ncell) return SPH_ERR_INVALID_ARGUMENT;
-		if (k >= v->canonical_count) app[v->cell[k]]++;
-	}
-	for (size_t k = 0; k < v->canonical_count; ++k) {
-		const int c = v->cell[k];
-		if ((int)k < v->cell_start[c] || (int)k >= v->cell_start[c] + v->cell_count[c])
-			return SPH_ERR_INVALID_ARGUMENT;
-	}
-	sc.pendPos.clear();
-	sc.pendForce.clear();
-	BufferSet &A = s->buf[s->cur];
+	// The state goes into the back buffer set and the back cell tables (free
+	// between updates) and is checked there on the device; only a valid
+	// state becomes current, so an invalid one leaves the simulation as it
+	// was.  With pinned host arrays the copies run at full link speed and
+	// the host does no per-particle work.
+	BufferSet &B = s->buf[1 - s->cur];
 	cudaStream_t st = s->stream;
 	auto h2d = [&](void *dst, const void *src, size_t bytes) -> int {
 		if (bytes == 0) return SPH_OK;
 		return cuda_status(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
 	};
 	int rc;
-	if ((rc = h2d(A.pos, v->pos, n * 8)) || (rc = h2d(A.prev, v->prev, n * 8)) || (rc = h2d(A.vel, v->vel, n * 8)) ||
-	    (rc = h2d(A.acc, v->acc, n * 8)) || (rc = h2d(A.dens, v->dens, n * 8)) ||
-	    (rc = h2d(A.press, v->press, n * 8)) || (rc = h2d(A.id, v->id, n * 4)) ||
-	    (rc = h2d(A.cellOf, v->cell, n * 4)) || (rc = h2d(s->cellStartA, v->cell_start, sc.ncell * 4)) ||
-	    (rc = h2d(s->cellCountA, v->cell_count, sc.ncell * 4)))
+	if ((rc = h2d(B.pos, v->pos, n * 8)) || (rc = h2d(B.prev, v->prev, n * 8)) || (rc = h2d(B.vel, v->vel, n * 8)) ||
+	    (rc = h2d(B.acc, v->acc, n * 8)) || (rc = h2d(B.dens, v->dens, n * 8)) ||
+	    (rc = h2d(B.press, v->press, n * 8)) || (rc = h2d(B.id, v->id, n * 4)) ||
+	    (rc = h2d(B.cellOf, v->cell, n * 4)) || (rc = h2d(s->cellStartB, v->cell_start, sc.ncell * 4)) ||
+	    (rc = h2d(s->cellCountB, v->cell_count, sc.ncell * 4)))
 		return rc;
-	SPH_CUDA(cudaMemcpyAsync(s->T.appCount, app.data(), sc.ncell * 4, cudaMemcpyHostToDevice, st));
-	if (A.springN && n) SPH_CUDA(cudaMemsetAsync(A.springN, 0, n * sizeof(int), st));  // sph_load_springs sets them
-	SPH_CUDA(cudaStreamSynchronize(st));  // `app` is a host temporary
+	// Per-step scratch, free between updates: enterCount counts the added
+	// particles per cell, newLabel marks the AddParticle indices seen.
+	SPH_CUDA(cudaMemsetAsync(s->T.enterCount, 0, sc.ncell * sizeof(int), st));
+	SPH_CUDA(cudaMemsetAsync(s->T.newLabel, 0, std::max<size_t>(n, 1) * sizeof(int), st));
+	SPH_CUDA(cudaMemsetAsync(s->check, 0, 2 * sizeof(int), st));
+	const size_t items = std::max(n, (size_t)sc.ncell);
+	k_check_state<<<blocks_for(items, kElemThreads), kElemThreads, 0, st>>>(
+	    (int)n, (int)v->canonical_count, sc.ncell, B.cellOf, s->cellStartB, s->cellCountB, B.id, s->T.enterCount,
+	    s->T.newLabel, s->check);
+	SPH_LAUNCHED(s);
+	int verdict[2] = {0, 0};
+	SPH_CUDA(cudaMemcpyAsync(verdict, s->check, sizeof(verdict), cudaMemcpyDeviceToHost, st));
+	SPH_CUDA(cudaStreamSynchronize(st));
+	if (verdict[0] != 0 || (size_t)verdict[1] != v->canonical_count) return SPH_ERR_INVALID_ARGUMENT;
+	SPH_CUDA(cudaMemcpyAsync(s->T.appCount, s->T.enterCount, sc.ncell * 4, cudaMemcpyDeviceToDevice, st));
+	if (B.springN && n) SPH_CUDA(cudaMemsetAsync(B.springN, 0, n * sizeof(int), st));  // sph_load_springs sets them
+	s->cur = 1 - s->cur;
+	std::swap(s->cellStartA, s->cellStartB);
+	std::swap(s->cellCountA, s->cellCountB);
+	sc.pendPos.clear();
+	sc.pendForce.clear();
 	sc.n = sc.nDev = n;
 	sc.n0 = v->canonical_count;
 	s->sceneTableDirty = true;
+	drop_graphs(s);
 	return SPH_OK;
 }
 
@@ -1763,24 +1769,30 @@ int sph_dump_springs(sph_sim *s, size_t count, int32_t *spring_count, int32_t *p
 	if (rc) return rc;
 	if (count != sc->n) return SPH_ERR_INVALID_ARGUMENT;
 	const BufferSet &A = s->buf[s->cur];
-	std::vector<int32_t> cnt(count), part(count * kSprings);
-	std::vector<float> len(count * kSprings);
-	if (A.springN && count) {
-		SPH_CUDA(cudaMemcpyAsync(cnt.data(), A.springN, count * 4, cudaMemcpyDeviceToHost, s->stream));
-		SPH_CUDA(cudaMemcpyAsync(part.data(), A.springP, count * kSprings * 4, cudaMemcpyDeviceToHost, s->stream));
-		SPH_CUDA(cudaMemcpyAsync(len.data(), A.springL, count * kSprings * 4, cudaMemcpyDeviceToHost, s->stream));
-	}
-	rc = check_device_errors(s);
-	if (rc) return rc;
-	for (size_t i = 0; i < count; ++i) {
-		const int c = std::min(std::max(cnt[i], 0), kSprings);
-		if (spring_count) spring_count[i] = c;
-		for (int q = 0; q < kSprings; ++q) {
-			if (partner) partner[i * kSprings + q] = q < c ? part[i * kSprings + q] : -1;
-			if (rest) rest[i * kSprings + q] = q < c ? len[i * kSprings + q] : 0.0f;
+	const BufferSet &B = s->buf[1 - s->cur];  // free between updates: the cleaned copy
+	cudaStream_t st = s->stream;
+	if (!A.springN) {
+		// Springs were never enabled: no particle has one.
+		for (size_t i = 0; i < count; ++i) {
+			if (spring_count) spring_count[i] = 0;
+			for (int q = 0; q < kSprings; ++q) {
+				if (partner) partner[i * kSprings + q] = -1;
+				if (rest) rest[i * kSprings + q] = 0.0f;
+			}
 		}
+		return check_device_errors(s);
 	}
-	return SPH_OK;
+	if (count) {
+		k_clean_springs<<<blocks_for(count * kSprings, kElemThreads), kElemThreads, 0, st>>>(
+		    (int)count, A.springN, A.springP, A.springL, B.springN, B.springP, B.springL);
+		SPH_LAUNCHED(s);
+		if (spring_count)
+			SPH_CUDA(cudaMemcpyAsync(spring_count, B.springN, count * 4, cudaMemcpyDeviceToHost, st));
+		if (partner)
+			SPH_CUDA(cudaMemcpyAsync(partner, B.springP, count * kSprings * 4, cudaMemcpyDeviceToHost, st));
+		if (rest) SPH_CUDA(cudaMemcpyAsync(rest, B.springL, count * kSprings * 4, cudaMemcpyDeviceToHost, st));
+	}
+	return check_device_errors(s);
 }
 
 int sph_load_springs(sph_sim *s, size_t count, const int32_t *spring_count, const int32_t *partner,
@@ -1788,24 +1800,32 @@ int sph_load_springs(sph_sim *s, size_t count, const int32_t *spring_count, cons
 	Scene *sc = single(s);
 	if (!sc) return not_single(s);
 	if (!spring_count || !partner || !rest) return SPH_ERR_INVALID_ARGUMENT;
-	BufferSet &A = s->buf[s->cur];
-	if (!A.springN) return SPH_ERR_NOT_SUPPORTED;  // springs were never enabled
+	if (!s->buf[0].springN) return SPH_ERR_NOT_SUPPORTED;  // springs were never enabled
 	int rc = flush_adds(s);
 	if (rc) return rc;
 	if (count != sc->n) return SPH_ERR_INVALID_ARGUMENT;
-	for (size_t i = 0; i < count; ++i) {
-		if (spring_count[i] < 0 || spring_count[i] > kSprings) return SPH_ERR_INVALID_ARGUMENT;
-		for (int q = 0; q < spring_count[i]; ++q) {
-			const int32_t p = partner[i * kSprings + q];
-			if (p < 0 || (size_t)p >= count || (size_t)p == i) return SPH_ERR_INVALID_ARGUMENT;
-		}
-	}
+	// Into the back buffer set's spring tables, checked on the device, then
+	// swapped in: invalid tables leave the current springs as they were.
+	BufferSet &A = s->buf[s->cur];
+	BufferSet &B = s->buf[1 - s->cur];
+	cudaStream_t st = s->stream;
 	if (count) {
-		SPH_CUDA(cudaMemcpyAsync(A.springN, spring_count, count * 4, cudaMemcpyHostToDevice, s->stream));
-		SPH_CUDA(cudaMemcpyAsync(A.springP, partner, count * kSprings * 4, cudaMemcpyHostToDevice, s->stream));
-		SPH_CUDA(cudaMemcpyAsync(A.springL, rest, count * kSprings * 4, cudaMemcpyHostToDevice, s->stream));
+		SPH_CUDA(cudaMemcpyAsync(B.springN, spring_count, count * 4, cudaMemcpyHostToDevice, st));
+		SPH_CUDA(cudaMemcpyAsync(B.springP, partner, count * kSprings * 4, cudaMemcpyHostToDevice, st));
+		SPH_CUDA(cudaMemcpyAsync(B.springL, rest, count * kSprings * 4, cudaMemcpyHostToDevice, st));
+		SPH_CUDA(cudaMemsetAsync(s->check, 0, sizeof(int), st));
+		k_check_springs<<<blocks_for(count, kElemThreads), kElemThreads, 0, st>>>((int)count, B.springN, B.springP,
+		                                                                          s->check);
+		SPH_LAUNCHED(s);
 	}
-	SPH_CUDA(cudaStreamSynchronize(s->stream));
+	int bad = 0;
+	if (count) SPH_CUDA(cudaMemcpyAsync(&bad, s->check, sizeof(int), cudaMemcpyDeviceToHost, st));
+	SPH_CUDA(cudaStreamSynchronize(st));
+	if (bad) return SPH_ERR_INVALID_ARGUMENT;
+	std::swap(A.springN, B.springN);
+	std::swap(A.springP, B.springP);
+	std::swap(A.springL, B.springL);
+	drop_graphs(s);  // graphs hold the spring tables' addresses
 	return SPH_OK;
 }
 

@@ -2377,6 +2377,39 @@ __global__ void k_add(int first, int count, int scene, int firstId, const float2
 	atomicMax(&T.stats[4 * scene + 3], now);
 }
 
+// Checks of a state given to sph_load_state, on the device (one thread per
+// particle and per cell): every cell range lies within the canonical
+// particles, every particle's cell and AddParticle index are in range, and
+// every canonical particle lies in its cell's range, and no two particles
+// share an AddParticle index (seen[] starts at zero).  Particles added since
+// the last update (numbers >= n0) are counted per cell into appOut.
+// verdict[0] collects failures, verdict[1] the sum of the cell counts.
+__global__ void k_check_state(int n, int n0, int ncell, const int *cell, const int *start, const int *count,
+                              const int *id, int *appOut, int *seen, int *verdict) {
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	int bad = 0;
+	if (i < ncell) {
+		const int st = start[i], cn = count[i];
+		bad |= st < 0 || cn < 0 || (long long)st + cn > n0;
+		if (!bad && cn) atomicAdd(&verdict[1], cn);
+	}
+	if (i < n) {
+		const int c = cell[i];
+		const int k = id[i];
+		bad |= c < 0 || c >= ncell || k < 0 || k >= n;
+		if (!bad) bad |= atomicAdd(&seen[k], 1) != 0;  // AddParticle indices are distinct
+		if (!bad) {
+			if (i >= n0) {
+				atomicAdd(&appOut[c], 1);
+			} else {
+				const int st = start[c], cn = count[c];
+				bad |= i < st || i >= st + cn;
+			}
+		}
+	}
+	if (bad) atomicOr(&verdict[0], 1);
+}
+
 // Scatter numbers [first, first+count) into AddParticle order for host reads.
 __global__ void k_gather_by_id(int first, int count, const int *id, const float2 *src, float2 *dst) {
 	const int j = blockIdx.x * blockDim.x + threadIdx.x;

@@ -86,6 +86,11 @@ __global__ void k_collide(Totals tt, Particles P, Particles Q, SimTables T);
 __global__ void k_add(int first, int count, int scene, int firstId, const float2 *pos, const float2 *force,
                       Particles P, SimTables T);
 __global__ void k_gather_by_id(int first, int count, const int *id, const float2 *src, float2 *dst);
+__global__ void k_check_state(int n, int n0, int ncell, const int *cell, const int *start, const int *count,
+                              const int *id, int *appOut, int *seen, int *verdict);
+__global__ void k_check_springs(int n, const int *cnt, const int *partner, int *verdict);
+__global__ void k_clean_springs(int n, const int *cnt, const int *partner, const float *rest, int *cntOut,
+                                int *partnerOut, float *restOut);
 __global__ void k_particle_colors(int first, int count, const int *id, const float2 *dens, const float2 *press,
                                   const float2 *vel, float rho0, float4 *out);
 __global__ void k_splat_points(int first, int count, const int *id, const float2 *pos, const float2 *dens,

@@ -66,18 +66,22 @@ __device__ __forceinline__ int staged_index(int num, const int (&off)[9], const 
 
 // One warp per new cell: the 3x3 block of new cells (positions, numbers'
 // AddParticle indices) is staged once; each lane handles one particle of the
-// cell.  The candidate scan runs over the block in the same order for every
-// lane, so the warp stays converged apart from the insertions.
+// cell's existing springs.  Candidates are then chosen either by the whole
+// warp for one particle at a time (when at most kSpringWarpChoice of the 32
+// particles have free slots) or by every lane for its own particle with a
+// converged scan over the block.
+constexpr int kSpringWarpChoice = 16;
 struct SpringWarp {
 	float2 pos[kStageCap];
 	int tag[kStageCap];
 	// Per-lane lists, slot-major ([slot][lane]) so that the lanes' accesses
 	// fall on distinct banks.
 	int ex[kSprings][kWarp];     // existing partners (new numbers)
-	float kr2[kSprings][kWarp];  // chosen candidates, sorted
+	float kr2[kSprings][kWarp];  // chosen candidates, sorted (per-lane scan)
 	int ktag[kSprings][kWarp];
 	int kj[kSprings][kWarp];
 	uint32_t exbits[kStageCap / 32][kWarp];  // per lane: staged entries that are existing partners
+	unsigned long long key[kStageCap];  // one particle's candidate keys (warp-wide choice)
 };
 
 size_t springs_smem_bytes() { return sizeof(SpringWarp) * kSpringWarps; }
@@ -155,9 +159,56 @@ __global__ void __launch_bounds__(kSpringWarps * kWarp) k_springs_select(Totals 
 				}
 				freeSlots = s.springMax - m;
 			}
-			// Candidates: every list member in range without a spring (the
-			// warp skips the scan when no lane has a free slot).
-			const bool scan = active && freeSlots > 0;
+			// Candidates: every list member in range without a spring,
+			// nearest first, then the smaller AddParticle index.  Few
+			// particles with free slots (the steady state: most hold all
+			// their springs): each chooses with the whole warp, by rounds of
+			// a warp-wide minimum over 64-bit keys (r^2 bits, index) -- keys
+			// of distinct entries differ, and a non-negative float's bits
+			// order like its value.  Many (the first updates): every lane
+			// scans the list for its own particle with an ordered insertion.
+			// Both give the same choices in the same order.
+			const unsigned needy = __ballot_sync(kFullMask, active && freeSlots > 0);
+			const bool perLane = __popc(needy) > kSpringWarpChoice;
+			__syncwarp();  // every lane's existing-partner bits are in place
+			for (unsigned todo = perLane ? 0u : needy; todo != 0u; todo &= todo - 1u) {
+				const int lp = __ffs(todo) - 1;
+				const int fs = __shfl_sync(kFullMask, freeSlots, lp);
+				const float px = __shfl_sync(kFullMask, xi.x, lp), py = __shfl_sync(kFullMask, xi.y, lp);
+				const int selfE = segOff[4] + g + lp;  // the particle's own entry (own cell = segment 4)
+				for (int e = lane; e < L; e += kWarp) {
+					const float2 xj = S.pos[e];
+					const float rx = xj.x - px, ry = xj.y - py;
+					const float r2 = rx * rx + ry * ry;
+					const bool ok = r2 < s.h2 && e != selfE && !((S.exbits[e >> 5][lp] >> (e & 31)) & 1u);
+					S.key[e] = ok ? ((unsigned long long)__float_as_uint(r2) << 32) | (unsigned)S.tag[e] : ~0ull;
+				}
+				__syncwarp();
+				unsigned long long last = 0ull;
+				int chosen = 0;
+				for (; chosen < fs; ++chosen) {
+					unsigned long long best = ~0ull;
+					int bestE = -1;
+					for (int e = lane; e < L; e += kWarp) {
+						const unsigned long long k = S.key[e];
+						if (k < best && (chosen == 0 || k > last)) {
+							best = k;
+							bestE = e;
+						}
+					}
+					const unsigned hi = __reduce_min_sync(kFullMask, (unsigned)(best >> 32));
+					const unsigned lo = __reduce_min_sync(kFullMask, (unsigned)(best >> 32) == hi ? (unsigned)best : ~0u);
+					const unsigned long long mk = ((unsigned long long)hi << 32) | lo;
+					if (mk == ~0ull) break;
+					const int wl = __ffs(__ballot_sync(kFullMask, best == mk)) - 1;
+					const int we = __shfl_sync(kFullMask, bestE, wl);
+					last = mk;
+					if (lane == 0) T.accP[(st + g + lp) * kSprings + chosen] = seg_number<9>(we, segOff, segStart);
+				}
+				if (lane == lp) kc = chosen;
+				__syncwarp();
+			}
+			const bool scan = perLane && active && freeSlots > 0;
 			const int scanLen = __any_sync(kFullMask, scan) ? L : 0;
 			for (int e = 0; e < scanLen; ++e) {
 				const int num = seg_number<9>(e, segOff, segStart);
@@ -182,7 +233,8 @@ __global__ void __launch_bounds__(kSpringWarps * kWarp) k_springs_select(Totals 
 			}
 			if (active) {
 				T.accN[j] = kc;
-				for (int q = 0; q < kc; ++q) T.accP[j * kSprings + q] = S.kj[q][lane];
+				if (perLane)
+					for (int q = 0; q < kc; ++q) T.accP[j * kSprings + q] = S.kj[q][lane];
 				Q.springN[j] = m;
 				for (int q = 0; q < ne; ++q) {
 					const int e = S.ex[q][lane];
@@ -259,6 +311,34 @@ __global__ void k_springs_apply(Totals tt, Particles Q, SimTables T) {
 		dy = dy - (f * ny) * 0.5f;
 	}
 	T.springPos[j] = make_float2(dx + xi.x, dy + xi.y);
+}
+
+// Checks of spring tables given to sph_load_springs (one thread per
+// particle): counts within [0, kSprings], partners within [0, n) and not the
+// particle itself.  verdict[0] collects failures.
+__global__ void k_check_springs(int n, const int *cnt, const int *partner, int *verdict) {
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	const int c = cnt[i];
+	int bad = c < 0 || c > kSprings;
+	for (int q = 0; q < kSprings && !bad; ++q) {
+		const int p = partner[i * kSprings + q];
+		if (q < c) bad |= p < 0 || p >= n || p == i;
+	}
+	if (bad) atomicOr(&verdict[0], 1);
+}
+
+// Spring tables as sph_dump_springs reports them: slots past a particle's
+// count hold partner -1 and rest length 0.
+__global__ void k_clean_springs(int n, const int *cnt, const int *partner, const float *rest, int *cntOut,
+                                int *partnerOut, float *restOut) {
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n * kSprings) return;
+	const int j = i / kSprings, q = i - j * kSprings;
+	const int c = min(max(cnt[j], 0), kSprings);
+	if (q == 0) cntOut[j] = c;
+	partnerOut[i] = q < c ? partner[i] : -1;
+	restOut[i] = q < c ? rest[i] : 0.0f;
 }
 
 }  // namespace sphgb

@@ -198,3 +198,50 @@ def test_load_oracle_made_state():
     assert res["cells_equal"] == 1.0 and res["pos_ulp"] == 0 and res["vel_ulp"] == 0, res
     sim.close()
     orc.close()
+
+
+def test_invalid_state_and_springs_are_rejected_without_change():
+    """sph_load_state and sph_load_springs check their input on the device;
+    an invalid input returns SPH_ERR_INVALID_ARGUMENT and leaves the
+    simulation as it was."""
+    from nbodysimulation_experiment_gb300.simulation import SPH_ERR_INVALID_ARGUMENT
+    springs = dict(yield_ratio=0.1, plasticity=0.3, stiffness=0.3, max_per_particle=16)
+    scene = scenes.scaled_block(32, seed=13)
+    sim = pkg.Simulation(scene.domain())
+    scene.apply(sim)
+    sim.set_springs(True, **springs)
+    for _ in range(4):
+        sim.update(DT)
+    st, spr = sim.dump_state(), sim.dump_springs()
+    bad_cases = []
+    for key, k, value in (("cell", 5, -1), ("id", 7, st["id"][8]), ("cell_count", int(np.argmax(st["cell_count"])),
+                                                                     10 ** 6)):
+        b = {kk: (np.array(vv, copy=True) if isinstance(vv, np.ndarray) else vv) for kk, vv in st.items()}
+        b[key][k] = value
+        bad_cases.append(b)
+    moved = {kk: (np.array(vv, copy=True) if isinstance(vv, np.ndarray) else vv) for kk, vv in st.items()}
+    moved["cell"][0] = (moved["cell"][0] + 1) % len(moved["cell_count"])  # outside its cell's range
+    bad_cases.append(moved)
+    for b in bad_cases:
+        with pytest.raises(SphError) as e:
+            sim.load_state(b)
+        assert e.value.status == SPH_ERR_INVALID_ARGUMENT
+        _equal_states(sim.dump_state(), st)
+    cnt, part, rest = (np.array(a, copy=True) for a in spr)
+    i = int(np.argmax(cnt))
+    part[i, 0] = i  # a spring to itself
+    with pytest.raises(SphError) as e:
+        sim.load_springs(cnt, part, rest)
+    assert e.value.status == SPH_ERR_INVALID_ARGUMENT
+    for x, y in zip(sim.dump_springs(), spr):
+        assert np.array_equal(x, y)
+    cnt2 = np.array(spr[0], copy=True)
+    cnt2[0] = 17
+    with pytest.raises(SphError):
+        sim.load_springs(cnt2, spr[1], spr[2])
+    # A valid load still works and the run continues as the original.
+    sim.load_state(st)
+    sim.load_springs(*spr)
+    sim.update(DT)
+    sim.synchronize()
+    sim.close()
