@@ -77,11 +77,15 @@ struct SpringWarp {
 	// Per-lane lists, slot-major ([slot][lane]) so that the lanes' accesses
 	// fall on distinct banks.
 	int ex[kSprings][kWarp];     // existing partners (new numbers)
-	float kr2[kSprings][kWarp];  // chosen candidates, sorted (per-lane scan)
-	int ktag[kSprings][kWarp];
-	int kj[kSprings][kWarp];
 	uint32_t exbits[kStageCap / 32][kWarp];  // per lane: staged entries that are existing partners
-	unsigned long long key[kStageCap];  // one particle's candidate keys (warp-wide choice)
+	union {
+		struct {
+			float kr2[kSprings][kWarp];  // chosen candidates, sorted (per-lane scan)
+			int ktag[kSprings][kWarp];
+			int kj[kSprings][kWarp];
+		};
+		unsigned long long key[kStageCap];  // one particle's candidate keys (warp-wide choice)
+	};
 };
 
 size_t springs_smem_bytes() { return sizeof(SpringWarp) * kSpringWarps; }
@@ -137,22 +141,48 @@ __global__ void __launch_bounds__(kSpringWarps * kWarp) k_springs_select(Totals 
 				xi = Q.pos[j];
 				const int o = T.newIdx[j];
 				ne = P.springN[o];
-				if (ne > kSprings) {
+				if (ne > kSprings || ne < 0) {
 					atomicOr(T.error, kErrIndex);
-					ne = kSprings;
+					ne = ne < 0 ? 0 : kSprings;
 				}
-				for (int q = 0; q < ne; ++q) {
-					const int pn = T.newLabel[P.springP[o * kSprings + q]];
-					float rest = P.springL[o * kSprings + q];
-					const int e = staged_index(pn, segOff, segStart, L);
+				// The particle's spring rows, four slots per load, then the
+				// partners' new numbers, all issued before any is used.
+				int pn[kSprings];
+				float rl[kSprings];
+				const int4 *rowP = reinterpret_cast<const int4 *>(P.springP + (size_t)o * kSprings);
+				const float4 *rowL = reinterpret_cast<const float4 *>(P.springL + (size_t)o * kSprings);
+#pragma unroll
+				for (int v = 0; v < kSprings / 4; ++v) {
+					int4 a = make_int4(0, 0, 0, 0);
+					float4 b = make_float4(0.f, 0.f, 0.f, 0.f);
+					if (4 * v < ne) {
+						a = rowP[v];
+						b = rowL[v];
+					}
+					pn[4 * v] = a.x;
+					pn[4 * v + 1] = a.y;
+					pn[4 * v + 2] = a.z;
+					pn[4 * v + 3] = a.w;
+					rl[4 * v] = b.x;
+					rl[4 * v + 1] = b.y;
+					rl[4 * v + 2] = b.z;
+					rl[4 * v + 3] = b.w;
+				}
+#pragma unroll
+				for (int q = 0; q < kSprings; ++q) pn[q] = q < ne ? T.newLabel[pn[q]] : 0;
+#pragma unroll
+				for (int q = 0; q < kSprings; ++q) {
+					if (q >= ne) break;
+					float rest = rl[q];
+					const int e = staged_index(pn[q], segOff, segStart, L);
 					S.ex[q][lane] = e;
 					if (e >= 0) S.exbits[e >> 5][lane] |= 1u << (e & 31);
-					const float2 xp = Q.pos[pn];
+					const float2 xp = e >= 0 ? S.pos[e] : Q.pos[pn[q]];
 					const float rx = xp.x - xi.x, ry = xp.y - xi.y;
 					const float r2 = rx * rx + ry * ry;
 					if (r2 < s.h2) rest = plastic(rest, sqrtf(r2), s);
 					if (rest <= s.h) {
-						Q.springP[j * kSprings + m] = pn;
+						Q.springP[j * kSprings + m] = pn[q];
 						Q.springL[j * kSprings + m] = rest;
 						++m;
 					}
