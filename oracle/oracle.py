@@ -402,12 +402,22 @@ class OracleSim(_CpuSim):
     SPRING_SLOTS = 16
 
     def set_springs(self, enabled: bool, yield_ratio: float = 0.1, plasticity: float = 0.3,
-                    stiffness: float = 0.3, max_per_particle: int = 16):
+                    stiffness: float = 0.3, max_per_particle: int = 16, serial: bool = False):
+        """Springs on or off.  ``serial`` applies the spring displacements as
+        the paper's loop does (Clavet et al. 2005, Algorithm 3: one spring at
+        a time, positions updated at once, springs in order of their lower
+        end's number); otherwise every particle moves by its springs'
+        displacements from the positions before the phase (the library's
+        form)."""
         fn = self._lib.sph_oracle_set_springs
         fn.argtypes = [_vp, _i, _f, _f, _f, _i]
         fn.restype = None
         fn(self._h, 1 if enabled else 0, float(yield_ratio), float(plasticity), float(stiffness),
            int(max_per_particle))
+        fs = self._lib.sph_oracle_set_spring_serial
+        fs.argtypes = [_vp, _i]
+        fs.restype = None
+        fs(self._h, 1 if serial else 0)
 
     def set_spring_state(self, count, partner, rest, tag=None):
         """Springs per particle: count (n,), partner (n, 16) particle

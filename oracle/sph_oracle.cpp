@@ -164,6 +164,7 @@ struct SimBase {
 	virtual void SetParams(const float *p) = 0;
 	virtual void GetParams(float *p) = 0;
 	virtual size_t Count() = 0;
+	virtual void SetSpringSerial(int serial) = 0;
 	virtual void GetParticles(double *pos, double *prev, double *acc, double *vel, double *dens, double *press) = 0;
 	virtual void GetIndex(int *cellXY, uint64_t *inCell, uint64_t *nbCount) = 0;
 	virtual void GetNeighbors(size_t i, uint64_t *out) = 0;
@@ -220,6 +221,7 @@ struct Sim : SimBase {
 	// index, rest length per spring; tag = AddParticle index (tie-break).
 	static constexpr int kSprings = 16;
 	int springsOn = 0, springMax = kSprings;
+	int springSerial = 0;  // 1: displacements applied one spring at a time (Clavet 2005, Algorithm 3)
 	T springYield = 0, springPlastic = 0, springK = 0;
 	std::vector<int32_t> sN, sP, accN, accP;
 	std::vector<T> sL;
@@ -683,7 +685,8 @@ struct Sim : SimBase {
 	//     length starts at h and is adjusted like the others;
 	//  3. every particle moves by -D/2 of each of its springs, from the
 	//     positions before this phase (Jacobi), summed in slot order, with
-	//     D = dt^2 k_spring (1 - L/h) (L - r) r_hat.
+	//     D = dt^2 k_spring (1 - L/h) (L - r) r_hat -- or, with springSerial,
+	//     the paper's serial loop over the springs with immediate updates.
 	void Springs(T dt) {
 		const T h2 = h * h;
 		const T dtAlpha = dt * springPlastic;
@@ -762,6 +765,28 @@ struct Sim : SimBase {
 				nN[i] = m;
 			}
 		});
+		if (springSerial) {
+			// The paper's loop as published: foreach spring ij, D from the
+			// current positions, x_i -= D/2 and x_j += D/2 at once.  Springs
+			// in particle-number order of their lower end, then slot order.
+			for (size_t i = 0; i < n; ++i) {
+				for (int q = 0; q < nN[i]; ++q) {
+					const size_t p = (size_t)nP[i * K + q];
+					if (p <= i) continue;
+					const T L = nL[i * K + q];
+					const V2<T> rij = sub(parts[p].cur, parts[i].cur);
+					const T r = sqrt_t(dot(rij, rij));
+					const T len = r == T(0) ? T(1) : r;
+					const T inv = T(1) / len;
+					const T nx = rij.x * inv, ny = rij.y * inv;
+					const T f = ((dt2 * springK) * (T(1) - L * invH)) * (L - r);
+					const V2<T> half((f * nx) * T(0.5f), (f * ny) * T(0.5f));
+					parts[i].cur = sub(parts[i].cur, half);
+					parts[p].cur = add(parts[p].cur, half);
+				}
+			}
+			for (size_t i = 0; i < n; ++i) springPos[i] = parts[i].cur;
+		} else
 		ForEachChunk(n, [&](size_t s, size_t e) {
 			for (size_t i = s; i <= e; ++i) {
 				const V2<T> xi = parts[i].cur;
@@ -972,6 +997,7 @@ struct Sim : SimBase {
 		counts[3] = statMaxCell;
 		for (int k = 0; k < 9; ++k) t[k] = times[k];
 	}
+	void SetSpringSerial(int serial) override { springSerial = serial ? 1 : 0; }
 	void SetSprings(int enabled, float yield, float plasticity, float stiffness, int maxPer) override {
 		springYield = yield;
 		springPlastic = plasticity;
@@ -1117,6 +1143,7 @@ void sph_oracle_get_spring_state(void *p, int32_t *count, int32_t *partner, floa
 	B(p)->GetSpringState(count, partner, rest);
 }
 uint64_t sph_oracle_spring_total(void *p) { return B(p)->SpringTotal(); }
+void sph_oracle_set_spring_serial(void *p, int serial) { B(p)->SetSpringSerial(serial); }
 uint64_t sph_oracle_hardware_threads(void) {
 	unsigned t = std::thread::hardware_concurrency();
 	return t ? t : 1;

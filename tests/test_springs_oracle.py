@@ -5,8 +5,10 @@ The reference has no springs; the oracle restates Clavet et al. 2005
 ("Particle-based viscoelastic fluid simulation", Algorithms 3 and 4) in a
 deterministic parallel form: adjust and remove existing springs, add springs
 between mutually nearest free candidates, then move every particle by -D/2 of
-each of its springs from the positions before the phase.  Parity for springs
-is therefore pinned against this restatement only.
+each of its springs from the positions before the phase (the library's
+form).  It also applies the displacements in the paper's own serial form
+(Algorithm 3: one spring at a time, positions updated at once).  Both are
+pinned here against this independent restatement.
 
 Isolation: viscosity, pressure, gravity and bodies are zero, so within one
 update only prediction and the spring phase move particles, and the expected
@@ -32,8 +34,11 @@ def _plastic(L, r, dt_alpha):
     return F(L)
 
 
-def _spring_phase(x, count, partner, rest, tag, h, inv_h, dt, max_per=SLOTS):
-    """One spring phase on float32 positions x (n, 2)."""
+def _spring_phase(x, count, partner, rest, tag, h, inv_h, dt, max_per=SLOTS, serial=False):
+    """One spring phase on float32 positions x (n, 2).  ``serial`` applies
+    the displacements as Clavet et al. 2005 write the loop (Algorithm 3):
+    foreach spring ij, D from the current positions, x_i -= D/2, x_j += D/2,
+    springs in order of their lower end's number, then slot order."""
     n = len(x)
     h2 = F(h * h)
     dt_alpha = F(dt * PLASTIC)
@@ -66,6 +71,22 @@ def _spring_phase(x, count, partner, rest, tag, h, inv_h, dt, max_per=SLOTS):
                 if L <= h:
                     lst.append((p, L))
         springs.append(lst)
+    if serial:
+        out = x.copy()
+        for i in range(n):
+            for p, L in springs[i]:
+                if p <= i:
+                    continue
+                rx, ry = F(out[p, 0] - out[i, 0]), F(out[p, 1] - out[i, 1])
+                r = F(np.sqrt(F(F(rx * rx) + F(ry * ry))))
+                length = F(1) if r == 0 else r
+                inv = F(F(1) / length)
+                nx, ny = F(rx * inv), F(ry * inv)
+                f = F(F(F(dt2 * KSPRING) * F(F(1) - F(L * inv_h))) * F(L - r))
+                hx, hy = F(F(f * nx) * F(0.5)), F(F(f * ny) * F(0.5))
+                out[i] = np.array([F(out[i, 0] - hx), F(out[i, 1] - hy)], F)
+                out[p] = np.array([F(out[p, 0] + hx), F(out[p, 1] + hy)], F)
+        return out, springs
     out = x.copy()
     for i in range(n):
         dx = np.zeros(2, F)
@@ -94,11 +115,12 @@ def _quiet_scene(side=14, seed=5):
     return sc
 
 
-def test_spring_phase_matches_restatement():
+@pytest.mark.parametrize("serial", [False, True])
+def test_spring_phase_matches_restatement(serial):
     sc = _quiet_scene()
     orc = OracleSim(sc.oracle_domain(OracleSim))
     sc.apply(orc)
-    orc.set_springs(True, YIELD, PLASTIC, KSPRING, SLOTS)
+    orc.set_springs(True, YIELD, PLASTIC, KSPRING, SLOTS, serial=serial)
     dt = F(scenes.DT)
     h, inv_h = F(sc.params[0]), F(sc.params[3])
     n = sc.n
@@ -109,7 +131,7 @@ def test_spring_phase_matches_restatement():
     for step in range(4):
         before = orc.get_state(lists=False)
         x_star = (before["vel"].astype(F) * dt + before["pos"].astype(F)).astype(F)
-        want_pos, want_springs = _spring_phase(x_star, count, partner, rest, tag, h, inv_h, dt)
+        want_pos, want_springs = _spring_phase(x_star, count, partner, rest, tag, h, inv_h, dt, serial=serial)
         orc.update(float(dt))
         got = orc.get_state(lists=False)
         assert np.array_equal(got["pos"].astype(F), want_pos), step
