@@ -526,6 +526,7 @@ def bench_learned(torch, pkg, scenes, device: int, args):
 
     ms_l, used, err_l = run(True)
     ms_p, _, err_p = run(False)
+    quality = learned_quality(pkg, scene, model, device, frame, sub, args.learned_rollout_frames)
     n, nf = scene.n, args.learned_eval_frames
     model.close()
     return {"value": n / (ms_l / 1e3), "unit": "particle-frames/s",
@@ -533,13 +534,78 @@ def bench_learned(torch, pkg, scenes, device: int, args):
             "particle_steps_per_s": n * sub / (ms_l / 1e3),
             "ms_per_frame": ms_l, "plain_ms_per_frame": ms_p, "speedup_vs_plain_frame": ms_p / ms_l,
             "frames": nf, "accepted_frames": used, "density_error": err_l,
-            "density_error_plain_frame": err_p, "judge_bound": 0.01, "particles": n,
+            "density_error_plain_frame": err_p, "judge_bound": 0.01,
+            "judge": "a learned frame stands if its mean |rho - rho0| / rho0 exceeds that of the single plain "
+                     "update of the whole frame it corrects by at most judge_bound; an absolute bound of 1% "
+                     "of rho0 would reject every frame here, the plain four-update frame included "
+                     "(density_error_plain_frame)",
+            "quality": quality, "particles": n,
             "workload": "dam_break_262144: 512x512 jittered block, 102.4 x 57.6 box, 4 walls + 8 circles + "
                         "4 segments; 2-round MPNN (edge 6-128-128, node 130-128-2, BF16 tcgen05 GEMMs)",
             "train": {"samples": ntrain, "scenes": args.learned_scenes, "frames_per_scene": args.learned_frames,
                       "scene": "obstacles_65536 seeds 1000..", "steps": args.learned_steps,
                       "collect_s": t_collect, "train_s": t_train, "final_loss": float(np.mean(losses[-50:])),
                       "held_out_loss": ev["learned"], "held_out_loss_without_network": ev["without_network"]}}
+
+
+def learned_quality(pkg, scene, model, device, frame, sub, rollout_frames):
+    """Accuracy of the learned frame against the plain frame it stands in
+    for (four updates of dt/4), on the benchmark's scene: (a) per frame, from
+    the same state, the RMS and largest position difference in units of h
+    (the network's correction applied without the judge); (b) a free rollout
+    of learned frames against one of plain frames from the same start: mean
+    density deviation, kinetic energy and density histogram at the end."""
+    from nbodysimulation_experiment_gb300 import scenes as sc_mod  # noqa: F401
+    h = float(scene.params[0])
+    rho0 = float(scene.params[4])
+
+    def fresh():
+        sim = pkg.Simulation(scene.domain(), device=device)
+        scene.apply(sim)
+        for _ in range(3):
+            sim.update(frame / sub)
+        return sim
+
+    # (a) the same state advanced both ways, at several points of a run
+    sim = fresh()
+    rms, worst = [], []
+    for f in range(12):
+        st = sim.dump_state()
+        sim.learned_frame(model, frame, sub, bound=1e30)
+        a = sim.read_particles(("pos",))["pos"].astype(np.float64)
+        sim.load_state(st)
+        for _ in range(sub):
+            sim.update(frame / sub)
+        b = sim.read_particles(("pos",))["pos"].astype(np.float64)
+        d = np.sqrt(np.sum((a - b) ** 2, axis=1)) / h
+        if f % 3 == 2:
+            rms.append(float(np.sqrt(np.mean(d ** 2))))
+            worst.append(float(d.max()))
+    sim.close()
+
+    # (b) free rollouts from the same start
+    def rollout(use_network):
+        sim = fresh()
+        for _ in range(rollout_frames):
+            if use_network:
+                sim.learned_frame(model, frame, sub, bound=1e30)
+            else:
+                for _ in range(sub):
+                    sim.update(frame / sub)
+        r = sim.read_particles(("pos", "vel", "dens"))
+        sim.close()
+        d = r["dens"][:, 0].astype(np.float64)
+        hist, _ = np.histogram(d / rho0, bins=20, range=(0.0, 2.0))
+        return {"density_error": float(np.mean(np.abs(d - rho0)) / rho0),
+                "kinetic_energy": float(0.5 * np.mean(np.sum(r["vel"].astype(np.float64) ** 2, axis=1))),
+                "mean_height": float(np.mean(r["pos"][:, 1])), "hist": hist / len(d)}
+
+    lr, pr = rollout(True), rollout(False)
+    return {"per_frame_rms_position_error_h": float(np.mean(rms)), "per_frame_max_position_error_h": max(worst),
+            "rollout_frames": rollout_frames,
+            "rollout_learned": {k: v for k, v in lr.items() if k != "hist"},
+            "rollout_plain": {k: v for k, v in pr.items() if k != "hist"},
+            "rollout_density_histogram_l1": float(np.abs(lr["hist"] - pr["hist"]).sum())}
 
 
 def parse_args(argv=None):
@@ -563,6 +629,7 @@ def parse_args(argv=None):
     ap.add_argument("--learned-steps", type=int, default=1500, help="Adam steps")
     ap.add_argument("--learned-eval-frames", type=int, default=20)
     ap.add_argument("--learned-warmup", type=int, default=3)
+    ap.add_argument("--learned-rollout-frames", type=int, default=200)
     args = ap.parse_args(argv)
     args.warmup = max(3, args.warmup)
     return args

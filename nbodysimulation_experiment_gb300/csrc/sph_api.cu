@@ -135,7 +135,7 @@ struct sph_sim {
 	BufferSet snap;
 	int *snapCellStart = nullptr, *snapCellCount = nullptr;
 	float2 *lz0 = nullptr, *lu = nullptr, *lbyId = nullptr, *ldens = nullptr;
-	float *lerr = nullptr;
+	double *lerr = nullptr;  // judge's reduction: kErrBlocks partial sums, then the total
 	uint32_t *lstats = nullptr;
 
 	// Headless render output (allocated on first use).
@@ -927,7 +927,7 @@ int ensure_learned(sph_sim *s) {
 	    (rc = dalloc(&B.acc, N)) || (rc = dalloc(&B.dens, N)) || (rc = dalloc(&B.press, N)) ||
 	    (rc = dalloc(&B.id, N)) || (rc = dalloc(&B.cellOf, N)) || (rc = dalloc(&s->snapCellStart, C)) ||
 	    (rc = dalloc(&s->snapCellCount, C)) || (rc = dalloc(&s->lz0, N)) || (rc = dalloc(&s->lu, N)) ||
-	    (rc = dalloc(&s->lbyId, N)) || (rc = dalloc(&s->ldens, N)) || (rc = dalloc(&s->lerr, 1)) ||
+	    (rc = dalloc(&s->lbyId, N)) || (rc = dalloc(&s->ldens, N)) || (rc = dalloc(&s->lerr, kErrBlocks + 1)) ||
 	    (rc = dalloc(&s->lstats, 4)))
 		return rc;
 	return SPH_OK;
@@ -975,14 +975,16 @@ int density_error(sph_sim *s, float *out) {
 	Q.press = s->lbyId;
 	k_density<<<s->densBlocks, kDensWarps * kWarp, dens_smem_bytes(), s->stream>>>(tt, Q, T);
 	SPH_LAUNCHED(s);
-	SPH_CUDA(cudaMemsetAsync(s->lerr, 0, sizeof(float), s->stream));
-	k_density_error<<<blocks_for(tt.n, 256), 256, 0, s->stream>>>(tt.n, s->ldens, sc.params.rest_density, s->lerr);
+	const int blocks = std::min(blocks_for(tt.n, kErrThreads), kErrBlocks);
+	k_density_error<<<blocks, kErrThreads, 0, s->stream>>>(tt.n, s->ldens, sc.params.rest_density, s->lerr);
 	SPH_LAUNCHED(s);
-	float sum = 0.0f;
-	SPH_CUDA(cudaMemcpyAsync(&sum, s->lerr, sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+	k_density_error_total<<<1, kErrBlocks, 0, s->stream>>>(blocks, s->lerr, s->lerr + kErrBlocks);
+	SPH_LAUNCHED(s);
+	double sum = 0.0;
+	SPH_CUDA(cudaMemcpyAsync(&sum, s->lerr + kErrBlocks, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
 	rc = check_device_errors(s);
 	if (rc) return rc;
-	*out = tt.n > 0 ? sum / ((float)tt.n * sc.params.rest_density) : 0.0f;
+	*out = tt.n > 0 ? (float)(sum / ((double)tt.n * (double)sc.params.rest_density)) : 0.0f;
 	return SPH_OK;
 }
 

@@ -102,7 +102,10 @@ __global__ void k_springs_commit(Totals tt, Particles Q, SimTables T);
 __global__ void k_springs_apply(Totals tt, Particles Q, SimTables T);
 __global__ void k_learned_z0(int n, int np, const float2 *pos, const float2 *prev, float invH, float2 *z0);
 __global__ void k_learned_finish(Totals tt, Particles P, const float2 *u, SimTables T);
-__global__ void k_density_error(int n, const float2 *dens, float rho0, float *out);
+constexpr int kErrThreads = 256;  // judge's reduction: threads per block
+constexpr int kErrBlocks = 512;   // and at most this many blocks
+__global__ void k_density_error(int n, const float2 *dens, float rho0, double *partial);
+__global__ void k_density_error_total(int blocks, const double *partial, double *out);
 __global__ void k_scatter_by_id(int n, const float2 *pos, const int *id, float2 *byId);
 __global__ void k_learned_target(int n, const float2 *byId, const int *ids, const float2 *xstar, float invH,
                                  float2 *target);

@@ -112,6 +112,25 @@ def test_judge_falls_back_to_the_plain_frame():
     b.close()
 
 
+def test_judge_is_deterministic():
+    """The judge's density deviation is summed in a fixed order: the same
+    frame from the same state gives the same deviation and verdict, bit for
+    bit, however often it is repeated."""
+    scene = scenes.scaled_block(48, seed=7)
+    model = pkg.Mpnn(4096, seed=4)
+    sim = _sim(scene)
+    st = sim.dump_state()
+    seen = set()
+    for _ in range(5):
+        sim.load_state(st)
+        used, err = sim.learned_frame(model, FRAME, SUBSTEPS, bound=1e9)
+        seen.add((used, np.float32(err).tobytes()))
+        after = sim.dump_state()["pos"].tobytes()
+        seen.add(after)
+    assert len(seen) == 2, "the learned frame or its judged deviation varied between repeats"
+    sim.close()
+
+
 def test_trained_network_gains_over_the_method_without_it():
     """Held-out frames: the trained network's correction beats the single
     plain update without it (u = 0) by a wide margin, and the judge takes
