@@ -286,11 +286,12 @@ class ReferenceSim(_CpuSim):
     _prefix = "sphref_"
     _real = np.float32
     _lib = None
+    _libname = "libsphref.so"
 
     @classmethod
     def load(cls):
         if cls._lib is None:
-            path = os.path.join(REF_DIR, "libsphref.so")
+            path = os.path.join(REF_DIR, cls._libname)
             if not os.path.exists(path):
                 raise FileNotFoundError(path)
             lib = ctypes.CDLL(path)
@@ -339,6 +340,44 @@ class ReferenceSim(_CpuSim):
         out = np.zeros(9, np.float32)
         lib.sphref_params_from_ctor8(_ptr(a, _c.c_float), _ptr(out, _c.c_float))
         return out
+
+
+class ReferenceSimBox51(ReferenceSim):
+    """The reference's own Demo4 solver built with raised compile-time
+    constants (oracle/Makefile target ``reference``): a 51.2-wide box
+    (kSPHBoundaryWidth; the height follows from the reference's 16:9 aspect,
+    170 x 96 cells) holding up to 65,536 particles, for the 65,536-particle
+    scene.  Cell and neighbour capacities are the reference's."""
+
+    _lib = None
+    _libname = "libsphref_box51.so"
+
+    @classmethod
+    def available(cls) -> bool:
+        return os.path.exists(os.path.join(REF_DIR, cls._libname))
+
+    @classmethod
+    def oracle_domain(cls):
+        """The restatement's domain with exactly this build's box and
+        capacities."""
+        lim = cls.limits()
+        d = OracleSim.reference_domain()
+        d.width = float(np.float32(lim["half_width"]) * np.float32(2.0))
+        d.height = float(np.float32(lim["half_height"]) * np.float32(2.0))
+        d.max_particles = lim["max_particles"]
+        d.max_cell_particles = lim["max_cell"]
+        d.max_neighbors = lim["max_neighbors"]
+        return d
+
+
+class ReferenceSimBox205(ReferenceSimBox51):
+    """The reference's own solver with a 204.8-wide box (682 x 384 cells)
+    holding up to 1,048,576 particles, for the 1,048,576-particle block
+    (about 9.5 GB of host memory: the reference's fixed 1,000-entry
+    neighbour arrays)."""
+
+    _lib = None
+    _libname = "libsphref_box205.so"
 
 
 class OracleSim(_CpuSim):

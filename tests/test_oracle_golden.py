@@ -103,3 +103,63 @@ def test_reference_multithreading_is_racy_but_single_worker_deterministic():
             ref.update(float(scenes.DT))
         outs.append(ref.get_state(lists=False)["pos"])
     assert np.array_equal(outs[0], outs[1])
+
+
+@pytest.mark.skipif(not oracle.reference_tree_present(), reason="reference tree not present")
+def test_restatement_matches_raised_constant_reference_on_the_65536_scene():
+    """The restatement's runtime domain against the reference's own solver
+    compiled with raised constants (kSPHBoundaryWidth 51.2, so a 170 x 96
+    grid, and room for 65,536 particles; oracle/Makefile): the full
+    65,536-particle obstacle scene, first updates from the scene as loaded,
+    bit for bit -- grid sizing, clamping, cell arrays and statistics on a box
+    other than the reference's 10 x 5.625 one."""
+    from oracle.oracle import ReferenceSimBox51
+    assert ReferenceSimBox51.available()
+    scene = scenes.obstacles_65536()
+    ref = ReferenceSimBox51(multithreading=False)
+    orc = OracleSim(ReferenceSimBox51.oracle_domain())
+    assert (orc.gx, orc.gy) == (ReferenceSimBox51.limits()["gx"], ReferenceSimBox51.limits()["gy"])
+    scene.apply(ref)
+    scene.apply(orc)
+    for step in range(3):
+        ref.update(float(scenes.DT))
+        orc.update(float(scenes.DT))
+        a = ref.get_state(lists=(step == 1))
+        b = orc.get_state(lists=(step == 1))
+        for k in ("pos", "prev", "vel", "dens", "press"):
+            assert np.array_equal(a[k], b[k].astype(np.float32)), (step, k)
+        assert np.array_equal(a["cell_count"], b["cell_count"]) and np.array_equal(a["cell_flat"], b["cell_flat"])
+        if step == 1:
+            assert np.array_equal(a["nb_flat"], b["nb_flat"])
+        assert np.array_equal(ref.get_stats()[0], orc.get_stats()[0])
+    ref.close()
+    orc.close()
+
+
+@pytest.mark.skipif(not oracle.reference_tree_present(), reason="reference tree not present")
+def test_restatement_matches_raised_constant_reference_on_the_1m_block():
+    """The same on the 1,048,576-particle block (the reference built with a
+    204.8-wide box and room for 1,048,576 particles): the first two updates
+    from the block as loaded, bit for bit.  The reference has no springs, so
+    this pins the plain step at that size."""
+    from conftest import host_memory_gb
+    from oracle.oracle import ReferenceSimBox205
+    if host_memory_gb() < 40:
+        pytest.skip("the reference at 1M particles needs ~10 GB of host memory")
+    assert ReferenceSimBox205.available()
+    scene = scenes.block_1m()
+    ref = ReferenceSimBox205(multithreading=False)
+    orc = OracleSim(ReferenceSimBox205.oracle_domain())
+    scene.apply(ref)
+    scene.apply(orc)
+    for step in range(2):
+        ref.update(float(scenes.DT))
+        orc.update(float(scenes.DT))
+    a = ref.get_state(lists=False)
+    b = orc.get_state(lists=False)
+    for k in ("pos", "prev", "vel", "dens", "press"):
+        assert np.array_equal(a[k], b[k].astype(np.float32)), k
+    assert np.array_equal(a["cell_count"], b["cell_count"]) and np.array_equal(a["cell_flat"], b["cell_flat"])
+    assert np.array_equal(ref.get_stats()[0], orc.get_stats()[0])
+    ref.close()
+    orc.close()
