@@ -698,6 +698,7 @@ __device__ __forceinline__ bool slot_claim(ViscMultiSmemT<C> &S, int s, const Si
 		S.state[s] = kSlotWait;
 		S.waitSince[s] = global_ns();
 	}
+	stamp(T, 0, t, 0, lane);
 	__syncwarp();
 	return true;
 }
@@ -763,6 +764,7 @@ __device__ __forceinline__ void slot_produce(ViscMultiSmemT<C> &S, int s, const 
 		slot_copy_vel<C>(S, s, P, lane, false);
 		__threadfence();
 		__syncwarp();
+		stamp(T, 0, S.task[s], 3, lane);
 		if (lane == 0) {
 			if (S.claim[s] != T.hold[0]) st_release(&T.done[S.task[s]], 1u);
 			S.state[s] = kSlotFree;
@@ -796,6 +798,7 @@ __device__ __forceinline__ void slot_produce(ViscMultiSmemT<C> &S, int s, const 
 			__syncwarp();
 			return;
 		}
+		stamp(T, 0, S.task[s], 1, lane);
 		slot_copy_vel<C>(S, s, P, lane, true);
 		slot_geometry<C>(S, s, 0, P, lane);
 		if (lane == 0) S.state[s] = kSlotStaged;
