@@ -2444,6 +2444,12 @@ cudaError_t sweep_attributes() {
 	if (e == cudaSuccess)
 		e = cudaFuncSetAttribute(k_delta<DeltaMid>, cudaFuncAttributeMaxDynamicSharedMemorySize,
 		                         (int)delta_smem_bytes<DeltaMid>());
+	if (e == cudaSuccess)
+		e = cudaFuncSetAttribute(k_delta<DeltaTri>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                         (int)delta_smem_bytes<DeltaTri>());
+	if (e == cudaSuccess)
+		e = cudaFuncSetAttribute(k_delta<DeltaQuad>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                         (int)delta_smem_bytes<DeltaQuad>());
 	return e;
 }
 
@@ -2461,6 +2467,12 @@ cudaError_t sweep_occupancy(bool viscLean, int deltaShape, int *occV, int *occD)
 	if (deltaShape == kDeltaMid)
 		return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occD, k_delta<DeltaMid>, DeltaMid::kWarps * kWarp,
 		                                                     delta_smem_bytes<DeltaMid>());
+	if (deltaShape == kDeltaTri)
+		return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occD, k_delta<DeltaTri>, DeltaTri::kWarps * kWarp,
+		                                                     delta_smem_bytes<DeltaTri>());
+	if (deltaShape == kDeltaQuad)
+		return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occD, k_delta<DeltaQuad>, DeltaQuad::kWarps * kWarp,
+		                                                     delta_smem_bytes<DeltaQuad>());
 	return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occD, k_delta<DeltaWide>, DeltaWide::kWarps * kWarp,
 	                                                     delta_smem_bytes<DeltaWide>());
 }
@@ -2478,6 +2490,10 @@ void launch_delta(int shape, int blocks, cudaStream_t st, Totals tt, Particles Q
 		k_delta<DeltaLean><<<blocks, DeltaLean::kWarps * kWarp, delta_smem_bytes<DeltaLean>(), st>>>(tt, Q, T);
 	else if (shape == kDeltaMid)
 		k_delta<DeltaMid><<<blocks, DeltaMid::kWarps * kWarp, delta_smem_bytes<DeltaMid>(), st>>>(tt, Q, T);
+	else if (shape == kDeltaTri)
+		k_delta<DeltaTri><<<blocks, DeltaTri::kWarps * kWarp, delta_smem_bytes<DeltaTri>(), st>>>(tt, Q, T);
+	else if (shape == kDeltaQuad)
+		k_delta<DeltaQuad><<<blocks, DeltaQuad::kWarps * kWarp, delta_smem_bytes<DeltaQuad>(), st>>>(tt, Q, T);
 	else
 		k_delta<DeltaWide><<<blocks, DeltaWide::kWarps * kWarp, delta_smem_bytes<DeltaWide>(), st>>>(tt, Q, T);
 }

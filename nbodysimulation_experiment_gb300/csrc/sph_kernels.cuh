@@ -42,11 +42,26 @@ struct DeltaMid {
 	static constexpr int kWarps = 8, kStage = kDeltaStageCap, kChainW = 128, kPrefetch = 128, kMinBlocks = 2;
 	static constexpr bool kPipelined = true, kShortEntry = true;
 };
+// Small pipelined shapes for large scenes, where the sweep is bound by how
+// many tasks run at once rather than by one task's latency: two (tri) or
+// three (quad) producer warps and the summer warp, several blocks per SM.
+struct DeltaTri {
+	static constexpr int kWarps = 3, kStage = 1536, kChainW = 256, kPrefetch = 64, kMinBlocks = 5;
+	static constexpr bool kPipelined = true, kShortEntry = true;
+};
+struct DeltaQuad {
+	static constexpr int kWarps = 4, kStage = 1536, kChainW = 192, kPrefetch = 128, kMinBlocks = 4;
+	static constexpr bool kPipelined = true, kShortEntry = true;
+};
 // Delta shapes by index (sph_set_sweep_shape names them by warp count).
-constexpr int kDeltaShapes = 3;
-constexpr int kDeltaWide = 0, kDeltaLean = 1, kDeltaMid = 2;
+constexpr int kDeltaShapes = 5;
+constexpr int kDeltaWide = 0, kDeltaLean = 1, kDeltaMid = 2, kDeltaTri = 3, kDeltaQuad = 4;
 constexpr int delta_shape_warps(int shape) {
-	return shape == kDeltaLean ? DeltaLean::kWarps : (shape == kDeltaMid ? DeltaMid::kWarps : DeltaWide::kWarps);
+	return shape == kDeltaLean   ? DeltaLean::kWarps
+	       : shape == kDeltaMid  ? DeltaMid::kWarps
+	       : shape == kDeltaTri  ? DeltaTri::kWarps
+	       : shape == kDeltaQuad ? DeltaQuad::kWarps
+	                             : DeltaWide::kWarps;
 }
 constexpr int kDensWarps = 8;
 constexpr int kViscRefWarps = 4;  // reference-order viscosity sweep: one task per warp

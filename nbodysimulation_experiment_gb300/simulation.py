@@ -126,10 +126,10 @@ class SpringParams(ctypes.Structure):
 
 SPRING_SLOTS = 16
 #: Warps per task of the ordered sweeps' launch shapes, (wide, lean) and for
-#: the delta sweep (wide, lean, mid): the values ``sph_set_sweep_shape``
-#: accepts (csrc/sph_kernels.cuh).
+#: the delta sweep (wide, lean, mid, tri, quad): the values
+#: ``sph_set_sweep_shape`` accepts (csrc/sph_kernels.cuh).
 VISC_WARPS = (4, 5)
-DELTA_WARPS = (12, 2, 8)
+DELTA_WARPS = (12, 2, 8, 3, 4)
 
 
 class BodyDesc(ctypes.Structure):

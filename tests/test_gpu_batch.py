@@ -166,7 +166,9 @@ def _run_with_shape(scene, shape, steps):
 @pytest.mark.parametrize("shape", [(VISC_WARPS[1], None, DELTA_WARPS[1], None),
                                    (VISC_WARPS[1], 152, DELTA_WARPS[0], 152),
                                    (VISC_WARPS[0], 152 * 3, DELTA_WARPS[1], 152 * 5),
-                                   (VISC_WARPS[0], 152, DELTA_WARPS[2], 304)])
+                                   (VISC_WARPS[0], 152, DELTA_WARPS[2], 304),
+                                   (VISC_WARPS[1], 152 * 3, DELTA_WARPS[3], 152 * 5),
+                                   (VISC_WARPS[0], 152, DELTA_WARPS[4], 152 * 4)])
 def test_sweep_shapes_give_identical_results(shape):
     """Lean, mid and wide sweeps, with any resident block count, compute the
     same update."""
