@@ -281,8 +281,8 @@ int sph_kernel_launches(sph_sim *sim, uint64_t *out);
  * kernel one by one instead.  Results are identical either way.  Default 1. */
 int sph_use_graphs(sph_sim *sim, int enable);
 /* No counterpart in the reference.  Launch shapes of the two ordered sweeps
- * (viscosity, delta): shape[4] = {viscosity shape (4 = wide, 5 = lean,
- * 6 = paired lean), viscosity blocks, delta warps per block (12 = wide, 8 = mid,
+ * (viscosity, delta): shape[4] = {viscosity warps per block (4 = wide,
+ * 5 = lean), viscosity blocks, delta warps per block (12 = wide, 8 = mid,
  * 4 = quad, 3 = tri, 2 = lean), delta blocks}.  The wide shapes shorten one
  * scene's critical path: one task per block; the wide viscosity sweep runs
  * each particle's head beside the previous particle's tail on two lanes; the
@@ -290,9 +290,8 @@ int sph_use_graphs(sph_sim *sim, int enable);
  * with the next particle's pairs (11, 7, 3 and 2 producer warps beside one
  * summer warp; mid, quad and tri run several blocks per SM).  The lean ones
  * fit more tasks on an SM (the lean viscosity sweep runs five tasks per
- * block; the paired lean one four, each on two lanes running a particle's
- * head beside the previous particle's tail, as the wide shape does) for
- * large scenes and many scenes.  Results do not depend on the shape.  sph_autotune times the
+ * block) for large scenes and many scenes.  Results do not depend on the
+ * shape.  sph_autotune times the
  * next update (step dt) from the current state for every shape and resident
  * block count per SM, keeps the fastest for each sweep, restores the state
  * and reports the choice; it needs a state after an update. */

@@ -96,7 +96,7 @@ struct sph_sim {
 	cudaStream_t stream = nullptr;
 	int numSMs = 0;
 	int viscBlocks = 0, deltaBlocks = 0, densBlocks = 0, gridBlocks = 0;
-	int viscShape = 0;  // viscosity shape: kViscWide, kViscLean or kViscPair (sph_kernels.cuh)
+	int viscLean = 0;   // viscosity shape: 0 = wide, 1 = lean (sph_kernels.cuh)
 	bool refOrder = false;  // sweeps and grid events in AddParticle order (sph_set_reference_order)
 	int viscRefBlocks = 0;
 	int deltaShape = 0;  // delta shape: kDeltaWide, kDeltaLean or kDeltaMid
@@ -510,7 +510,7 @@ int enqueue_step(sph_sim *s, bool capturing) {
 		SPH_CUDA(cudaMemsetAsync(T.taskCounter, 0, sizeof(int), st));
 		SimTables v = T;
 		v.done = s->doneV;
-		launch_viscosity(s->viscShape, s->viscBlocks, st, tt, A.view(), v);
+		launch_viscosity(s->viscLean, s->viscBlocks, st, tt, A.view(), v);
 		SPH_LAUNCHED(s);
 	}
 	SPH_CUDA(mark(kEvVisc));
@@ -765,8 +765,7 @@ int allocate(sph_sim *s) {
 	                         (int)springs_smem_bytes()) != cudaSuccess)
 		return SPH_ERR_CUDA;
 	int occV = 0, occD = 0;
-	if (sweep_occupancy(kViscWide, kDeltaWide, &occV, &occD) != cudaSuccess || occV < 1 || occD < 1)
-		return SPH_ERR_CUDA;
+	if (sweep_occupancy(false, kDeltaWide, &occV, &occD) != cudaSuccess || occV < 1 || occD < 1) return SPH_ERR_CUDA;
 	s->viscBlocks = occV * s->numSMs;
 	s->deltaBlocks = occD * s->numSMs;
 	s->densBlocks = std::max(1, std::min(blocks_for(C, kDensWarps), 64 * s->numSMs));
@@ -1855,8 +1854,8 @@ int sph_autotune(sph_sim *s, float dt, int *shape) {
 	if (rc) return rc;
 	// Median of three timed updates per shape (after one warm-up update); the
 	// current shape is kept unless another is faster by more than 2%.
-	auto measure = [&](int vShape, int vBlocks, int dShape, int dBlocks, float *tv, float *td) -> int {
-		s->viscShape = vShape;
+	auto measure = [&](int vLean, int vBlocks, int dShape, int dBlocks, float *tv, float *td) -> int {
+		s->viscLean = vLean;
 		s->viscBlocks = vBlocks;
 		s->deltaShape = dShape;
 		s->deltaBlocks = dBlocks;
@@ -1876,19 +1875,16 @@ int sph_autotune(sph_sim *s, float dt, int *shape) {
 		*td = d[1];
 		return SPH_OK;
 	};
-	int pick[4] = {s->viscShape, s->viscBlocks, s->deltaShape, s->deltaBlocks};
+	int pick[4] = {s->viscLean, s->viscBlocks, s->deltaShape, s->deltaBlocks};
 	float bestV = 0.f, bestD = 0.f;
 	rc = measure(pick[0], pick[1], pick[2], pick[3], &bestV, &bestD);
-	// Candidates: every delta shape, each timed with a viscosity shape of the
-	// same kind (lean with lean, paired with tri and quad, wide with wide and
-	// mid), at every resident block count per SM; the two sweeps' picks are
-	// independent.
+	// Candidates: every delta shape, each timed with the viscosity shape of
+	// the same kind (lean with lean, wide with both pipelined delta shapes),
+	// at every resident block count per SM.
 	for (int dShape = 0; dShape < kDeltaShapes && !rc; ++dShape) {
-		const int lean = dShape == kDeltaLean                         ? kViscLean
-		                 : (dShape == kDeltaTri || dShape == kDeltaQuad) ? kViscPair
-		                                                                 : kViscWide;
+		const int lean = dShape == kDeltaLean ? 1 : 0;
 		int occV = 0, occD = 0;
-		rc = cuda_status(sweep_occupancy(lean, dShape, &occV, &occD));
+		rc = cuda_status(sweep_occupancy(lean != 0, dShape, &occV, &occD));
 		const int maxPer = std::max(occV, occD);
 		for (int per = 1; per <= maxPer && !rc; ++per) {
 			const int vb = std::min(per, occV) * s->numSMs, db = std::min(per, occD) * s->numSMs;
@@ -1908,7 +1904,7 @@ int sph_autotune(sph_sim *s, float dt, int *shape) {
 		}
 	}
 	if (!rc) rc = copy_state(s, false);
-	s->viscShape = pick[0];
+	s->viscLean = pick[0];
 	s->viscBlocks = pick[1];
 	s->deltaShape = pick[2];
 	s->deltaBlocks = pick[3];
@@ -1918,7 +1914,7 @@ int sph_autotune(sph_sim *s, float dt, int *shape) {
 	if (rc) return rc;
 	SPH_CUDA(cudaStreamSynchronize(s->stream));
 	if (shape) {
-		shape[0] = visc_shape_id(s->viscShape);
+		shape[0] = s->viscLean ? ViscLean::kWarps : ViscWide::kWarps;
 		shape[1] = s->viscBlocks;
 		shape[2] = delta_shape_warps(s->deltaShape);
 		shape[3] = s->deltaBlocks;
@@ -1928,7 +1924,7 @@ int sph_autotune(sph_sim *s, float dt, int *shape) {
 
 int sph_get_sweep_shape(sph_sim *s, int *shape) {
 	if (!s || !shape) return SPH_ERR_INVALID_ARGUMENT;
-	shape[0] = visc_shape_id(s->viscShape);
+	shape[0] = s->viscLean ? ViscLean::kWarps : ViscWide::kWarps;
 	shape[1] = s->viscBlocks;
 	shape[2] = delta_shape_warps(s->deltaShape);
 	shape[3] = s->deltaBlocks;
@@ -1937,10 +1933,7 @@ int sph_get_sweep_shape(sph_sim *s, int *shape) {
 
 int sph_set_sweep_shape(sph_sim *s, const int *shape) {
 	if (!s || !shape) return SPH_ERR_INVALID_ARGUMENT;
-	int vShape = -1;
-	for (int k = 0; k < kViscShapes; ++k)
-		if (shape[0] == visc_shape_id(k)) vShape = k;
-	const bool vOk = vShape >= 0;
+	const bool vOk = shape[0] == ViscLean::kWarps || shape[0] == ViscWide::kWarps;
 	int dShape = -1;
 	for (int k = 0; k < kDeltaShapes; ++k)
 		if (shape[2] == delta_shape_warps(k)) dShape = k;
@@ -1948,7 +1941,7 @@ int sph_set_sweep_shape(sph_sim *s, const int *shape) {
 	if (!vOk || !dOk || shape[1] < 1 || shape[3] < 1 || shape[1] > (1 << 20) || shape[3] > (1 << 20))
 		return SPH_ERR_INVALID_ARGUMENT;
 	SPH_CUDA(cudaStreamSynchronize(s->stream));
-	s->viscShape = vShape;
+	s->viscLean = shape[0] == ViscLean::kWarps;
 	s->viscBlocks = shape[1];
 	s->deltaShape = dShape;
 	s->deltaBlocks = shape[3];

@@ -649,8 +649,8 @@ __device__ __forceinline__ void slot_geometry(ViscMultiSmemT<C> &S, int s, int k
 
 // Claim the next task into slot s (one warp).  Returns false when none is
 // left.
-template <class SM>
-__device__ __forceinline__ bool slot_claim(SM &S, int s, const SimTables &T, int nLive, int lane) {
+template <class C>
+__device__ __forceinline__ bool slot_claim(ViscMultiSmemT<C> &S, int s, const SimTables &T, int nLive, int lane) {
 	int i = 0;
 	if (lane == 0) i = atomicAdd(&T.taskCounter[0], 1);
 	i = __shfl_sync(kFull, i, 0);
@@ -705,8 +705,8 @@ __device__ __forceinline__ bool slot_claim(SM &S, int s, const SimTables &T, int
 
 // One non-blocking poll of slot s's earlier conflicting tasks (cells of the
 // scene at most two apart, as k_viscosity).  True when all are done.
-template <class SM>
-__device__ __forceinline__ bool slot_ready(SM &S, int s, const SimTables &T, int lane) {
+template <class C>
+__device__ __forceinline__ bool slot_ready(ViscMultiSmemT<C> &S, int s, const SimTables &T, int lane) {
 	const int t = S.task[s], c = S.cell[s];
 	const SceneDev &sc = T.scenes[T.sceneOfCell[c]];
 	const int base = sc.cellBase, gx = sc.p.gx, gy = sc.p.gy;
@@ -721,8 +721,8 @@ __device__ __forceinline__ bool slot_ready(SM &S, int s, const SimTables &T, int
 	return !__any_sync(kFull, pending);
 }
 
-template <class SM>
-__device__ __forceinline__ void slot_copy_vel(SM &S, int s, const Particles &P, int lane, bool in) {
+template <class C>
+__device__ __forceinline__ void slot_copy_vel(ViscMultiSmemT<C> &S, int s, const Particles &P, int lane, bool in) {
 	int segStart[9], segOff[9];
 #pragma unroll
 	for (int q = 0; q < 9; ++q) {
@@ -761,7 +761,7 @@ __device__ __forceinline__ void slot_produce(ViscMultiSmemT<C> &S, int s, const 
 	int state = S.state[s];
 	if (state == kSlotDone) {
 		// Chain finished: write the block's velocities back and release.
-		slot_copy_vel(S, s, P, lane, false);
+		slot_copy_vel<C>(S, s, P, lane, false);
 		__threadfence();
 		__syncwarp();
 		stamp(T, 0, S.task[s], 3, lane);
@@ -774,14 +774,14 @@ __device__ __forceinline__ void slot_produce(ViscMultiSmemT<C> &S, int s, const 
 	}
 	if (state == kSlotFree) {
 		if (__shfl_sync(kFull, S.exhausted, 0)) return;
-		if (!slot_claim(S, s, T, nLive, lane)) {
+		if (!slot_claim<C>(S, s, T, nLive, lane)) {
 			if (lane == 0) S.exhausted = 1;
 			return;
 		}
 		state = kSlotWait;
 	}
 	if (state == kSlotWait) {
-		if (!slot_ready(S, s, T, lane)) {
+		if (!slot_ready<C>(S, s, T, lane)) {
 			if (lane == 0 && global_ns() - S.waitSince[s] > T.waitLimitNs) {
 				atomicOr(T.error, kErrTimeout);
 				atomicExch(T.abort, 1u);
@@ -799,7 +799,7 @@ __device__ __forceinline__ void slot_produce(ViscMultiSmemT<C> &S, int s, const 
 			return;
 		}
 		stamp(T, 0, S.task[s], 1, lane);
-		slot_copy_vel(S, s, P, lane, true);
+		slot_copy_vel<C>(S, s, P, lane, true);
 		slot_geometry<C>(S, s, 0, P, lane);
 		if (lane == 0) S.state[s] = kSlotStaged;
 		__syncwarp();
@@ -891,269 +891,6 @@ __global__ void __launch_bounds__(C::kWarps * kWarp, C::kMinBlocks) k_viscosity_
 			if (tid == kWarp && ld_acquire(T.abort) != 0u) S.aborted = 1;
 			__syncwarp();
 			for (int s = warp - 1; s < C::kSlots; s += C::kProd) slot_produce<C>(S, s, P, T, nLive, lane);
-		}
-		__syncthreads();
-	}
-}
-
-// ---------------------------------------------------------------------------
-// Viscosity sweep, paired lean shape (ViscPair): the lean shape's block of
-// several tasks with the wide shape's head/tail lockstep.  Slot s has two
-// chain lanes of warp 0 (2s and 2s+1) and one producer warp (1 + s).  In
-// phase k of a slot, lane 2s + (k & 1) runs particle k's head (its pairs
-// before list slot own + k - 1) beside the other lane's tail of particle k - 1
-// (its pairs after slot own + k), in lockstep; once k - 1 is finished
-// and stored, the first lane runs k's middle (its pairs with k - 1, itself
-// and k + 1) and keeps k's velocity for its tail in phase k + 1.  The
-// argument is the wide shape's (k_viscosity): the two chains touch disjoint
-// slots, and every velocity sees the pairs that touch it in the reference's
-// order.  A task of cnt particles takes cnt + 1 phases; the producer computes
-// particle k + 1's geometry (and where its middle and tail begin) into the
-// third buffer during phase k.
-template <class C>
-struct ViscPairSlotT {
-	float2 vel[kStageCap + 2];  // + a scratch slot (kStageCap) for the chains' idle steps
-	float4 geo[3][C::kGeom];    // per particle k % 3: in-range pairs (slot, unit vector, 1 - q)
-	float4 pad;
-};
-template <class C>
-struct ViscPairSmemT {
-	ViscPairSlotT<C> slot[C::kSlots];
-	int segStart[C::kSlots][9], segOff[C::kSlots][9];
-	int state[C::kSlots], task[C::kSlots], first[C::kSlots], cnt[C::kSlots], own[C::kSlots], L[C::kSlots],
-	    k[C::kSlots], cell[C::kSlots], claim[C::kSlots];
-	int m[C::kSlots][3];
-	int2 split[C::kSlots][3];  // first pair of the middle, first pair of the tail
-	float h2[C::kSlots], invH[C::kSlots], sigma[C::kSlots], beta[C::kSlots], hdt[C::kSlots];
-	unsigned long long waitSince[C::kSlots];
-	int exhausted;
-	int aborted;
-};
-
-namespace {
-
-// Pair geometry of particle k of slot s (one warp), as slot_geometry, into
-// buffer k % 3, with the split of its compacted list into head (entries
-// before list slot own + k - 1), middle (up to slot own + k + 1) and tail.
-template <class C>
-__device__ __forceinline__ void pair_geometry(ViscPairSmemT<C> &S, int s, int k, const Particles &P, int lane) {
-	const int buf = k % 3;
-	float4 *G = S.slot[s].geo[buf];
-	int segStart[9], segOff[9];
-#pragma unroll
-	for (int q = 0; q < 9; ++q) {
-		segStart[q] = S.segStart[s][q];
-		segOff[q] = S.segOff[s][q];
-	}
-	const int L = S.L[s];
-	const int me = S.own[s] + k;
-	const float h2 = S.h2[s], invH = S.invH[s];
-	const float2 xi = __ldg(&P.pos[S.first[s] + k]);
-	int m = 0, nHead = 0, nToTail = 0;
-	for (int b0 = 0; b0 < L; b0 += 4 * kWarp) {
-		float2 xj[4];
-#pragma unroll
-		for (int u = 0; u < 4; ++u) {
-			const int e = b0 + u * kWarp + lane;
-			xj[u] = e < L ? __ldg(&P.pos[seg_src<9>(e, segOff, segStart)]) : make_float2(0.f, 0.f);
-		}
-#pragma unroll
-		for (int u = 0; u < 4; ++u) {
-			const int e = b0 + u * kWarp + lane;
-			const float rx = xj[u].x - xi.x, ry = xj[u].y - xi.y;
-			const float r2 = rx * rx + ry * ry;
-			const bool in = e < L && r2 < h2;
-			const unsigned mask = __ballot_sync(kFull, in);
-			nHead += __popc(__ballot_sync(kFull, in && e < me - 1));
-			nToTail += __popc(__ballot_sync(kFull, in && e <= me + 1));
-			const int at = m + __popc(mask & lanemask_lt());
-			if (in && at < C::kGeom) G[at] = make_float4(__int_as_float(e), rx, ry, r2);
-			m += __popc(mask);
-		}
-	}
-	__syncwarp();
-	const int mm = min(m, C::kGeom);
-	for (int q = lane; q < mm; q += kWarp) {
-		const float4 g = G[q];
-		const float r = sqrtf(g.w);
-		const float qq = r * invH;
-		float len = r;  // Vec2Length(Rij) == rij
-		if (len == 0.0f) len = 1.0f;
-		const float inv = 1.0f / len;
-		G[q] = make_float4(g.x, g.y * inv, g.z * inv, 1.0f - qq);
-	}
-	if (lane == 0) {
-		S.m[s][buf] = m;
-		S.split[s][buf] = make_int2(nHead, nToTail);
-	}
-}
-
-// Phase k of slot s for chain lane `sub` (0 or 1) of the slot's pair; vi is
-// the lane's particle velocity, carried from a particle's head and middle to
-// its tail in the next phase.  A particle with more in-range pairs than the
-// geometry buffer holds runs its whole chain in the middle, computing the
-// geometry there.
-template <class C>
-__device__ __forceinline__ void pair_wave(ViscPairSmemT<C> &S, int s, int sub, float2 &vi, const Particles &P) {
-	const int k = S.k[s], cnt = S.cnt[s], own = S.own[s];
-	float2 *V = S.slot[s].vel;
-	const float sigma = S.sigma[s], beta = S.beta[s], hdt = S.hdt[s];
-	const unsigned pm = 3u << (2 * s);
-	const bool head = (k & 1) == sub;  // head and middle of particle k; else the tail of particle k - 1
-	const bool has = head ? k < cnt : k >= 1;
-	const int buf = has ? (head ? k : k - 1) % 3 : 0;
-	int start = 0, len = 0, m = 0;
-	int2 sp = make_int2(0, 0);
-	if (has) {
-		m = S.m[s][buf];
-		sp = S.split[s][buf];
-		const bool inl = m > C::kGeom;
-		if (head) {
-			vi = V[own + k];
-			len = inl ? 0 : sp.x;
-		} else {
-			start = sp.y;
-			len = inl ? 0 : m - sp.y;
-		}
-	}
-	const int n = max(len, __shfl_xor_sync(pm, len, 1));
-	visc_run_range<false>(V, S.slot[s].geo[buf], start, len, n, vi, sigma, beta, hdt);
-	if (has && !head) V[own + k - 1] = vi;  // particle k - 1 is finished
-	__syncwarp(pm);
-	if (!(has && head)) return;
-	if (m > C::kGeom) {
-		int segStart[9], segOff[9];
-#pragma unroll
-		for (int q = 0; q < 9; ++q) {
-			segStart[q] = S.segStart[s][q];
-			segOff[q] = S.segOff[s][q];
-		}
-		const int L = S.L[s];
-		const float h2 = S.h2[s], invH = S.invH[s];
-		const float2 xi = __ldg(&P.pos[S.first[s] + k]);
-		for (int e = 0; e < L; ++e) {
-			const float2 xj = __ldg(&P.pos[seg_src<9>(e, segOff, segStart)]);
-			const float rx = xj.x - xi.x, ry = xj.y - xi.y;
-			const float r2 = rx * rx + ry * ry;
-			if (!(r2 < h2)) continue;
-			const float r = sqrtf(r2);
-			const float qq = r * invH;
-			float lenr = r;
-			if (lenr == 0.0f) lenr = 1.0f;
-			const float inv = 1.0f / lenr;
-			visc_pair<false>(V, e, make_float2(rx * inv, ry * inv), 1.0f - qq, V[e], vi, sigma, beta, hdt);
-		}
-		return;
-	}
-	const float4 *G = S.slot[s].geo[buf];
-	for (int q = sp.x; q < sp.y; ++q) {
-		const float4 g = G[q];
-		const int j = __float_as_int(g.x);
-		visc_pair<false>(V, j, make_float2(g.y, g.z), g.w, V[j], vi, sigma, beta, hdt);
-	}
-}
-
-// The producer warp's turn for slot s in one phase (as slot_produce).
-template <class C>
-__device__ __forceinline__ void pair_produce(ViscPairSmemT<C> &S, int s, const Particles &P, const SimTables &T,
-                                             int nLive, int lane) {
-	int state = S.state[s];
-	if (state == kSlotDone) {
-		slot_copy_vel(S, s, P, lane, false);
-		__threadfence();
-		__syncwarp();
-		stamp(T, 0, S.task[s], 3, lane);
-		if (lane == 0) {
-			if (S.claim[s] != T.hold[0]) st_release(&T.done[S.task[s]], 1u);
-			S.state[s] = kSlotFree;
-		}
-		__syncwarp();
-		state = kSlotFree;
-	}
-	if (state == kSlotFree) {
-		if (__shfl_sync(kFull, S.exhausted, 0)) return;
-		if (!slot_claim(S, s, T, nLive, lane)) {
-			if (lane == 0) S.exhausted = 1;
-			return;
-		}
-		state = kSlotWait;
-	}
-	if (state == kSlotWait) {
-		if (!slot_ready(S, s, T, lane)) {
-			if (lane == 0 && global_ns() - S.waitSince[s] > T.waitLimitNs) {
-				atomicOr(T.error, kErrTimeout);
-				atomicExch(T.abort, 1u);
-			}
-			return;
-		}
-		if (S.L[s] > kStageCap) {
-			if (lane == 0) {
-				atomicOr(T.error, kErrStageOverflow);
-				st_release(&T.done[S.task[s]], 1u);
-				S.state[s] = kSlotFree;
-			}
-			__syncwarp();
-			return;
-		}
-		stamp(T, 0, S.task[s], 1, lane);
-		slot_copy_vel(S, s, P, lane, true);
-		pair_geometry<C>(S, s, 0, P, lane);
-		if (lane == 0) S.state[s] = kSlotStaged;
-		__syncwarp();
-		return;
-	}
-	if (state == kSlotRun) {
-		const int k = S.k[s];
-		if (k + 1 < S.cnt[s]) pair_geometry<C>(S, s, k + 1, P, lane);
-	}
-}
-
-}  // namespace
-
-template <class C>
-__global__ void __launch_bounds__(C::kWarps * kWarp, C::kMinBlocks) k_viscosity_pair(Totals tt, Particles P,
-                                                                                    SimTables T) {
-	static_assert(C::kProd == C::kSlots && 2 * C::kSlots <= kWarp, "one producer warp and two chain lanes per slot");
-	extern __shared__ __align__(16) unsigned char smem_raw[];
-	ViscPairSmemT<C> &S = *reinterpret_cast<ViscPairSmemT<C> *>(smem_raw);
-	const int tid = threadIdx.x, warp = tid / kWarp, lane = tid & (kWarp - 1);
-	const int nLive = *T.nLive;
-	if (tid < C::kSlots) {
-		S.state[tid] = kSlotFree;
-		S.k[tid] = 0;
-	}
-	if (tid == 0) {
-		S.exhausted = 0;
-		S.aborted = 0;
-	}
-	__syncthreads();
-	float2 vi = make_float2(0.0f, 0.0f);  // chain lanes: the velocity of the lane's current particle
-	for (;;) {
-		// Bookkeeping of the phase just ended: thread s advances slot s.  A
-		// task of cnt particles runs phases 0 .. cnt.
-		int busy = 0;
-		if (tid < C::kSlots) {
-			int st = S.state[tid];
-			if (st == kSlotStaged) {
-				st = kSlotRun;
-				S.k[tid] = 0;
-			} else if (st == kSlotRun) {
-				const int k = S.k[tid] + 1;
-				S.k[tid] = k;
-				if (k == S.cnt[tid] + 1) st = kSlotDone;
-			}
-			S.state[tid] = st;
-			busy = st != kSlotFree;
-		}
-		const int anyBusy = __syncthreads_or(busy);
-		if ((!anyBusy && S.exhausted) || S.aborted) break;
-		if (warp == 0) {
-			const int s = lane >> 1;
-			if (lane < 2 * C::kSlots && S.state[s] == kSlotRun) pair_wave<C>(S, s, lane & 1, vi, P);
-		} else {
-			if (tid == kWarp && ld_acquire(T.abort) != 0u) S.aborted = 1;
-			__syncwarp();
-			pair_produce<C>(S, warp - 1, P, T, nLive, lane);
 		}
 		__syncthreads();
 	}
@@ -2696,9 +2433,6 @@ cudaError_t sweep_attributes() {
 	cudaError_t e = cudaFuncSetAttribute(k_viscosity<ViscWide>, cudaFuncAttributeMaxDynamicSharedMemorySize,
 	                                     (int)visc_smem_bytes<ViscWide>());
 	if (e == cudaSuccess)
-		e = cudaFuncSetAttribute(k_viscosity_pair<ViscPair>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-		                         (int)sizeof(ViscPairSmemT<ViscPair>));
-	if (e == cudaSuccess)
 		e = cudaFuncSetAttribute(k_viscosity_multi<ViscLean>, cudaFuncAttributeMaxDynamicSharedMemorySize,
 		                         (int)sizeof(ViscMultiSmemT<ViscLean>));
 	if (e == cudaSuccess)
@@ -2719,17 +2453,13 @@ cudaError_t sweep_attributes() {
 	return e;
 }
 
-cudaError_t sweep_occupancy(int viscShape, int deltaShape, int *occV, int *occD) {
-	cudaError_t e =
-	    viscShape == kViscLean   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(occV, k_viscosity_multi<ViscLean>,
-	                                                                           ViscLean::kWarps * kWarp,
-	                                                                           sizeof(ViscMultiSmemT<ViscLean>))
-	    : viscShape == kViscPair ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(occV, k_viscosity_pair<ViscPair>,
-	                                                                             ViscPair::kWarps * kWarp,
-	                                                                             sizeof(ViscPairSmemT<ViscPair>))
-	                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(occV, k_viscosity<ViscWide>,
-	                                                                             ViscWide::kWarps * kWarp,
-	                                                                             visc_smem_bytes<ViscWide>());
+cudaError_t sweep_occupancy(bool viscLean, int deltaShape, int *occV, int *occD) {
+	cudaError_t e = viscLean ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(occV, k_viscosity_multi<ViscLean>,
+	                                                                         ViscLean::kWarps * kWarp,
+	                                                                         sizeof(ViscMultiSmemT<ViscLean>))
+	                         : cudaOccupancyMaxActiveBlocksPerMultiprocessor(occV, k_viscosity<ViscWide>,
+	                                                                         ViscWide::kWarps * kWarp,
+	                                                                         visc_smem_bytes<ViscWide>());
 	if (e != cudaSuccess) return e;
 	if (deltaShape == kDeltaLean)
 		return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occD, k_delta<DeltaLean>, DeltaLean::kWarps * kWarp,
@@ -2747,13 +2477,10 @@ cudaError_t sweep_occupancy(int viscShape, int deltaShape, int *occV, int *occD)
 	                                                     delta_smem_bytes<DeltaWide>());
 }
 
-void launch_viscosity(int shape, int blocks, cudaStream_t st, Totals tt, Particles P, SimTables T) {
-	if (shape == kViscLean)
+void launch_viscosity(bool lean, int blocks, cudaStream_t st, Totals tt, Particles P, SimTables T) {
+	if (lean)
 		k_viscosity_multi<ViscLean>
 		    <<<blocks, ViscLean::kWarps * kWarp, sizeof(ViscMultiSmemT<ViscLean>), st>>>(tt, P, T);
-	else if (shape == kViscPair)
-		k_viscosity_pair<ViscPair>
-		    <<<blocks, ViscPair::kWarps * kWarp, sizeof(ViscPairSmemT<ViscPair>), st>>>(tt, P, T);
 	else
 		k_viscosity<ViscWide><<<blocks, ViscWide::kWarps * kWarp, visc_smem_bytes<ViscWide>(), st>>>(tt, P, T);
 }

@@ -18,17 +18,6 @@ struct ViscWide {
 struct ViscLean {
 	static constexpr int kSlots = 5, kProd = 4, kWarps = 1 + kProd, kGeom = 192, kMinBlocks = 3;
 };
-// Paired lean viscosity: kSlots tasks per block, two chain lanes of warp 0
-// per task (head of a particle beside the tail of the previous one) and one
-// producer warp per task (k_viscosity_pair).
-struct ViscPair {
-	static constexpr int kSlots = 4, kProd = 4, kWarps = 1 + kProd, kGeom = 192, kMinBlocks = 3;
-};
-// Viscosity shapes by index; sph_set_sweep_shape names them 4 (wide),
-// 5 (lean) and 6 (paired).
-constexpr int kViscShapes = 3;
-constexpr int kViscWide = 0, kViscLean = 1, kViscPair = 2;
-constexpr int visc_shape_id(int shape) { return shape == kViscLean ? 5 : (shape == kViscPair ? 6 : 4); }
 // Delta sweep.  Pipelined shapes run kWarps - 1 producer warps and one
 // summer warp per task; the others relax one particle at a time on the
 // whole block.  kChainW in-range pairs are buffered per warp; a particle's
@@ -87,8 +76,8 @@ struct DensWarp;
 
 // The two ordered sweeps in a chosen shape (lean or wide), and their set-up.
 cudaError_t sweep_attributes();
-cudaError_t sweep_occupancy(int viscShape, int deltaShape, int *occV, int *occD);
-void launch_viscosity(int shape, int blocks, cudaStream_t st, Totals tt, Particles P, SimTables T);
+cudaError_t sweep_occupancy(bool viscLean, int deltaShape, int *occV, int *occD);
+void launch_viscosity(bool lean, int blocks, cudaStream_t st, Totals tt, Particles P, SimTables T);
 void launch_delta(int shape, int blocks, cudaStream_t st, Totals tt, Particles Q, SimTables T);
 size_t dens_smem_bytes();
 size_t springs_smem_bytes();

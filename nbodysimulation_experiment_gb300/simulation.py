@@ -125,11 +125,10 @@ class SpringParams(ctypes.Structure):
 
 
 SPRING_SLOTS = 16
-#: The values ``sph_set_sweep_shape`` accepts for the ordered sweeps' launch
-#: shapes (csrc/sph_kernels.cuh): viscosity (wide, lean, paired lean) and
-#: delta (wide, lean, mid, tri, quad); the delta shapes are named by their
-#: warps per block.
-VISC_WARPS = (4, 5, 6)
+#: Warps per task of the ordered sweeps' launch shapes, (wide, lean) and for
+#: the delta sweep (wide, lean, mid, tri, quad): the values
+#: ``sph_set_sweep_shape`` accepts (csrc/sph_kernels.cuh).
+VISC_WARPS = (4, 5)
 DELTA_WARPS = (12, 2, 8, 3, 4)
 
 

@@ -167,8 +167,8 @@ def _run_with_shape(scene, shape, steps):
                                    (VISC_WARPS[1], 152, DELTA_WARPS[0], 152),
                                    (VISC_WARPS[0], 152 * 3, DELTA_WARPS[1], 152 * 5),
                                    (VISC_WARPS[0], 152, DELTA_WARPS[2], 304),
-                                   (VISC_WARPS[2], 152 * 3, DELTA_WARPS[3], 152 * 5),
-                                   (VISC_WARPS[2], 152, DELTA_WARPS[4], 152 * 4)])
+                                   (VISC_WARPS[1], 152 * 3, DELTA_WARPS[3], 152 * 5),
+                                   (VISC_WARPS[0], 152, DELTA_WARPS[4], 152 * 4)])
 def test_sweep_shapes_give_identical_results(shape):
     """Lean, mid and wide sweeps, with any resident block count, compute the
     same update."""
@@ -178,15 +178,14 @@ def test_sweep_shapes_give_identical_results(shape):
     _assert_same_state(got, want, str(shape))
 
 
-@pytest.mark.parametrize("visc", [1, 2])
-def test_lean_viscosity_with_long_pair_lists(visc):
-    """Particles with more in-range pairs than the lean and paired sweeps'
-    geometry buffers (spacing h/10: ~300 pairs) take the inline path, with
-    the same result."""
+def test_lean_viscosity_with_long_pair_lists():
+    """Particles with more in-range pairs than the lean sweep's geometry
+    buffer (spacing h/10: ~300 pairs) take the inline path, with the same
+    result."""
     h = float(scenes.H)
     pos = scenes.jittered_lattice(28, 28, -1.4, -2.5, spacing=h / 10, jitter=h / 200, seed=3)
     scene = scenes.Scene("dense", scenes.REF_WIDTH, scenes.REF_HEIGHT, pos,
                          scenes.box_planes(scenes.REF_WIDTH, scenes.REF_HEIGHT))
     want = _run_with_shape(scene, None, 6)
-    got = _run_with_shape(scene, (VISC_WARPS[visc], None, DELTA_WARPS[1], None), 6)
+    got = _run_with_shape(scene, (VISC_WARPS[1], None, DELTA_WARPS[1], None), 6)
     _assert_same_state(got, want, "dense")
