@@ -553,8 +553,9 @@ def learned_quality(pkg, scene, model, device, frame, sub, rollout_frames):
     for (four updates of dt/4), on the benchmark's scene: (a) per frame, from
     the same state, the RMS and largest position difference in units of h
     (the network's correction applied without the judge); (b) a free rollout
-    of learned frames against one of plain frames from the same start: mean
-    density deviation, kinetic energy and density histogram at the end."""
+    of learned frames (under the benchmark's judge) against one of plain
+    frames from the same start: mean density deviation, kinetic energy and
+    density histogram at the end."""
     from nbodysimulation_experiment_gb300 import scenes as sc_mod  # noqa: F401
     h = float(scene.params[0])
     rho0 = float(scene.params[4])
@@ -583,12 +584,14 @@ def learned_quality(pkg, scene, model, device, frame, sub, rollout_frames):
             worst.append(float(d.max()))
     sim.close()
 
-    # (b) free rollouts from the same start
+    # (b) free rollouts from the same start, the learned one under the judge
+    taken = [0]
+
     def rollout(use_network):
         sim = fresh()
         for _ in range(rollout_frames):
             if use_network:
-                sim.learned_frame(model, frame, sub, bound=1e30)
+                taken[0] += int(sim.learned_frame(model, frame, sub, bound=0.01)[0])
             else:
                 for _ in range(sub):
                     sim.update(frame / sub)
@@ -602,7 +605,7 @@ def learned_quality(pkg, scene, model, device, frame, sub, rollout_frames):
 
     lr, pr = rollout(True), rollout(False)
     return {"per_frame_rms_position_error_h": float(np.mean(rms)), "per_frame_max_position_error_h": max(worst),
-            "rollout_frames": rollout_frames,
+            "rollout_frames": rollout_frames, "rollout_frames_taken_by_network": taken[0],
             "rollout_learned": {k: v for k, v in lr.items() if k != "hist"},
             "rollout_plain": {k: v for k, v in pr.items() if k != "hist"},
             "rollout_density_histogram_l1": float(np.abs(lr["hist"] - pr["hist"]).sum())}

@@ -1066,6 +1066,12 @@ int sph_learned_frame(sph_sim *s, sph_mpnn *m, float dt, int substeps, float bou
 		    tt, s->buf[s->cur].view(), s->lu, tables(s));
 		SPH_LAUNCHED(s);
 		rc = density_error(s, &err);
+		// A corrected frame that packs a neighbourhood beyond capacity is as
+		// bad as a frame can be: the judge rejects it.
+		if (rc == SPH_ERR_DEVICE_OVERFLOW) {
+			err = INFINITY;
+			rc = SPH_OK;
+		}
 		if (rc) return rc;
 		// The judge: the correction stands if it leaves the mean density
 		// deviation of the plain update it corrects at most `bound` (a
