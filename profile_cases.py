@@ -95,9 +95,9 @@ def learned_frame(frames: int = 3) -> None:
 
 def block(side: int = 512, updates: int = 3) -> None:
     """A side x side jittered block with springs on (yield 0.1, plasticity
-    0.3, stiffness 0.3, at most 16), in the lean sweep shapes the autotuner
-    picks for the 1,048,576-particle block (5-warp viscosity at 3 blocks per
-    SM, 2-warp delta at 5 per SM): 3 + `updates` updates."""
+    0.3, stiffness 0.3, at most 16), in the sweep shapes the autotuner picks
+    for the 1,048,576-particle block (lean 5-warp viscosity at 3 blocks per
+    SM, pipelined 3-warp delta at 5 per SM): 3 + `updates` updates."""
     scene = scenes.block_1m() if side == 1024 else scenes.scaled_block(side, seed=3, obstacles=False)
     sim = Simulation(scene.domain())
     scene.apply(sim)
@@ -105,7 +105,7 @@ def block(side: int = 512, updates: int = 3) -> None:
     for _ in range(3):
         sim.update(float(scenes.DT))
     sms = sim.sweep_shape()[3]  # the default delta shape runs one block per SM
-    sim.set_sweep_shape((VISC_WARPS[1], 3 * sms, DELTA_WARPS[1], 5 * sms))
+    sim.set_sweep_shape((VISC_WARPS[1], 3 * sms, DELTA_WARPS[3], 5 * sms))
     for _ in range(updates):
         sim.update(float(scenes.DT))
     sim.synchronize()
@@ -125,11 +125,31 @@ def everything() -> None:
     scene = scenes.dam_break_4096()
     sim = Simulation(scene.domain())
     scene.apply(sim)
+    sim.set_springs(True, yield_ratio=0.1, plasticity=0.3, stiffness=0.3, max_per_particle=16)
     sim.update(float(scenes.DT))
     sim.read_particles(("pos", "vel"))
     sim.particle_colors()
     sim.render_points(320, 180)
+    st, spr = sim.dump_state(), sim.dump_springs()  # snapshot: device-side checks on load
+    sim.load_state(st)
+    sim.load_springs(*spr)
+    sim.set_reference_order(True)  # the reference-order sweeps
+    for _ in range(2):
+        sim.update(float(scenes.DT))
+    sim.synchronize()
     sim.close()
+    import ctypes
+    import torch
+    from nbodysimulation_experiment_gb300 import simulation as sm
+    lib = sm.load_library()
+    fn = lib.sph_density_pressure_noalloc
+    fn.argtypes = [ctypes.POINTER(sm.Domain), ctypes.POINTER(sm.Params), ctypes.c_void_p, ctypes.c_size_t,
+                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    pos = torch.from_numpy(scene.positions).cuda()
+    out = torch.empty((2, scene.n, 2), device="cuda")
+    d, p = scene.domain(), sm.Params.from_array(scene.params)
+    fn(ctypes.byref(d), ctypes.byref(p), pos.data_ptr(), scene.n, out[0].data_ptr(), out[1].data_ptr(), None)
+    torch.cuda.synchronize()
     print("all cases ran")
 
 
