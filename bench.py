@@ -589,17 +589,24 @@ def learned_quality(pkg, scene, model, device, frame, sub, rollout_frames):
 
     def rollout(use_network):
         sim = fresh()
-        for _ in range(rollout_frames):
-            if use_network:
-                taken[0] += int(sim.learned_frame(model, frame, sub, bound=0.01)[0])
-            else:
-                for _ in range(sub):
-                    sim.update(frame / sub)
+        done, failure = 0, None
+        try:
+            for _ in range(rollout_frames):
+                if use_network:
+                    taken[0] += int(sim.learned_frame(model, frame, sub, bound=0.01)[0])
+                else:
+                    for _ in range(sub):
+                        sim.update(frame / sub)
+                sim.synchronize()
+                done += 1
+        except pkg.SphError as exc:  # reported, not hidden: how far the rollout got
+            failure = str(exc)
         r = sim.read_particles(("pos", "vel", "dens"))
         sim.close()
         d = r["dens"][:, 0].astype(np.float64)
         hist, _ = np.histogram(d / rho0, bins=20, range=(0.0, 2.0))
-        return {"density_error": float(np.mean(np.abs(d - rho0)) / rho0),
+        return {"frames_completed": done, "failure": failure,
+                "density_error": float(np.mean(np.abs(d - rho0)) / rho0),
                 "kinetic_energy": float(0.5 * np.mean(np.sum(r["vel"].astype(np.float64) ** 2, axis=1))),
                 "mean_height": float(np.mean(r["pos"][:, 1])), "hist": hist / len(d)}
 

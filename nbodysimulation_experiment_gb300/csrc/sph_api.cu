@@ -1053,30 +1053,39 @@ int sph_learned_frame(sph_sim *s, sph_mpnn *m, float dt, int substeps, float bou
 		if (!rc) rc = density_error(s, &err);
 	} else {
 		// One plain update over the whole frame, corrected by the network
-		// towards the `substeps` updates it stands in for.
+		// towards the `substeps` updates it stands in for.  A capacity
+		// overflow anywhere on this path (the long plain update, or the
+		// corrected positions) rejects the learned frame: the plain frame
+		// takes over from the snapshot taken before it.
 		rc = copy_state(s, true);
 		if (!rc) rc = run_step(s, dt);
 		float err1 = 0.0f;
 		if (!rc) rc = density_error(s, &err1);
-		if (!rc) rc = learned_z0(s, sc);
-		if (!rc) rc = mpnn_forward_dev(m, learned_graph(s, sc), s->lu, s->stream);
-		if (rc) return rc;
-		const Totals tt = totals(s);
-		k_learned_finish<<<blocks_for(tt.n, kCollideThreads), kCollideThreads, 0, s->stream>>>(
-		    tt, s->buf[s->cur].view(), s->lu, tables(s));
-		SPH_LAUNCHED(s);
-		rc = density_error(s, &err);
-		// A corrected frame that packs a neighbourhood beyond capacity is as
-		// bad as a frame can be: the judge rejects it.
+		bool reject = false;
 		if (rc == SPH_ERR_DEVICE_OVERFLOW) {
-			err = INFINITY;
+			reject = true;
 			rc = SPH_OK;
 		}
 		if (rc) return rc;
+		if (!reject) {
+			rc = learned_z0(s, sc);
+			if (!rc) rc = mpnn_forward_dev(m, learned_graph(s, sc), s->lu, s->stream);
+			if (rc) return rc;
+			const Totals tt = totals(s);
+			k_learned_finish<<<blocks_for(tt.n, kCollideThreads), kCollideThreads, 0, s->stream>>>(
+			    tt, s->buf[s->cur].view(), s->lu, tables(s));
+			SPH_LAUNCHED(s);
+			rc = density_error(s, &err);
+			if (rc == SPH_ERR_DEVICE_OVERFLOW) {
+				reject = true;
+				rc = SPH_OK;
+			}
+			if (rc) return rc;
+		}
 		// The judge: the correction stands if it leaves the mean density
 		// deviation of the plain update it corrects at most `bound` (a
 		// fraction of the rest density) higher.
-		if (std::isfinite(err) && err <= err1 + bound) {
+		if (!reject && std::isfinite(err) && err <= err1 + bound) {
 			used = 1;
 		} else {
 			rc = copy_state(s, false);
