@@ -287,7 +287,8 @@ def sweep_kernels(shape):
     """Kernel names of the two ordered sweeps for a launch shape
     (viscosity warps, blocks, delta warps, blocks)."""
     visc = "k_viscosity_multi<ViscLean>" if shape[0] == 5 else "k_viscosity<ViscWide>"
-    delta = {12: "k_delta<DeltaWide>", 8: "k_delta<DeltaMid>", 2: "k_delta<DeltaLean>"}.get(shape[2], "k_delta")
+    delta = {12: "k_delta<DeltaWide>", 8: "k_delta<DeltaMid>", 2: "k_delta<DeltaLean>", 3: "k_delta<DeltaTri>",
+             4: "k_delta<DeltaQuad>"}.get(shape[2], "k_delta")
     return visc, delta
 
 

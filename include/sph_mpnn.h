@@ -75,9 +75,12 @@ int sph_mpnn_train_step(sph_mpnn *model, size_t index, float lr, float *loss);
 /* One learned frame of length frame_dt, judged by the plain method: the
  * network's correction stands if the mean |rho - rho0| / rho0 of the
  * corrected positions exceeds that of the plain update it corrects by at
- * most `bound`; otherwise the state is restored and the frame runs as
- * `substeps` plain updates of frame_dt / substeps.  Reports which ran and the
- * density error of the result.  Single-scene simulations without springs. */
+ * most `bound`, its densest neighbourhood lists at most 70% of the neighbour
+ * capacity, and no capacity overflowed on the way; otherwise the state is
+ * restored and the frame runs as `substeps` plain updates of
+ * frame_dt / substeps.  Reports which ran and the density error of the
+ * result (summed in a fixed order: the verdict is reproducible).
+ * Single-scene simulations without springs. */
 int sph_learned_frame(sph_sim *sim, sph_mpnn *model, float frame_dt, int substeps, float bound, int *used_learned,
                       float *density_error);
 

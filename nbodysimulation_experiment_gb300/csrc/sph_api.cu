@@ -162,6 +162,9 @@ struct sph_sim {
 namespace {
 
 constexpr unsigned long long kDefaultWaitLimitNs = 2000000000ull;  // 2 s per bounded wait
+// The learned frame's judge rejects a corrected frame whose longest
+// neighbour list exceeds this fraction of the neighbour capacity.
+constexpr double kLearnedCrowding = 0.7;
 
 // Text of the last failing CUDA call on this thread (sph_last_error).
 thread_local char g_last_error[256] = "";
@@ -961,10 +964,14 @@ int copy_state(sph_sim *s, bool save) {
 
 // Mean |rho - rho0| / rho0 of the canonical state's final positions (density
 // from the cell ranges, as the step computes it), on scratch arrays.
-int density_error(sph_sim *s, float *out) {
+// Mean |rho - rho0| / rho0 of the current positions (over the current cell
+// arrays) and, in *maxNb, the longest neighbour list.
+int density_error(sph_sim *s, float *out, uint32_t *maxNb = nullptr) {
 	const Scene &sc = s->scenes[0];
 	int rc = upload_scenes(s, s->tableDt > 0.0f ? s->tableDt : 1.0f);
 	if (rc) return rc;
+	const uint32_t seed[4] = {0xffffffffu, 0u, 0xffffffffu, 0u};
+	SPH_CUDA(cudaMemcpyAsync(s->lstats, seed, sizeof(seed), cudaMemcpyHostToDevice, s->stream));
 	const Totals tt = totals(s);
 	SimTables T = tables(s);
 	T.newStart = s->cellStartA;
@@ -981,10 +988,13 @@ int density_error(sph_sim *s, float *out) {
 	k_density_error_total<<<1, kErrBlocks, 0, s->stream>>>(blocks, s->lerr, s->lerr + kErrBlocks);
 	SPH_LAUNCHED(s);
 	double sum = 0.0;
+	uint32_t st[4] = {0u, 0u, 0u, 0u};
 	SPH_CUDA(cudaMemcpyAsync(&sum, s->lerr + kErrBlocks, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+	SPH_CUDA(cudaMemcpyAsync(st, s->lstats, sizeof(st), cudaMemcpyDeviceToHost, s->stream));
 	rc = check_device_errors(s);
 	if (rc) return rc;
 	*out = tt.n > 0 ? (float)(sum / ((double)tt.n * (double)sc.params.rest_density)) : 0.0f;
+	if (maxNb) *maxNb = st[1];
 	return SPH_OK;
 }
 
@@ -1075,12 +1085,19 @@ int sph_learned_frame(sph_sim *s, sph_mpnn *m, float dt, int substeps, float bou
 			k_learned_finish<<<blocks_for(tt.n, kCollideThreads), kCollideThreads, 0, s->stream>>>(
 			    tt, s->buf[s->cur].view(), s->lu, tables(s));
 			SPH_LAUNCHED(s);
-			rc = density_error(s, &err);
+			uint32_t maxNb = 0;
+			rc = density_error(s, &err, &maxNb);
 			if (rc == SPH_ERR_DEVICE_OVERFLOW) {
 				reject = true;
 				rc = SPH_OK;
 			}
 			if (rc) return rc;
+			// Local crowding does not show in the mean deviation: a frame
+			// whose densest neighbourhood lists more than kLearnedCrowding of
+			// the neighbour capacity is rejected too, so the plain method
+			// relaxes crowding before it nears the capacity.
+			const uint32_t cap = std::min<uint32_t>(sc.dom.max_neighbors, (uint32_t)kStageCap);
+			if ((double)maxNb > kLearnedCrowding * (double)cap) reject = true;
 		}
 		// The judge: the correction stands if it leaves the mean density
 		// deviation of the plain update it corrects at most `bound` (a
