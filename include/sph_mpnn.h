@@ -3,9 +3,10 @@
  *
  * A small message-passing network stands in for one frame of the plain
  * method (the reference's four Update(dt/4) substeps per frame,
- * kSPHSubsteps, sph.h:32-34 / app.cpp:231-233).  Its dense layers run on the
- * GB300's 5th-generation tensor cores (tcgen05, BF16 operands, FP32
- * accumulation); the plain step stays its judge and fallback.
+ * kSPHSubsteps, sph.h:32-34 / app.cpp:231-233).  Its layers run on the
+ * GB300's 5th-generation tensor cores (tcgen05; BF16 operands for the dense
+ * layers, TF32 for the edge layer; FP32 accumulation); the plain step stays
+ * its judge and fallback.
  */
 #ifndef SPH_MPNN_H
 #define SPH_MPNN_H
@@ -50,6 +51,18 @@ int sph_mpnn_param_count(size_t *out);
  * W4[2][128], b4[2].  Setting them resets the optimizer state. */
 int sph_mpnn_get_params(sph_mpnn *model, float *out);
 int sph_mpnn_set_params(sph_mpnn *model, const float *in);
+
+/* Where the edge MLP's first layer (6 -> 128, summed over a particle's
+ * edges) runs in the forward pass: path 0 (default) on the tensor cores
+ * (per tile of edges, a kind::tf32 MMA computes W1 e + b1 for every edge
+ * into tensor memory, the ReLU is applied and rounded to BF16 in place, and
+ * a kind::f16 MMA with that operand read from tensor memory sums it per
+ * particle against a 0/1 segment matrix), path 1 on the CUDA cores (FP32
+ * FMAs).  Both round the edge features, W1 and b1 to TF32 and each edge's
+ * activation to BF16, so they compute the same function up to summation
+ * order. */
+int sph_mpnn_set_edge_path(sph_mpnn *model, int path);
+int sph_mpnn_get_edge_path(sph_mpnn *model, int *path);
 
 /* Training samples, stored on the device.  sph_mpnn_capture takes one from
  * `sim` (a single-scene simulation in a canonical state, i.e. after an

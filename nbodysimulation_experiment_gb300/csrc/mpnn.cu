@@ -87,6 +87,8 @@ struct sph_mpnn {
 	float *dX = nullptr, *dH = nullptr;
 	float *loss = nullptr;
 	uint32_t *error = nullptr;
+	int edgePath = 0;  // 0: edge layer on the tensor cores, 1: on the CUDA cores
+	int sms = 0;
 	std::vector<Sample> samples;
 };
 
@@ -129,8 +131,14 @@ int forward(sph_mpnn *m, const MpnnGraph &G, bool training, cudaStream_t st) {
 	const float2 *zin = G.z0;
 	for (int r = 0; r < kRounds; ++r) {
 		const float *P = m->params + (size_t)r * kRoundParams;
-		k_mpnn_edge_fwd<<<edge_blocks(G), kEdgeWarps * kWarp, mpnn_edge_smem(false), st>>>(G, P + kOffW1, P + kOffB1, zin,
-		                                                                          m->Hb[r], m->degS, np, m->error);
+		if (m->edgePath == 0) {
+			const int grid = std::max(1, std::min(G.gx * G.gy, mpnn_edge_tc_blocks_per_sm() * m->sms));
+			k_mpnn_edge_fwd_tc<<<grid, 128, mpnn_edge_tc_smem(), st>>>(G, P + kOffW1, P + kOffB1, zin, m->Hb[r],
+			                                                          m->degS, np, m->error);
+		} else {
+			k_mpnn_edge_fwd<<<edge_blocks(G), kEdgeWarps * kWarp, mpnn_edge_smem(false), st>>>(
+			    G, P + kOffW1, P + kOffB1, zin, m->Hb[r], m->degS, np, m->error);
+		}
 		MPNN_CUDA(cudaGetLastError());
 		if (training) {
 			dim3 tg(blocks(kHidden, 32), blocks(np, 32));
@@ -357,7 +365,10 @@ int sph_mpnn_create(int device, size_t max_particles, uint64_t seed, sph_mpnn **
 	if (cudaFuncSetAttribute(k_mpnn_edge_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize,
 	                         (int)mpnn_edge_smem(false)) != cudaSuccess ||
 	    cudaFuncSetAttribute(k_mpnn_edge_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize,
-	                         (int)mpnn_edge_smem(true)) != cudaSuccess)
+	                         (int)mpnn_edge_smem(true)) != cudaSuccess ||
+	    cudaFuncSetAttribute(k_mpnn_edge_fwd_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+	                         (int)mpnn_edge_tc_smem()) != cudaSuccess ||
+	    cudaDeviceGetAttribute(&m->sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
 		return fail(SPH_ERR_CUDA);
 	if ((rc = zalloc(&m->params, kParams)) || (rc = zalloc(&m->grads, kParams)) || (rc = zalloc(&m->adamM, kParams)) ||
 	    (rc = zalloc(&m->adamV, kParams)) || (rc = zalloc(&m->W2b, kRounds * kHidden * kHidden)) ||
@@ -419,6 +430,19 @@ int sph_mpnn_set_params(sph_mpnn *m, const float *in) {
 	m->adamStep = 0;
 	int rc = refresh(m, m->stream);
 	return rc ? rc : check_error(m, m->stream);
+}
+
+int sph_mpnn_set_edge_path(sph_mpnn *m, int path) {
+	if (!m || (path != 0 && path != 1)) return SPH_ERR_INVALID_ARGUMENT;
+	MPNN_CUDA(cudaStreamSynchronize(m->stream));
+	m->edgePath = path;
+	return SPH_OK;
+}
+
+int sph_mpnn_get_edge_path(sph_mpnn *m, int *path) {
+	if (!m || !path) return SPH_ERR_INVALID_ARGUMENT;
+	*path = m->edgePath;
+	return SPH_OK;
 }
 
 int sph_mpnn_sample_count(sph_mpnn *m, size_t *out) {

@@ -81,9 +81,13 @@ struct MpnnGraph {
 
 constexpr int kEdgeWarps = 4;
 size_t mpnn_edge_smem(bool backward);
+size_t mpnn_edge_tc_smem();
+int mpnn_edge_tc_blocks_per_sm();
 
 __global__ void k_mpnn_edge_fwd(MpnnGraph G, const float *W1, const float *b1, const float2 *z, __nv_bfloat16 *Hb,
                                 float *degS, int np, uint32_t *error);
+__global__ void k_mpnn_edge_fwd_tc(MpnnGraph G, const float *W1, const float *b1, const float2 *z,
+                                   __nv_bfloat16 *Hb, float *degS, int np, uint32_t *error);
 __global__ void k_mpnn_edge_bwd(MpnnGraph G, const float *W1, const float *b1, const float2 *z, const float *dH,
                                 float2 *dzEdge, float *gW1, float *gb1, int needDz, uint32_t *error);
 __global__ void k_mpnn_x3_tail(const float2 *z, __nv_bfloat16 *X3b, __nv_bfloat16 *X3f, int np, int ldf);

@@ -245,6 +245,8 @@ def load_library(build_if_missing: bool = True):
         "sph_mpnn_param_count": [P(_c.c_size_t)],
         "sph_mpnn_get_params": [vp, vp],
         "sph_mpnn_set_params": [vp, vp],
+        "sph_mpnn_set_edge_path": [vp, _c.c_int],
+        "sph_mpnn_get_edge_path": [vp, P(_c.c_int)],
         "sph_mpnn_capture": [vp, vp, _c.c_float, _c.c_int],
         "sph_mpnn_sample_count": [vp, P(_c.c_size_t)],
         "sph_mpnn_clear_samples": [vp],
@@ -289,7 +291,7 @@ C_SYMBOLS = (
     "sph_use_graphs", "sph_autotune", "sph_set_reference_order", "sph_get_reference_order",
     "sph_set_wait_limit", "sph_test_hold_task", "sph_get_sweep_shape", "sph_set_sweep_shape", "sph_set_springs", "sph_get_spring_count", "sph_dump_springs", "sph_load_springs",
     "sph_mpnn_create", "sph_mpnn_destroy", "sph_mpnn_param_count", "sph_mpnn_get_params", "sph_mpnn_set_params",
-    "sph_mpnn_capture", "sph_mpnn_sample_count", "sph_mpnn_clear_samples", "sph_mpnn_sample_info",
+    "sph_mpnn_set_edge_path", "sph_mpnn_get_edge_path", "sph_mpnn_capture", "sph_mpnn_sample_count", "sph_mpnn_clear_samples", "sph_mpnn_sample_info",
     "sph_mpnn_read_sample", "sph_mpnn_eval", "sph_mpnn_gradient", "sph_mpnn_train_step", "sph_learned_frame",
     "sph_batch_create", "sph_batch_scene_count", "sph_batch_read_particles", "sph_batch_get_stats",
     "sph_batch_state_info", "sph_batch_dump_state",
@@ -849,6 +851,19 @@ class Mpnn:
         p = np.ascontiguousarray(p, np.float32)
         assert p.size == self.param_count()
         self._call("sph_mpnn_set_params", p.ctypes.data)
+
+    #: Edge-layer paths of ``sph_mpnn_set_edge_path``.
+    EDGE_TENSOR_CORES, EDGE_CUDA_CORES = 0, 1
+
+    @property
+    def edge_path(self) -> int:
+        out = _c.c_int()
+        self._call("sph_mpnn_get_edge_path", _c.byref(out))
+        return out.value
+
+    @edge_path.setter
+    def edge_path(self, path: int) -> None:
+        self._call("sph_mpnn_set_edge_path", int(path))
 
     def capture(self, sim: Simulation, frame_dt: float, substeps: int = 4) -> None:
         _check(self._lib.sph_mpnn_capture(sim._h, self._h, float(np.float32(frame_dt)), int(substeps)),

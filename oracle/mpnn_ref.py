@@ -13,8 +13,11 @@ Network (per round r = 0, 1, separate weights):
     c_i      = relu(W3 [M_i, z_i, 0...] + b3)                       (128; input padded to 144)
     z_i     += W4 c_i + b4                                          (2)
 with z^0 = v dt / h, output u = z^2 - z^0 and loss mean_i |u_i - t_i|^2.
-``bf16=True`` rounds where the GPU stores BF16 (H, [M, z], c, the GEMM
-weights W2 and W3, and in the backward pass da3 and dM).
+``emulate_bf16=True`` rounds where the GPU rounds: to BF16 where it
+stores BF16 (H, [M, z], c, the GEMM weights W2 and W3, and in the backward
+pass da3 and dM, and each edge's activation relu(W1 e + b1) before the
+per-particle sum), to TF32 the edge layer's inputs (the edge features, W1
+and b1, which the tensor cores read as TF32).
 """
 from __future__ import annotations
 
@@ -63,6 +66,17 @@ def bf16(x: np.ndarray) -> np.ndarray:
     return u.astype(np.uint32).view(np.float32).astype(np.float64)
 
 
+def tf32(x: np.ndarray) -> np.ndarray:
+    """Round to TF32 (10 explicit mantissa bits), to nearest with ties away
+    from zero (PTX cvt.rna.tf32.f32), through float32."""
+    f = np.ascontiguousarray(x, np.float32)
+    u = f.view(np.uint32).astype(np.uint64)
+    mag = u & 0x7FFFFFFF
+    mag = (mag + 0x1000) & 0x7FFFE000
+    u = (u & 0x80000000) | mag
+    return u.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
 def edges(pos, cell_start, cell_count, gx: int, gy: int, h: float, cell_of) -> Tuple[np.ndarray, np.ndarray]:
     """Directed edges (i, j) in the GPU's enumeration order: particle i's
     3x3 block of cells y-major, each cell in number order."""
@@ -91,6 +105,7 @@ def edges(pos, cell_start, cell_count, gx: int, gy: int, h: float, cell_of) -> T
 def forward(flat, pos, z0, I, J, h, emulate_bf16=False):
     P = unpack(np.asarray(flat, np.float64))
     rnd = bf16 if emulate_bf16 else (lambda a: a)
+    rnd_edge = tf32 if emulate_bf16 else (lambda a: a)
     n = len(pos)
     pos = pos.astype(np.float64)
     d = pos[J] - pos[I]
@@ -102,9 +117,9 @@ def forward(flat, pos, z0, I, J, h, emulate_bf16=False):
         p = P[rd]
         dz = z[J] - z[I]
         q = r / h
-        e = np.stack([d[:, 0] / h, d[:, 1] / h, q, dz[:, 0], dz[:, 1], (1 - q) ** 2], 1)
-        a = e @ p["W1"].T + p["b1"]
-        act = np.maximum(a, 0)
+        e = rnd_edge(np.stack([d[:, 0] / h, d[:, 1] / h, q, dz[:, 0], dz[:, 1], (1 - q) ** 2], 1))
+        a = e @ rnd_edge(p["W1"]).T + rnd_edge(p["b1"])
+        act = rnd(np.maximum(a, 0))
         H = np.zeros((n, HIDDEN))
         np.add.at(H, I, act)
         H = rnd(H / S)
@@ -132,6 +147,7 @@ def backward(flat, cache, u, target, emulate_bf16=False) -> np.ndarray:
     grad = np.zeros(param_count())
     G = unpack(grad)
     rnd = bf16 if emulate_bf16 else (lambda a: a)
+    rnd_edge = tf32 if emulate_bf16 else (lambda a: a)
     I, J, deg = cache["I"], cache["J"], cache["deg"]
     n = len(u)
     dz = 2.0 * (u - target) / n
@@ -153,7 +169,7 @@ def backward(flat, cache, u, target, emulate_bf16=False) -> np.ndarray:
         da = (dH[I] / S) * (a > 0)
         g["W1"][...] = da.T @ e
         g["b1"][...] = da.sum(0)
-        de = da @ p["W1"]
+        de = da @ rnd_edge(p["W1"])
         dz_edge = np.zeros((n, 2))
         np.add.at(dz_edge, J, de[:, 3:5])
         np.add.at(dz_edge, I, -de[:, 3:5])

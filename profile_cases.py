@@ -7,6 +7,7 @@ inputs larger than L2 but a few hundred MB on the device at most).
     python profile_cases.py mpnn
     python profile_cases.py batched
     python profile_cases.py learned_frame
+    python profile_cases.py learned_dam    # 262,144-particle dam break, learned frames
     python profile_cases.py block [side]   # side x side block, springs on, lean sweep shapes
     python profile_cases.py all            # every kernel of the library, small sizes
 """
@@ -93,6 +94,24 @@ def learned_frame(frames: int = 3) -> None:
     sim.close()
 
 
+def learned_dam(frames: int = 3) -> None:
+    """Learned frames (untrained network, judge on at a bound that accepts
+    every frame) on the 262,144-particle dam break with obstacles, the
+    benchmark's learned-frame scene, after 4 plain updates."""
+    scene = scenes.dam_break_262144()
+    sim = Simulation(scene.domain())
+    scene.apply(sim)
+    for _ in range(4):
+        sim.update(float(scenes.DT) / 4)
+    model = Mpnn(scene.n + 128, seed=2)
+    for _ in range(frames):
+        sim.learned_frame(model, float(scenes.DT), 4, bound=1e9)
+    sim.synchronize()
+    print("frames", frames)
+    model.close()
+    sim.close()
+
+
 def block(side: int = 512, updates: int = 3) -> None:
     """A side x side jittered block with springs on (yield 0.1, plasticity
     0.3, stiffness 0.3, at most 16), in the sweep shapes the autotuner picks
@@ -154,7 +173,7 @@ def everything() -> None:
 
 
 CASES = {"plain": plain, "springs": springs, "mpnn": mpnn, "batched": batched, "learned_frame": learned_frame,
-         "block": block, "all": everything}
+         "learned_dam": learned_dam, "block": block, "all": everything}
 
 if __name__ == "__main__":
     CASES[sys.argv[1]](*[int(a) for a in sys.argv[2:]])

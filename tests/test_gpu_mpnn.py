@@ -42,10 +42,13 @@ def _oracle_case(sample):
     return I, J
 
 
-def test_forward_and_gradients_match_oracle():
+@pytest.mark.parametrize("edge_path", [pkg.Mpnn.EDGE_TENSOR_CORES, pkg.Mpnn.EDGE_CUDA_CORES])
+def test_forward_and_gradients_match_oracle(edge_path):
     scene = scenes.scaled_block(20, seed=3)
     sim = _sim(scene)
     model = pkg.Mpnn(4096, seed=11)
+    assert model.edge_path == pkg.Mpnn.EDGE_TENSOR_CORES  # the default
+    model.edge_path = edge_path
     p = model.get_params()
     # Nonzero biases so that every parameter block is exercised.
     p = p + np.random.default_rng(0).normal(0, 0.02, p.shape).astype(np.float32)
@@ -68,6 +71,44 @@ def test_forward_and_gradients_match_oracle():
             den = np.linalg.norm(gr[name])
             assert den > 0, (rd, name)
             assert num / den < GRAD_TOL, (rd, name, num / den)
+    model.close()
+    sim.close()
+
+
+def test_edge_layer_paths_agree_on_dense_and_isolated_particles():
+    """The tensor-core edge layer against the CUDA-core one and the oracle
+    on a dense cluster (spacing h/9: ~250 edges per particle, so a
+    particle's run of columns spans two or three 128-column tiles, and ~80
+    particles per cell, so a cell takes ten batches) plus three isolated
+    particles (no edges: H = 0).  A frame of 1e-6 s keeps the captured
+    positions at the lattice."""
+    h = float(scenes.H)
+    sim = pkg.Simulation(pkg.reference_domain())
+    sim.set_params(pkg.Params.from_array(scenes.scenario_params()))
+    for nx, ny, d in scenes.box_planes(scenes.REF_WIDTH, scenes.REF_HEIGHT):
+        sim.add_plane((nx, ny), d)
+    dense = scenes.jittered_lattice(36, 36, -3.0, -2.0, spacing=np.float32(h / 9.0), jitter=np.float32(0.02 * h), seed=5)
+    lone = np.array([[3.0, 2.0], [3.8, -2.0], [4.5, 0.5]], np.float32)
+    sim.add_particles(np.concatenate([dense, lone]))
+    sim.update(1e-6)
+    model = pkg.Mpnn(4096, seed=12)
+    p = model.get_params()
+    model.set_params(p + np.random.default_rng(1).normal(0, 0.02, p.shape).astype(np.float32))
+    model.capture(sim, 1e-6, SUBSTEPS)
+    s = model.sample(0)
+    I, J = _oracle_case(s)
+    deg = np.bincount(I, minlength=len(s["pos"]))
+    assert deg.max() > 2 * 128 and np.count_nonzero(deg == 0) == 3, (deg.max(), np.count_nonzero(deg == 0))
+    u_ref, _ = mpnn_ref.forward(model.get_params().astype(np.float64), s["pos"], s["z0"], I, J, s["h"],
+                                emulate_bf16=True)
+    out = {}
+    for path in (pkg.Mpnn.EDGE_TENSOR_CORES, pkg.Mpnn.EDGE_CUDA_CORES):
+        model.edge_path = path
+        out[path] = model.eval(0, want_u=True)[1].astype(np.float64)
+        err = np.linalg.norm(out[path] - u_ref) / np.linalg.norm(u_ref)
+        assert err < FWD_TOL, (path, err)
+    diff = np.linalg.norm(out[0] - out[1]) / np.linalg.norm(out[1])
+    assert diff < 5e-3, diff  # same function, different summation order (then BF16 H)
     model.close()
     sim.close()
 

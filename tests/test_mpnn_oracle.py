@@ -78,3 +78,19 @@ def test_bf16_rounding():
     assert r[0] == 1.0 and r[1] == 1.0  # ties to even
     assert r[2] == 1.0078125
     assert abs(r[3] - -3.140625) < 1e-9
+
+
+def test_tf32_rounding():
+    """To nearest with ties away from zero, 10 explicit mantissa bits
+    (cvt.rna.tf32.f32): the low 13 bits of the float32 are zero."""
+    ulp = 2.0 ** -10
+    x = np.array([1.0, 1.0 + ulp / 2, -(1.0 + ulp / 2), 1.0 + 1.5 * ulp, 1.0 + ulp / 2 - 2.0 ** -20, 0.1, 0.0])
+    r = mpnn_ref.tf32(x)
+    assert r[0] == 1.0
+    assert r[1] == 1.0 + ulp and r[2] == -(1.0 + ulp)  # ties away from zero
+    assert r[3] == 1.0 + 2 * ulp
+    assert r[4] == 1.0
+    assert abs(r[5] - 0.1) <= 0.1 * ulp / 2 and r[6] == 0.0
+    bits = np.asarray(r, np.float32).view(np.uint32)
+    assert np.all(bits & 0x1FFF == 0)
+    assert np.array_equal(mpnn_ref.tf32(r), r)
