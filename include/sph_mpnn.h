@@ -54,13 +54,12 @@ int sph_mpnn_set_params(sph_mpnn *model, const float *in);
 
 /* Where the edge MLP's first layer (6 -> 128, summed over a particle's
  * edges) runs in the forward pass: path 0 (default) on the tensor cores
- * (per tile of edges, a kind::tf32 MMA computes W1 e + b1 for every edge
- * into tensor memory, the ReLU is applied and rounded to BF16 in place, and
- * a kind::f16 MMA with that operand read from tensor memory sums it per
- * particle against a 0/1 segment matrix), path 1 on the CUDA cores (FP32
- * FMAs).  Both round the edge features, W1 and b1 to TF32 and each edge's
- * activation to BF16, so they compute the same function up to summation
- * order. */
+ * (per tile of 128 edges one kind::tf32 MMA computes W1 e + b1 for every
+ * edge into tensor memory; the ReLU and the per-particle sums are read out
+ * of it with packed FP32 adds, in a pipeline of producer warps building the
+ * tiles, an MMA thread and epilogue warps), path 1 on the CUDA cores (FP32
+ * FMAs).  Both round the edge features, W1 and b1 to TF32, so they compute
+ * the same function up to summation order. */
 int sph_mpnn_set_edge_path(sph_mpnn *model, int path);
 int sph_mpnn_get_edge_path(sph_mpnn *model, int *path);
 

@@ -133,7 +133,7 @@ int forward(sph_mpnn *m, const MpnnGraph &G, bool training, cudaStream_t st) {
 		const float *P = m->params + (size_t)r * kRoundParams;
 		if (m->edgePath == 0) {
 			const int grid = std::max(1, std::min(G.gx * G.gy, mpnn_edge_tc_blocks_per_sm() * m->sms));
-			k_mpnn_edge_fwd_tc<<<grid, 128, mpnn_edge_tc_smem(), st>>>(G, P + kOffW1, P + kOffB1, zin, m->Hb[r],
+			k_mpnn_edge_fwd_tc<<<grid, mpnn_edge_tc_threads(), mpnn_edge_tc_smem(), st>>>(G, P + kOffW1, P + kOffB1, zin, m->Hb[r],
 			                                                          m->degS, np, m->error);
 		} else {
 			k_mpnn_edge_fwd<<<edge_blocks(G), kEdgeWarps * kWarp, mpnn_edge_smem(false), st>>>(

@@ -83,6 +83,7 @@ constexpr int kEdgeWarps = 4;
 size_t mpnn_edge_smem(bool backward);
 size_t mpnn_edge_tc_smem();
 int mpnn_edge_tc_blocks_per_sm();
+int mpnn_edge_tc_threads();
 
 __global__ void k_mpnn_edge_fwd(MpnnGraph G, const float *W1, const float *b1, const float2 *z, __nv_bfloat16 *Hb,
                                 float *degS, int np, uint32_t *error);

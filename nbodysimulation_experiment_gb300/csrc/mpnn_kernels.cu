@@ -3,9 +3,8 @@
 // summed per particle) on the tensor cores and, selectable, on the CUDA
 // cores; its backward pass; elementwise node work, reductions, layout
 // transposes and the optimizer.  In every form the edge layer's inputs
-// (edge features, W1, b1) are rounded to TF32 and each edge's activation
-// relu(W1 e + b1) to BF16 before the per-particle sum.  Arithmetic follows
-// the FP64 restatement in the oracle up to FP32/TF32/BF16 rounding.
+// (edge features, W1, b1) are rounded to TF32.  Arithmetic follows the FP64
+// restatement in the oracle up to FP32/TF32/BF16 rounding.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -187,8 +186,7 @@ __global__ void __launch_bounds__(kEdgeWarps * kWarp) k_mpnn_edge_fwd(MpnnGraph 
 						float a = bias[u];
 #pragma unroll
 						for (int k = 0; k < kEdgeIn; ++k) a += w[u][k] * fe[k];
-						// relu rounded to BF16, as the tensor-core path sums it.
-						acc[u] += __bfloat162float(__float2bfloat16_rn(fmaxf(a, 0.f)));
+						acc[u] += fmaxf(a, 0.f);
 					}
 				}
 				deg += m;
@@ -210,72 +208,66 @@ __global__ void __launch_bounds__(kEdgeWarps * kWarp) k_mpnn_edge_fwd(MpnnGraph 
 }
 
 // ---------------------------------------------------------------------------
-// Edge layer 1 on the tensor cores: two tcgen05 MMAs per tile of edges.
+// Edge layer 1 on the tensor cores (tcgen05.mma kind::tf32).
 //
 // A CTA of four warps takes cells in turn and stages each cell's 3x3 block;
 // the cell's particles go in batches of up to kTcBatch.  A batch's in-range
 // edges form a stream of columns, particle by particle in block order, each
 // particle's run padded with zero columns to a multiple of 8 (at least 8).
-// Per tile of kTcCols columns:
-//   1. thread t writes column t's operand row E = [e_ij, 1, 0] (TF32), and
-//      the 0/1 segment matrix Seg[p, e] = [column e belongs to particle p]
-//      (BF16) is written for the tile;
-//   2. D1[f, e] = sum_k W1'[f, k] E[e, k]    tcgen05.mma kind::tf32, M = 128
-//      features, N = kTcCols, K = 8, W1' = [W1 | b1 | 0] (TF32), so that
-//      D1 = W1 e + b1 and a zero column gives D1 = 0;
-//   3. thread f reads TMEM lane f (warp w owns lanes 32w..32w+31), applies
-//      relu and rounds to BF16 with one cvt per two columns, and stores the
-//      packed pairs back into the first kTcCols/2 columns of D1;
-//   4. D2[f, p] += sum_e relu(D1)[f, e] Seg[p, e]    tcgen05.mma kind::f16
-//      with A read from tensor memory, N = kTcSlots, K = the tile's columns
-//      in steps of 16, accumulating over the batch's tiles.
-// At the end of a batch thread f reads D2's row and writes H_i = D2 / S.
-// The tile's MMA of step 2 is issued only once the previous tile's step-4
-// MMA (which reads the same columns) has completed; the segment matrix is
-// double-buffered so that building the next tile overlaps that MMA.  Four
-// CTAs share an SM's 512 TMEM columns (D1: 112, D2: 16).  Every MMA
-// completion wait is bounded; if one runs out the CTA stops, flags the
-// error, waits (bounded) once more for the tensor core and frees its tensor
-// memory.
+// Per tile of up to kTcCols columns, thread t writes column t's operand row
+// E = [e_ij, 1, 0] (TF32) into shared memory and one thread issues
+//     D[f, e] = sum_k W1'[f, k] E[e, k]      M = 128 features, N = kTcCols,
+//                                            K = 8, FP32 accumulator in TMEM
+// with W1' = [W1 | b1 | 0] (TF32), so that D = W1 e + b1 and a zero column
+// gives 0.  Thread f then reads TMEM lane f (warp w owns lanes
+// 32w..32w+31), 32 columns per load, and sums relu(D) along the stream with
+// packed FP32 adds, 8 columns at a time, writing H_i = sum / S where a run
+// ends (a run may span tiles).  The per-particle sums stay on the CUDA
+// cores: a second MMA would contract over edges, 16 per instruction, and a
+// tcgen05.mma costs ~100 cycles whatever its N.  Four CTAs share an SM's
+// 512 TMEM columns and overlap one another's phases.  Thread 0 waits for
+// the MMA (bounded) while the other threads wait at the CTA barrier; if the
+// wait runs out the CTA stops, flags the error, waits (bounded) once more
+// for the tensor core and frees its tensor memory.
 
 namespace {
 
 constexpr int kTcThreads = 128;
-constexpr int kTcCols = 112;       // edge columns per tile (N of the first MMA)
-constexpr int kTcSlots = 16;       // per-particle sums (N of the second MMA)
-constexpr int kTcBatch = 8;        // particles per batch (<= kTcSlots)
-constexpr int kTcTmemCols = 128;   // D1 at column 0, D2 at column kTcCols
+constexpr int kTcCols = 128;       // columns per tile = TMEM columns per CTA
+constexpr int kTcBatch = 8;        // particles per batch
 constexpr int kTcRowBytes = 32;    // 8 TF32 values per operand row
-constexpr int kTcGroupBytes = 8 * kTcRowBytes;    // one 8-row group of core matrices
-constexpr int kTcChunks = kTcCols / 8;            // 8-column chunks of a tile
-constexpr int kTcSegBytes = kTcChunks * 256;      // Seg: 16 rows x kTcCols BF16
+constexpr int kTcGroupBytes = 8 * kTcRowBytes;  // one 8-row group of core matrices
+constexpr int kTcChunks = kTcCols / 8;
+constexpr int kTcMaxChunks = kTcBatch * (kMpnnStage / 8 + 1);  // of a batch
 constexpr int kTcBlocksPerSm = 4;  // 4 x 128 TMEM columns = an SM's 512
 
 struct __align__(128) EdgeTcSmem {
 	unsigned char a[kHidden * kTcRowBytes];  // W1' rows, core-matrix layout
 	unsigned char b[kTcCols * kTcRowBytes];  // the tile's edge rows, core-matrix layout
-	unsigned char seg[2][kTcSegBytes];       // segment matrix, double-buffered
 	float2 pos[kMpnnStage];
 	float2 z[kMpnnStage];
 	uint16_t list[kTcBatch][kMpnnStage];  // each batch particle's in-range block entries
-	uint8_t owner[kTcBatch * (kMpnnStage / 8 + 1)];  // batch particle of each 8-column chunk
+	uint8_t owner[kTcMaxChunks];          // batch particle of each 8-column chunk
+	int8_t endp[kTcMaxChunks];            // batch particle whose run ends with the chunk, or -1
 	int deg[kTcBatch];
 	int colStart[kTcBatch + 1];  // run starts; past the batch: the batch's column count
-	unsigned long long bar[2];   // step-2 and step-4 MMA completion
+	unsigned long long bar;
 	uint32_t tmem;
-	int ok;                      // thread 0's verdict on its bounded waits
+	int ok;                      // thread 0's verdict on the MMA wait
 };
 
-// Row r of a K-major TF32 operand with 8 values per row: 8-row groups 256
-// bytes apart, the two 16-byte halves of a row (K 0-3, K 4-7) 128 apart.
 __device__ __forceinline__ unsigned char *tc_row(unsigned char *base, int r) {
 	return base + (r >> 3) * kTcGroupBytes + (r & 7) * 16;
 }
 
-// Segment matrix, K-major BF16 (16 rows x kTcCols): the core matrix of rows
-// 8g..8g+7 and columns 8c..8c+7 at c * 256 + g * 128.
-__device__ __forceinline__ unsigned char *seg_chunk(unsigned char *base, int row, int chunk) {
-	return base + chunk * 256 + (row >> 3) * 128 + (row & 7) * 16;
+// Sum of relu over 8 columns, as two partial sums.
+__device__ __forceinline__ float2 relu_sum8(const uint32_t *v) {
+	float r[8];
+#pragma unroll
+	for (int q = 0; q < 8; ++q) r[q] = fmaxf(__uint_as_float(v[q]), 0.f);
+	const float2 a = __fadd2_rn(make_float2(r[0], r[1]), make_float2(r[2], r[3]));
+	const float2 b = __fadd2_rn(make_float2(r[4], r[5]), make_float2(r[6], r[7]));
+	return __fadd2_rn(a, b);
 }
 
 }  // namespace
@@ -287,6 +279,7 @@ size_t mpnn_edge_tc_smem() {
 }
 
 int mpnn_edge_tc_blocks_per_sm() { return kTcBlocksPerSm; }
+int mpnn_edge_tc_threads() { return kTcThreads; }
 
 __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
     k_mpnn_edge_fwd_tc(MpnnGraph G, const float *W1, const float *b1, const float2 *z, __nv_bfloat16 *Hb,
@@ -305,11 +298,10 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
 		*reinterpret_cast<float4 *>(row + 128) = make_float4(w[4], w[5], tc::to_tf32(b1[f]), 0.f);
 	}
 	if (tid == 0) {
-		tc::mbar_init(&S.bar[0], 1);
-		tc::mbar_init(&S.bar[1], 1);
+		tc::mbar_init(&S.bar, 1);
 		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 	}
-	if (warp == 0) tc::tmem_alloc(&S.tmem, kTcTmemCols);
+	if (warp == 0) tc::tmem_alloc(&S.tmem, kTcCols);
 	tc::fence_async_smem();
 	tc::fence_before();
 	__syncthreads();
@@ -318,12 +310,8 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
 	const uint32_t tlane = tmem + ((uint32_t)(warp * 32) << 16);
 	const uint64_t descA = tc::desc_noswizzle(tc::smem_u32(S.a), 128, kTcGroupBytes);
 	const uint64_t descB = tc::desc_noswizzle(tc::smem_u32(S.b), 128, kTcGroupBytes);
-	const uint32_t segBase = tc::smem_u32(S.seg[0]);
-	const uint32_t idesc1 = tc::idesc_tf32(kHidden, kTcCols);
-	const uint32_t idesc2 = tc::idesc_bf16(kHidden, kTcSlots);
-	uint32_t phase1 = 0, phase2 = 0;
-	bool pending2 = false;  // a step-4 MMA was issued and not yet waited for
-	int tileNo = 0;         // selects the segment-matrix buffer
+	const uint32_t idesc = tc::idesc_tf32(kHidden, kTcCols);
+	uint32_t phase = 0;
 	bool good = true;
 	const float h2 = __fmul_rn(G.h, G.h);
 	const int ncell = G.gx * G.gy;
@@ -380,24 +368,22 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
 				}
 			}
 			__syncthreads();
-			const int cols = S.colStart[kTcBatch];
-			{
-				int cs[kTcBatch + 1];
+			int cs[kTcBatch + 1];
 #pragma unroll
-				for (int p = 0; p <= kTcBatch; ++p) cs[p] = S.colStart[p];
-				for (int ch = tid; ch < cols / 8; ch += kTcThreads) {
-					int p = 0;
+			for (int p = 0; p <= kTcBatch; ++p) cs[p] = S.colStart[p];
+			const int cols = cs[kTcBatch];
+			for (int ch = tid; ch < cols / 8; ch += kTcThreads) {
+				int p = 0;
 #pragma unroll
-					for (int q = 1; q < kTcBatch; ++q) p += ch * 8 >= cs[q] ? 1 : 0;
-					S.owner[ch] = (uint8_t)p;
-				}
+				for (int q = 1; q < kTcBatch; ++q) p += ch * 8 >= cs[q] ? 1 : 0;
+				S.owner[ch] = (uint8_t)p;
+				S.endp[ch] = (int8_t)(ch * 8 + 8 == S.colStart[p + 1] ? p : -1);
 			}
 			__syncthreads();
-			for (int t0 = 0; t0 < cols; t0 += kTcCols, ++tileNo) {
+			float2 acc = make_float2(0.f, 0.f);
+			for (int t0 = 0; t0 < cols; t0 += kTcCols) {
 				const int ncol = min(kTcCols, cols - t0);
-				const int nk = (ncol + 15) >> 4;  // K steps of the step-4 MMA
-				// Step 1: the tile's edge rows (zero past the batch's columns)...
-				if (tid < kTcCols) {
+				{
 					const int col = t0 + tid;
 					float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), hi = lo;
 					if (col < cols) {
@@ -419,100 +405,47 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
 					*reinterpret_cast<float4 *>(row) = lo;
 					*reinterpret_cast<float4 *>(row + 128) = hi;
 				}
-				// ... and its segment matrix: chunk ch (8 columns) belongs to
-				// one particle, whose row holds BF16 ones there.
-				unsigned char *seg = S.seg[tileNo & 1];
-				for (int q = tid; q < kTcSlots * kTcChunks; q += kTcThreads) {
-					const int row = q & (kTcSlots - 1), ch = q / kTcSlots;  // consecutive threads: consecutive rows
-					const int chunk = (t0 >> 3) + ch;
-					const uint32_t one = (chunk < (cols >> 3) && S.owner[chunk] == row) ? 0x3F803F80u : 0u;
-					*reinterpret_cast<uint4 *>(seg_chunk(seg, row, ch)) = make_uint4(one, one, one, one);
-				}
 				tc::fence_async_smem();
 				__syncthreads();
-				// Step 2, by thread 0 alone (the others wait at the barrier
-				// below): the previous tile's step-4 MMA reads the columns
-				// step 2 writes, so it must be complete first.
 				if (tid == 0) {
-					bool ok = true;
-					if (pending2) {
-						ok = tc::mbar_wait(&S.bar[1], phase2);
-						phase2 ^= 1;
-					}
-					if (ok) {
-						tc::fence_after();
-						tc::mma_tf32(tmem, descA, descB, idesc1, false);
-						tc::commit(&S.bar[0]);
-						ok = tc::mbar_wait(&S.bar[0], phase1);
-						phase1 ^= 1;
-					}
-					S.ok = ok;
+					tc::fence_after();
+					tc::mma_tf32(tmem, descA, descB, idesc, false);
+					tc::commit(&S.bar);
+					S.ok = tc::mbar_wait(&S.bar, phase);
 				}
-				pending2 = false;
+				phase ^= 1;
 				__syncthreads();
 				if (!S.ok) {
 					good = false;
 					break;
 				}
 				tc::fence_after();
-				// Step 3: relu, BF16, packed two per column into D1's first
-				// columns (each store lands on columns already read).
 #pragma unroll
-				for (int c0 = 0; c0 < 96; c0 += 32) {
+				for (int half = 0; half < 2; ++half) {
+					const int c0 = half * (kTcCols / 2);
 					if (c0 < ncol) {
-						uint32_t v[32], pk[16];
-						tc::tmem_ld32(tlane + (uint32_t)c0, v);
+						uint32_t v[kTcCols / 2];
+						tc::tmem_ld32(tlane + (uint32_t)c0, *reinterpret_cast<uint32_t(*)[32]>(v));
+						tc::tmem_ld32(tlane + (uint32_t)(c0 + 32), *reinterpret_cast<uint32_t(*)[32]>(v + 32));
 						tc::tmem_wait_ld();
 #pragma unroll
-						for (int u = 0; u < 16; ++u) pk[u] = tc::relu_bf16x2(v[2 * u], v[2 * u + 1]);
-						tc::tmem_st16(tlane + (uint32_t)(c0 / 2), pk);
+						for (int q = 0; q < kTcChunks / 2; ++q) {
+							acc = __fadd2_rn(acc, relu_sum8(v + 8 * q));
+							const int ch = (t0 + c0) / 8 + q;
+							if (ch < cols / 8) {
+								const int pe = S.endp[ch];
+								if (pe >= 0) {
+									Hb[(size_t)(st + jb + pe) * kHidden + tid] =
+									    __float2bfloat16_rn((acc.x + acc.y) * kAggScale);
+									acc = make_float2(0.f, 0.f);
+								}
+							}
+						}
 					}
 				}
-				if (96 < ncol) {
-					uint32_t v[16], pk[8];
-					tc::tmem_ld16(tlane + 96u, v);
-					tc::tmem_wait_ld();
-#pragma unroll
-					for (int u = 0; u < 8; ++u) pk[u] = tc::relu_bf16x2(v[2 * u], v[2 * u + 1]);
-					tc::tmem_st8(tlane + 48u, pk);
-				}
-				tc::tmem_wait_st();
 				tc::fence_before();
 				__syncthreads();
-				// Step 4.
-				if (tid == 0) {
-					tc::fence_after();
-					const uint32_t segAddr = segBase + (uint32_t)((tileNo & 1) * kTcSegBytes);
-					for (int s = 0; s < nk; ++s)
-						tc::mma_bf16_tmem_a(tmem + kTcCols, tmem + (uint32_t)(8 * s),
-						                    tc::desc_noswizzle(segAddr + (uint32_t)(s * 512), 256, 128), idesc2,
-						                    t0 > 0 || s > 0);
-					tc::commit(&S.bar[1]);
-				}
-				pending2 = true;
 			}
-			if (!good) break;
-			// The batch's sums: H_i = D2[:, p] / S.
-			if (tid == 0) {
-				S.ok = tc::mbar_wait(&S.bar[1], phase2);
-				phase2 ^= 1;
-			}
-			pending2 = false;
-			__syncthreads();
-			if (!S.ok) {
-				good = false;
-				break;
-			}
-			tc::fence_after();
-			uint32_t v[16];
-			tc::tmem_ld16(tlane + (uint32_t)kTcCols, v);
-			tc::tmem_wait_ld();
-#pragma unroll
-			for (int p = 0; p < kTcBatch; ++p)
-				if (p < nb)
-					Hb[(size_t)(st + jb + p) * kHidden + tid] = __float2bfloat16_rn(__uint_as_float(v[p]) * kAggScale);
-			tc::fence_before();
-			__syncthreads();
 		}
 	}
 	// Padding rows [n, np) are zero.
@@ -521,14 +454,13 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)
 		Hb[(size_t)G.n * kHidden + t] = __float2bfloat16_rn(0.f);
 	if (!good && tid == 0) {
 		atomicOr(error, 1u);
-		// The tensor core may still be working: wait (bounded) for the
-		// MMAs issued before tensor memory is freed.
-		tc::mbar_wait(&S.bar[0], phase1 ^ 1);
-		tc::mbar_wait(&S.bar[1], phase2 ^ 1);
+		// The tensor core may still be working on the last tile: wait for
+		// it (bounded) before the tensor memory is freed.
+		tc::mbar_wait(&S.bar, phase ^ 1);
 	}
 	tc::fence_before();
 	__syncthreads();
-	if (warp == 0) tc::tmem_free(tmem, kTcTmemCols);
+	if (warp == 0) tc::tmem_free(tmem, kTcCols);
 }
 
 // Backward of the edge layer: dW1, db1 from every edge (i aggregates j),

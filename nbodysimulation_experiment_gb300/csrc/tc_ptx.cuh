@@ -8,7 +8,8 @@
 namespace sphgb {
 namespace tc {
 
-constexpr uint32_t kWaitPolls = 1u << 18;
+constexpr uint32_t kWaitPolls = 1u << 22;
+constexpr uint64_t kWaitNs = 200000000ull;  // 0.2 s
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -35,23 +36,58 @@ __device__ __forceinline__ void mbar_init(unsigned long long *bar, uint32_t coun
 	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
 
-// Bounded wait for the phase with the given parity: try_wait suspends the
-// thread in hardware until the phase completes or about a microsecond
-// passes; at most kWaitPolls tries (well under a second) before giving up.
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+	uint64_t t;
+	asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+	return t;
+}
+
+// Bounded wait for the phase with the given parity: try_wait (which may
+// suspend the thread for a while in hardware), after 8 tries a 64 ns sleep
+// between tries; gives up after kWaitNs nanoseconds or kWaitPolls tries.
 __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, uint32_t parity) {
 	const uint32_t addr = smem_u32(bar);
+	uint64_t start = 0;
 	for (uint32_t i = 0; i < kWaitPolls; ++i) {
 		uint32_t ok;
 		asm volatile(
 		    "{\n\t.reg .pred p;\n\t"
-		    "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+		    "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
 		    "selp.u32 %0, 1, 0, p;\n\t}"
 		    : "=r"(ok)
-		    : "r"(addr), "r"(parity), "r"(1000u)
+		    : "r"(addr), "r"(parity)
 		    : "memory");
 		if (ok) return true;
+		if (i == 8) start = globaltimer_ns();
+		if (i >= 8) {
+			__nanosleep(64);
+			if ((i & 255) == 0 && globaltimer_ns() - start > kWaitNs) return false;
+		}
 	}
 	return false;
+}
+
+__device__ __forceinline__ void mbar_arrive(unsigned long long *bar) {
+	asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Named barrier `id` over `count` threads (a multiple of 32); returns
+// whether any of them passed `pred` true.
+__device__ __forceinline__ bool bar_or(int id, int count, bool pred) {
+	uint32_t r;
+	asm volatile(
+	    "{\n\t.reg .pred p, q;\n\t"
+	    "setp.ne.u32 p, %1, 0;\n\t"
+	    "barrier.red.or.pred q, %2, %3, p;\n\t"
+	    "selp.u32 %0, 1, 0, q;\n\t}"
+	    : "=r"(r)
+	    : "r"((uint32_t)pred), "r"(id), "r"(count)
+	    : "memory");
+	return r != 0;
+}
+
+__device__ __forceinline__ void bar_sync(int id, int count) {
+	asm volatile("barrier.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
 }
 
 __device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc, bool acc) {

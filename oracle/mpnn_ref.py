@@ -15,8 +15,7 @@ Network (per round r = 0, 1, separate weights):
 with z^0 = v dt / h, output u = z^2 - z^0 and loss mean_i |u_i - t_i|^2.
 ``emulate_bf16=True`` rounds where the GPU rounds: to BF16 where it
 stores BF16 (H, [M, z], c, the GEMM weights W2 and W3, and in the backward
-pass da3 and dM, and each edge's activation relu(W1 e + b1) before the
-per-particle sum), to TF32 the edge layer's inputs (the edge features, W1
+pass da3 and dM), to TF32 the edge layer's inputs (the edge features, W1
 and b1, which the tensor cores read as TF32).
 """
 from __future__ import annotations
@@ -119,7 +118,7 @@ def forward(flat, pos, z0, I, J, h, emulate_bf16=False):
         q = r / h
         e = rnd_edge(np.stack([d[:, 0] / h, d[:, 1] / h, q, dz[:, 0], dz[:, 1], (1 - q) ** 2], 1))
         a = e @ rnd_edge(p["W1"]).T + rnd_edge(p["b1"])
-        act = rnd(np.maximum(a, 0))
+        act = np.maximum(a, 0)
         H = np.zeros((n, HIDDEN))
         np.add.at(H, I, act)
         H = rnd(H / S)
