@@ -520,13 +520,32 @@ def bench_learned(torch, pkg, scenes, device: int, args):
                 ms.append(e0.elapsed_time(e1))
                 used += int(u)
                 errs.append(err)
+        # End to end through the C ABI with host buffers: every frame loads
+        # the state from pinned host memory, advances it and reads it back.
+        st = sim.dump_state()
+        pinned = pinned_like(torch, {k: st[k] for k in STATE_KEYS})
+        pinned["canonical_count"] = st["canonical_count"]
+        pinned["grid"] = st["grid"]
+        pinned_out = pinned_like(torch, {k: st[k] for k in STATE_KEYS})
+        nbytes = sum(pinned[k].nbytes for k in STATE_KEYS)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.learned_eval_frames):
+            sim.load_state(pinned)
+            if use_network:
+                sim.learned_frame(model, frame, sub, bound=0.01)
+            else:
+                for _ in range(sub):
+                    sim.update(frame / sub)
+            sim.dump_state(out=pinned_out)
+        e2e_ms = (time.perf_counter() - t0) * 1e3 / args.learned_eval_frames
         if not use_network:  # density deviation of the plain result, as the judge measures it
             errs = [sim.learned_frame(model, frame, sub, bound=-1.0)[1]]
         sim.close()
-        return statistics.mean(ms), used, float(np.mean(errs))
+        return statistics.mean(ms), used, float(np.mean(errs)), e2e_ms, nbytes
 
-    ms_l, used, err_l = run(True)
-    ms_p, _, err_p = run(False)
+    ms_l, used, err_l, e2e_l, nbytes = run(True)
+    ms_p, _, err_p, e2e_p, _ = run(False)
     quality = learned_quality(pkg, scene, model, device, frame, sub, args.learned_rollout_frames)
     n, nf = scene.n, args.learned_eval_frames
     model.close()
@@ -534,6 +553,11 @@ def bench_learned(torch, pkg, scenes, device: int, args):
             "frame": "1/60 s = %d reference substeps" % sub,
             "particle_steps_per_s": n * sub / (ms_l / 1e3),
             "ms_per_frame": ms_l, "plain_ms_per_frame": ms_p, "speedup_vs_plain_frame": ms_p / ms_l,
+            "e2e": {"value": n / (e2e_l / 1e3), "unit": "particle-frames/s", "ms_per_frame": e2e_l,
+                    "plain_ms_per_frame": e2e_p, "speedup_vs_plain_frame": e2e_p / e2e_l,
+                    "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                    "path": "sph_load_state from pinned host memory, sph_learned_frame (or four sph_update), "
+                            "sph_dump_state into pinned host memory, every frame"},
             "frames": nf, "accepted_frames": used, "density_error": err_l,
             "density_error_plain_frame": err_p, "judge_bound": 0.01,
             "judge": "a learned frame stands if its mean |rho - rho0| / rho0 exceeds that of the single plain "

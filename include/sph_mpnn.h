@@ -24,8 +24,12 @@ extern "C" {
  * 256, K a multiple of 16, any M.  Optional bias [N] and ReLU; accumulate = 1
  * adds into C atomically (required when splits > 1 divides K over CTAs).
  * staging = 0 feeds the operands with TMA (cp.async.bulk.tensor, 128-byte
- * swizzle); 1 with plain loads.  Enqueued on `stream` (cudaStream_t) and
- * waited for. */
+ * swizzle): with splits = 1 and B small enough to stay in shared memory
+ * (N x K <= 48K elements), persistent CTAs (one per SM) loop over the row
+ * tiles with B resident, A through a 4-stage ring and the accumulator
+ * double-buffered in tensor memory; otherwise one CTA per row tile and K
+ * split.  staging = 2 forces the one-tile-per-CTA TMA form, 1 stages with
+ * plain loads.  Enqueued on `stream` (cudaStream_t) and waited for. */
 int sph_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K, int lda, int ldb, int ldc,
                   const float *bias, int relu, int accumulate, int splits, int staging, void *stream);
 

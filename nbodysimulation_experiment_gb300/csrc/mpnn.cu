@@ -575,7 +575,7 @@ extern "C" int sph_gemm_bf16(const void *A, const void *B, float *C, int M, int 
 	g.accumulate = accumulate;
 	g.noTma = staging;
 	g.error = gemm_error_word(device);
-	if (!A || !B || !C || !g.error || ldc < N) return SPH_ERR_INVALID_ARGUMENT;
+	if (!A || !B || !C || !g.error || ldc < N || staging < 0 || staging > 2) return SPH_ERR_INVALID_ARGUMENT;
 	if (gemm_check(g, splits) != 0) return SPH_ERR_INVALID_ARGUMENT;
 	cudaStream_t st = static_cast<cudaStream_t>(stream);
 	if (gemm_launch(g, splits, st) != cudaSuccess) return SPH_ERR_CUDA;

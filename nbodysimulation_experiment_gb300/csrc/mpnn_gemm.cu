@@ -21,6 +21,7 @@
 #include <cudaTypedefs.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <mutex>
 
 #include "mpnn_internal.cuh"
@@ -425,6 +426,171 @@ __global__ void __launch_bounds__(kGemmThreads, 1) k_gemm_bf16_tma(GemmArgs g, c
 	}
 }
 
+// ---------------------------------------------------------------------------
+// Persistent TMA-fed variant for one K split: each CTA loops over row tiles
+// blockIdx.x, blockIdx.x + gridDim.x, ...  B (all of N x K) is loaded once
+// per CTA and stays in shared memory; A arrives in 128 x 64 chunks through a
+// kPersistStages-deep ring (full/empty mbarriers); the accumulator is
+// double-buffered in tensor memory (tfull/tempty mbarriers), so one tile's
+// epilogue overlaps the next tile's loads and MMAs.  Warps 0-3 run the
+// epilogue (warp w owns TMEM lanes 32w..32w+31), lane 0 of warp 4 drives
+// TMA, lane 0 of warp 5 issues the MMAs.  Every wait is bounded; a wait that
+// runs out raises the CTA's abort flag and the error word, every role then
+// leaves its loop (collectively within a warp), and the MMA thread waits
+// (bounded) for its last MMAs before tensor memory is freed.
+
+namespace {
+
+constexpr int kPersistStages = 4;
+constexpr int kPersistThreads = 192;
+constexpr int kPersistMaxBBytes = 96 * 1024;
+
+struct PersistCtl {
+	unsigned long long full[kPersistStages], empty[kPersistStages];
+	unsigned long long bfull, tfull[2], tempty[2], fin;
+	uint32_t tmem;
+	volatile int abort;
+};
+
+__host__ __device__ inline int k_chunks(int K) { return (K + kChunkK - 1) / kChunkK; }
+__host__ __device__ inline size_t persist_b_bytes(int n, int K) { return (size_t)k_chunks(K) * n * kChunkK * 2; }
+
+}  // namespace
+
+size_t gemm_persist_smem_bytes(int n, int K) {
+	// More than half of an SM's shared memory: one CTA per SM, which then
+	// owns up to all 512 tensor-memory columns.
+	const size_t need = persist_b_bytes(n, K) + (size_t)kPersistStages * kTmaABytes + sizeof(PersistCtl) + 1024;
+	const size_t minimum = 116 * 1024;
+	return need > minimum ? need : minimum;
+}
+
+__global__ void __launch_bounds__(kPersistThreads, 1) k_gemm_bf16_persist(GemmArgs g,
+                                                                          const __grid_constant__ CUtensorMap mapA,
+                                                                          const __grid_constant__ CUtensorMap mapB) {
+	extern __shared__ unsigned char smem_raw[];
+	unsigned char *base =
+	    reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+	const int nk = k_chunks(g.K);
+	const size_t bBytes = persist_b_bytes(g.N, g.K);
+	unsigned char *bRes = base;                         // chunk c at c * N * 128 bytes
+	unsigned char *aRing = base + bBytes;               // 1 KiB-aligned: bBytes is a multiple of 1 KiB
+	PersistCtl &C = *reinterpret_cast<PersistCtl *>(aRing + kPersistStages * kTmaABytes);
+	const int tid = threadIdx.x, warp = tid / 32, lane = tid & 31;
+	const int ncols = g.N <= 32 ? 32 : (g.N <= 64 ? 64 : (g.N <= 128 ? 128 : 256));
+	const int tiles = (g.M + kTileM - 1) / kTileM;
+
+	if (tid == 0) {
+		for (int s = 0; s < kPersistStages; ++s) {
+			mbar_init(&C.full[s], 1);
+			mbar_init(&C.empty[s], 1);
+		}
+		mbar_init(&C.bfull, 1);
+		for (int b = 0; b < 2; ++b) {
+			mbar_init(&C.tfull[b], 1);
+			mbar_init(&C.tempty[b], 128);
+		}
+		mbar_init(&C.fin, 1);
+		C.abort = 0;
+		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+		asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapA)) : "memory");
+		asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapB)) : "memory");
+	}
+	if (warp == 5) {
+		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&C.tmem)),
+		             "r"(2 * ncols)
+		             : "memory");
+		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+	__syncthreads();
+	asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+	const uint32_t tmem = C.tmem;
+
+	if (warp == 4) {
+		if (lane == 0) {
+			// TMA: B once, then A chunk by chunk for every tile of this CTA.
+			mbar_expect_tx(&C.bfull, (uint32_t)bBytes);
+			for (int c = 0; c < nk; ++c) tma_load_2d(bRes + (size_t)c * g.N * kChunkK * 2, &mapB, c * kChunkK, 0, &C.bfull);
+			int it = 0;
+			for (int t = blockIdx.x; t < tiles && !C.abort; t += gridDim.x) {
+				for (int c = 0; c < nk; ++c, ++it) {
+					const int s = it % kPersistStages;
+					if (it >= kPersistStages && !mbar_wait(&C.empty[s], ((it / kPersistStages) - 1) & 1)) {
+						C.abort = 1;
+						break;
+					}
+					mbar_expect_tx(&C.full[s], (uint32_t)kTmaABytes);
+					tma_load_2d(aRing + s * kTmaABytes, &mapA, c * kChunkK, t * kTileM, &C.full[s]);
+				}
+			}
+		}
+		__syncwarp();
+	} else if (warp == 5) {
+		if (lane == 0) {
+			const uint32_t idesc = instr_desc(g.N);
+			bool ok = mbar_wait(&C.bfull, 0);
+			int it = 0, i = 0;
+			for (int t = blockIdx.x; ok && t < tiles && !C.abort; t += gridDim.x, ++i) {
+				const int b = i & 1;
+				// The epilogue has read this buffer's previous tile.
+				if (i >= 2 && !mbar_wait(&C.tempty[b], ((i - 2) >> 1) & 1)) {
+					ok = false;
+					break;
+				}
+				asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+				for (int c = 0; c < nk; ++c, ++it) {
+					const int s = it % kPersistStages;
+					if (!mbar_wait(&C.full[s], (it / kPersistStages) & 1)) {
+						ok = false;
+						break;
+					}
+					asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+					const uint32_t a0 = smem_u32(aRing + s * kTmaABytes);
+					const uint32_t b0 = smem_u32(bRes + (size_t)c * g.N * kChunkK * 2);
+					const int kc = min(kChunkK, g.K - c * kChunkK);
+					for (int k = 0; k < kc / 16; ++k)
+						mma_bf16(tmem + (uint32_t)(b * ncols), sw128_desc(a0 + k * 32), sw128_desc(b0 + k * 32), idesc,
+						         c > 0 || k > 0);
+					mma_commit(&C.empty[s]);
+				}
+				if (!ok) break;
+				mma_commit(&C.tfull[b]);
+			}
+			if (!ok) {
+				C.abort = 1;
+				atomicOr(g.error, 1u);
+			}
+			// Every MMA issued above is complete before tensor memory is freed.
+			mma_commit(&C.fin);
+			if (!mbar_wait(&C.fin, 0)) atomicOr(g.error, 1u);
+		}
+		__syncwarp();
+	} else {
+		// Epilogue warps 0-3.
+		int i = 0;
+		for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++i) {
+			const int b = i & 1;
+			if (__any_sync(0xffffffffu, C.abort != 0)) break;
+			const bool ok = mbar_wait(&C.tfull[b], (i >> 1) & 1);
+			if (!__all_sync(0xffffffffu, ok)) {
+				C.abort = 1;
+				atomicOr(g.error, 1u);
+				break;
+			}
+			asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+			epilogue(g, tmem + (uint32_t)(b * ncols), t * kTileM, warp, lane);
+			asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+			asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&C.tempty[b])) : "memory");
+		}
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+	__syncthreads();
+	if (warp == 5) {
+		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * ncols) : "memory");
+	}
+}
+
 namespace {
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -469,6 +635,7 @@ cudaError_t gemm_launch(const GemmArgs &g, int splits, cudaStream_t stream) {
 	// Kernel attributes are per device: set them once on each device used.
 	static std::mutex mu;
 	static bool done[64] = {};
+	static int sms[64] = {};
 	int device = 0;
 	cudaError_t e = cudaGetDevice(&device);
 	if (e != cudaSuccess) return e;
@@ -481,14 +648,24 @@ cudaError_t gemm_launch(const GemmArgs &g, int splits, cudaStream_t stream) {
 			if (e == cudaSuccess)
 				e = cudaFuncSetAttribute(k_gemm_bf16_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
 				                         (int)gemm_tma_smem_bytes(kMaxN));
+			if (e == cudaSuccess)
+				e = cudaFuncSetAttribute(k_gemm_bf16_persist, cudaFuncAttributeMaxDynamicSharedMemorySize,
+				                         (int)gemm_persist_smem_bytes(kMaxN, kPersistMaxBBytes / (kMaxN * 2)));
+			if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms[device], cudaDevAttrMultiProcessorCount, device);
 			if (e != cudaSuccess) return e;
 			done[device] = true;
 		}
 	}
-	dim3 grid((g.M + kTileM - 1) / kTileM, splits);
+	const int tiles = (g.M + kTileM - 1) / kTileM;
+	dim3 grid(tiles, splits);
 	CUtensorMap mapA, mapB;
-	if (!g.noTma && encode(&mapA, g.A, g.M, g.K, g.lda, kTileM) && encode(&mapB, g.B, g.N, g.K, g.ldb, g.N)) {
-		k_gemm_bf16_tma<<<grid, kGemmThreads, gemm_tma_smem_bytes(g.N), stream>>>(g, mapA, mapB);
+	if (g.noTma != 1 && encode(&mapA, g.A, g.M, g.K, g.lda, kTileM) && encode(&mapB, g.B, g.N, g.K, g.ldb, g.N)) {
+		if (g.noTma == 0 && splits == 1 && persist_b_bytes(g.N, g.K) <= (size_t)kPersistMaxBBytes) {
+			k_gemm_bf16_persist<<<std::min(tiles, sms[device]), kPersistThreads, gemm_persist_smem_bytes(g.N, g.K),
+			                      stream>>>(g, mapA, mapB);
+		} else {
+			k_gemm_bf16_tma<<<grid, kGemmThreads, gemm_tma_smem_bytes(g.N), stream>>>(g, mapA, mapB);
+		}
 	} else {
 		k_gemm_bf16<<<grid, kGemmThreads, gemm_smem_bytes(), stream>>>(g);
 	}

@@ -27,7 +27,7 @@ struct GemmArgs {
 	__nv_bfloat16 *CbT;     // bf16 transposed [N][ldcbT] (nullable)
 	int ldcbT;
 	uint32_t *error;        // set to 1 if a bounded wait ran out
-	int noTma;              // stage operands with plain loads instead of TMA
+	int noTma;              // 0: TMA (persistent CTAs for one K split), 1: plain loads, 2: TMA, one tile per CTA
 };
 
 size_t gemm_smem_bytes();
