@@ -331,6 +331,20 @@ int sph_test_hold_task(sph_sim *sim, int sweep, int claim);
 int sph_get_sweep_shape(sph_sim *sim, int *shape);
 int sph_set_sweep_shape(sph_sim *sim, const int *shape);
 
+/* Dense states.  With adaptive shapes on (the default), an update whose
+ * previous updates saw neighbour lists longer than 440 runs the wide
+ * viscosity shape, and one where a 3x3 block of the fullest cell's count
+ * nears the tuned delta shape's stage runs the 8-warp delta shape (4,096
+ * staged entries), or the 16-warp shape (12,288) once a 5x5 region of it
+ * would exceed 4,096, instead of the tuned shapes (results are identical in
+ * every shape; only the launch differs).  Single-scene simulations only: a
+ * batch keeps its tuned shapes.  The statistics come from the
+ * end of earlier updates, read without waiting.  sph_last_sweep_shape
+ * returns the shapes the last update ran with, in sph_get_sweep_shape's
+ * form.  sph_autotune times the shapes with adaptivity off. */
+int sph_set_adaptive_shapes(sph_sim *sim, int enable);
+int sph_last_sweep_shape(sph_sim *sim, int shape[4]);
+
 /* ---- Viscoelastic springs (no reference counterpart) ----------------------
  * Springs with plasticity after Clavet et al. 2005 ("Particle-based
  * viscoelastic fluid simulation", Algorithms 3 and 4), in a deterministic

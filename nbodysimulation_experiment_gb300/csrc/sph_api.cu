@@ -100,6 +100,17 @@ struct sph_sim {
 	bool refOrder = false;  // sweeps and grid events in AddParticle order (sph_set_reference_order)
 	int viscRefBlocks = 0;
 	int deltaShape = 0;  // delta shape: kDeltaWide, kDeltaLean or kDeltaMid
+	// Dense states (sph_set_adaptive_shapes): the shapes above are the tuned
+	// ones; an update whose previous updates saw long neighbour lists or
+	// crowded cells runs the sweep shapes that stay staged there instead.
+	// The statistics arrive in pinned host memory at the end of every update
+	// and are read without waiting, so the choice may lag by an update.
+	bool adaptive = true;
+	bool denseVisc = false, denseDelta = false, crowdedDelta = false;
+	int denseViscBlocks = 0, denseDeltaBlocks = 0, crowdedDeltaBlocks = 0;
+	int runViscLean = -1, runViscBlocks = 0, runDeltaShape = -1, runDeltaBlocks = 0;  // of the last update
+	uint32_t *hostStats = nullptr;  // pinned: 4 per scene, as T.stats
+	cudaEvent_t statsEv[2] = {nullptr, nullptr};  // after the copy, per update parity
 	bool batch = false;
 	int multithreading = 0;
 
@@ -513,7 +524,7 @@ int enqueue_step(sph_sim *s, bool capturing) {
 		SPH_CUDA(cudaMemsetAsync(T.taskCounter, 0, sizeof(int), st));
 		SimTables v = T;
 		v.done = s->doneV;
-		launch_viscosity(s->viscLean, s->viscBlocks, st, tt, A.view(), v);
+		launch_viscosity(s->runViscLean != 0, s->runViscBlocks, st, tt, A.view(), v);
 		SPH_LAUNCHED(s);
 	}
 	SPH_CUDA(mark(kEvVisc));
@@ -564,7 +575,7 @@ int enqueue_step(sph_sim *s, bool capturing) {
 	{
 		SimTables d = T;
 		d.done = s->doneD;
-		launch_delta(s->deltaShape, s->deltaBlocks, st, tt, B.view(), d);
+		launch_delta(s->runDeltaShape, s->runDeltaBlocks, st, tt, B.view(), d);
 		SPH_LAUNCHED(s);
 	}
 	SPH_CUDA(mark(kEvDelta));
@@ -572,7 +583,63 @@ int enqueue_step(sph_sim *s, bool capturing) {
 	k_collide<<<blocks_for(cellOrN, kCollideThreads), kCollideThreads, 0, st>>>(tt, A.view(), B.view(), T);
 	SPH_LAUNCHED(s);
 	SPH_CUDA(mark(kEvCollide));
+	// This update's neighbourhood statistics, for the next updates' choice
+	// of sweep shapes (read on the host without waiting).
+	SPH_CUDA(cudaMemcpyAsync(s->hostStats, T.stats, sizeof(uint32_t) * 4 * s->scenes.size(), cudaMemcpyDeviceToHost, st));
 	return SPH_OK;
+}
+
+// Viscosity pair lists longer than this send the lean viscosity shape's
+// chains through several rounds; the wide shape stays staged.
+constexpr uint32_t kDenseNeighbors = 440;
+
+// The sweep shapes of the next update: the tuned ones, or in dense states
+// (see sph_sim::adaptive) the wide viscosity shape and a delta shape whose
+// stage holds the task regions: the 8-warp shape (4,096 entries) once a 3x3
+// block of the fullest cell nears the tuned shape's stage, the 16-warp shape
+// (12,288 entries) once a 5x5 region of it would exceed 4,096.  The statistics are those of the update
+// before last at the latest: the host waits for its copy, so it never runs
+// more than two updates ahead.  Changing shapes drops the update graphs.
+void choose_shapes(sph_sim *s) {
+	int vl = s->viscLean, vb = s->viscBlocks, ds = s->deltaShape, db = s->deltaBlocks;
+	// A batch of many scenes keeps its tuned shapes: its sweeps are bound by
+	// how many tasks run at once, not by one crowded scene's tasks.
+	const bool adapt = s->adaptive && !s->batch && s->hostStats;
+	if (adapt && s->statsEv[s->cur]) cudaEventSynchronize(s->statsEv[s->cur]);
+	if (adapt) {
+		uint32_t maxNb = 0, maxCell = 0;
+		const volatile uint32_t *h = s->hostStats;
+		for (size_t k = 0; k < s->scenes.size(); ++k) {
+			const uint32_t nb = h[4 * k + 1], cell = h[4 * k + 3];
+			maxNb = std::max(maxNb, nb);
+			maxCell = std::max(maxCell, cell);
+		}
+		// Hysteresis: back to the tuned shape only well below the threshold.
+		s->denseVisc = s->denseVisc ? maxNb * 5 > kDenseNeighbors * 4 : maxNb > kDenseNeighbors;
+		const uint32_t cap = (uint32_t)delta_stage_capacity(ds);
+		const uint32_t block = 9 * maxCell;   // a 3x3 block at the fullest cell's count
+		const uint32_t spread = 25 * maxCell;  // a 5x5 region: a cell's particles spread over 3x3 new cells
+		s->denseDelta = s->denseDelta ? block * 5 > cap * 3 : block * 4 > cap * 3;
+		s->crowdedDelta = s->crowdedDelta ? spread * 5 > (uint32_t)kDeltaStageCap * 4 : spread > (uint32_t)kDeltaStageCap;
+		if (vl && s->denseVisc) {
+			vl = 0;
+			vb = s->denseViscBlocks;
+		}
+		if (cap < (uint32_t)kDeltaDenseStageCap && s->crowdedDelta) {
+			ds = kDeltaDense;
+			db = s->crowdedDeltaBlocks;
+		} else if (cap < (uint32_t)kDeltaStageCap && s->denseDelta) {
+			ds = kDeltaMid;
+			db = s->denseDeltaBlocks;
+		}
+	}
+	if (vl != s->runViscLean || vb != s->runViscBlocks || ds != s->runDeltaShape || db != s->runDeltaBlocks) {
+		drop_graphs(s);
+		s->runViscLean = vl;
+		s->runViscBlocks = vb;
+		s->runDeltaShape = ds;
+		s->runDeltaBlocks = db;
+	}
 }
 
 // Capture one update into an executable graph (nothing runs).
@@ -599,6 +666,7 @@ int run_step(sph_sim *s, float dt) {
 	if (rc) return rc;
 	rc = upload_appendix_tasks(s);
 	if (rc) return rc;
+	choose_shapes(s);
 	// A graph is captured once the same update has run eagerly (scene table,
 	// bodies and dt unchanged, no appendix), then replayed.
 	const bool replay = s->useGraphs && s->nApp == 0 && s->steadySteps >= 1;
@@ -614,6 +682,7 @@ int run_step(sph_sim *s, float dt) {
 		rc = enqueue_step(s, false);
 		if (rc) return rc;
 	}
+	SPH_CUDA(cudaEventRecord(s->statsEv[s->cur], s->stream));
 	if (s->nApp == 0) s->steadySteps++;
 
 	// The new cell arrays are the canonical ranges of the next step.
@@ -673,6 +742,8 @@ int allocate(sph_sim *s) {
 	if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) return SPH_ERR_CUDA;
 	for (int k = 0; k < kEvCount; ++k)
 		if (cudaEventCreate(&s->ev[k]) != cudaSuccess) return SPH_ERR_CUDA;
+	for (int k = 0; k < 2; ++k)
+		if (cudaEventCreateWithFlags(&s->statsEv[k], cudaEventDisableTiming) != cudaSuccess) return SPH_ERR_CUDA;
 	for (int b = 0; b < 2; ++b) {
 		BufferSet &B = s->buf[b];
 		if ((rc = dalloc(&B.pos, N)) || (rc = dalloc(&B.prev, N)) || (rc = dalloc(&B.vel, N)) ||
@@ -757,6 +828,10 @@ int allocate(sph_sim *s) {
 	    cudaMemcpy(T.sceneOf, sceneOf.data(), sceneOf.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
 	    cudaMemcpy(T.stats, seed.data(), seed.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess)
 		return SPH_ERR_CUDA;
+	if (s->hostStats) cudaFreeHost(s->hostStats);
+	s->hostStats = nullptr;
+	if (cudaMallocHost(&s->hostStats, sizeof(uint32_t) * 4 * S) != cudaSuccess) return SPH_ERR_CAPACITY;
+	std::memcpy(s->hostStats, seed.data(), seed.size() * 4);
 
 	cudaDeviceProp prop;
 	if (cudaGetDeviceProperties(&prop, s->device) != cudaSuccess) return SPH_ERR_CUDA;
@@ -771,6 +846,14 @@ int allocate(sph_sim *s) {
 	if (sweep_occupancy(false, kDeltaWide, &occV, &occD) != cudaSuccess || occV < 1 || occD < 1) return SPH_ERR_CUDA;
 	s->viscBlocks = occV * s->numSMs;
 	s->deltaBlocks = occD * s->numSMs;
+	s->denseViscBlocks = s->viscBlocks;  // the wide viscosity shape
+	{
+		int v2 = 0, d2 = 0;
+		if (sweep_occupancy(false, kDeltaMid, &v2, &d2) != cudaSuccess || d2 < 1) return SPH_ERR_CUDA;
+		s->denseDeltaBlocks = d2 * s->numSMs;
+		if (sweep_occupancy(false, kDeltaDense, &v2, &d2) != cudaSuccess || d2 < 1) return SPH_ERR_CUDA;
+		s->crowdedDeltaBlocks = d2 * s->numSMs;
+	}
 	s->densBlocks = std::max(1, std::min(blocks_for(C, kDensWarps), 64 * s->numSMs));
 	s->springBlocks = std::max(1, std::min(blocks_for(C, kSpringWarps), 64 * s->numSMs));
 	s->gridBlocks = std::max(1, std::min(blocks_for(C, kGridWarps), 64 * s->numSMs));
@@ -1291,10 +1374,13 @@ int sph_destroy(sph_sim *s) {
 	                s->imgRgba,    T.refOrd,      T.viscBox,     s->check};
 	for (void *p : ptrs)
 		if (p) cudaFree(p);
+	if (s->hostStats) cudaFreeHost(s->hostStats);
 	if (s->hostPos) cudaFreeHost(s->hostPos);
 	if (s->hostForce) cudaFreeHost(s->hostForce);
 	for (int k = 0; k < kEvCount; ++k)
 		if (s->ev[k]) cudaEventDestroy(s->ev[k]);
+	for (int k = 0; k < 2; ++k)
+		if (s->statsEv[k]) cudaEventDestroy(s->statsEv[k]);
 	if (s->stream) cudaStreamDestroy(s->stream);
 	delete s;
 	return SPH_OK;
@@ -1880,8 +1966,9 @@ int sph_autotune(sph_sim *s, float dt, int *shape) {
 	if (s->totalParticles() == 0) return SPH_ERR_NOT_SUPPORTED;
 	rc = ensure_learned(s);
 	if (rc) return rc;
-	const bool graphs = s->useGraphs;
+	const bool graphs = s->useGraphs, adaptive = s->adaptive;
 	s->useGraphs = false;
+	s->adaptive = false;  // time the shapes as given
 	rc = copy_state(s, true);
 	if (rc) return rc;
 	// Median of three timed updates per shape (after one warm-up update); the
@@ -1941,6 +2028,7 @@ int sph_autotune(sph_sim *s, float dt, int *shape) {
 	s->deltaShape = pick[2];
 	s->deltaBlocks = pick[3];
 	s->useGraphs = graphs;
+	s->adaptive = adaptive;
 	drop_graphs(s);
 	s->timed = false;
 	if (rc) return rc;
@@ -1978,6 +2066,22 @@ int sph_set_sweep_shape(sph_sim *s, const int *shape) {
 	s->deltaShape = dShape;
 	s->deltaBlocks = shape[3];
 	drop_graphs(s);
+	return SPH_OK;
+}
+
+int sph_set_adaptive_shapes(sph_sim *s, int enable) {
+	if (!s) return SPH_ERR_INVALID_ARGUMENT;
+	s->adaptive = enable != 0;
+	return SPH_OK;
+}
+
+int sph_last_sweep_shape(sph_sim *s, int *shape) {
+	if (!s || !shape) return SPH_ERR_INVALID_ARGUMENT;
+	if (s->runViscLean < 0) return sph_get_sweep_shape(s, shape);
+	shape[0] = s->runViscLean ? ViscLean::kWarps : ViscWide::kWarps;
+	shape[1] = s->runViscBlocks;
+	shape[2] = delta_shape_warps(s->runDeltaShape);
+	shape[3] = s->runDeltaBlocks;
 	return SPH_OK;
 }
 

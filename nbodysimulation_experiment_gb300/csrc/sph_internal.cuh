@@ -16,6 +16,8 @@ constexpr int kStageCap = 1024;
 // box grown by one (5x5 cells when particles left the cell in every
 // direction).
 constexpr int kDeltaStageCap = 4096;
+// The dense delta shape's stage: a 5x5 region of cells of ~490 particles.
+constexpr int kDeltaDenseStageCap = 12288;
 // In-range pairs buffered between the parallel geometry phase and the serial
 // chain of one particle; longer lists are drained in several rounds.
 constexpr int kChainCap = 256;

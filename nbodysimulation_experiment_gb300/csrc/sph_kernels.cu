@@ -2450,6 +2450,9 @@ cudaError_t sweep_attributes() {
 	if (e == cudaSuccess)
 		e = cudaFuncSetAttribute(k_delta<DeltaQuad>, cudaFuncAttributeMaxDynamicSharedMemorySize,
 		                         (int)delta_smem_bytes<DeltaQuad>());
+	if (e == cudaSuccess)
+		e = cudaFuncSetAttribute(k_delta<DeltaDense>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                         (int)delta_smem_bytes<DeltaDense>());
 	return e;
 }
 
@@ -2473,6 +2476,9 @@ cudaError_t sweep_occupancy(bool viscLean, int deltaShape, int *occV, int *occD)
 	if (deltaShape == kDeltaQuad)
 		return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occD, k_delta<DeltaQuad>, DeltaQuad::kWarps * kWarp,
 		                                                     delta_smem_bytes<DeltaQuad>());
+	if (deltaShape == kDeltaDense)
+		return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occD, k_delta<DeltaDense>, DeltaDense::kWarps * kWarp,
+		                                                     delta_smem_bytes<DeltaDense>());
 	return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occD, k_delta<DeltaWide>, DeltaWide::kWarps * kWarp,
 	                                                     delta_smem_bytes<DeltaWide>());
 }
@@ -2494,6 +2500,8 @@ void launch_delta(int shape, int blocks, cudaStream_t st, Totals tt, Particles Q
 		k_delta<DeltaTri><<<blocks, DeltaTri::kWarps * kWarp, delta_smem_bytes<DeltaTri>(), st>>>(tt, Q, T);
 	else if (shape == kDeltaQuad)
 		k_delta<DeltaQuad><<<blocks, DeltaQuad::kWarps * kWarp, delta_smem_bytes<DeltaQuad>(), st>>>(tt, Q, T);
+	else if (shape == kDeltaDense)
+		k_delta<DeltaDense><<<blocks, DeltaDense::kWarps * kWarp, delta_smem_bytes<DeltaDense>(), st>>>(tt, Q, T);
 	else
 		k_delta<DeltaWide><<<blocks, DeltaWide::kWarps * kWarp, delta_smem_bytes<DeltaWide>(), st>>>(tt, Q, T);
 }

@@ -53,15 +53,24 @@ struct DeltaQuad {
 	static constexpr int kWarps = 4, kStage = 1536, kChainW = 192, kPrefetch = 128, kMinBlocks = 4;
 	static constexpr bool kPipelined = true, kShortEntry = true;
 };
+// Dense: pipelined, sixteen warps, one block per SM, a 12,288-entry stage,
+// for crowded states where a task's region (the bounding box of its
+// particles' new cells, grown by one) outgrows the other shapes' stages and
+// their tasks would read unstaged from global memory.
+struct DeltaDense {
+	static constexpr int kWarps = 16, kStage = kDeltaDenseStageCap, kChainW = 96, kPrefetch = 128, kMinBlocks = 1;
+	static constexpr bool kPipelined = true, kShortEntry = true;
+};
 // Delta shapes by index (sph_set_sweep_shape names them by warp count).
-constexpr int kDeltaShapes = 5;
-constexpr int kDeltaWide = 0, kDeltaLean = 1, kDeltaMid = 2, kDeltaTri = 3, kDeltaQuad = 4;
+constexpr int kDeltaShapes = 6;
+constexpr int kDeltaWide = 0, kDeltaLean = 1, kDeltaMid = 2, kDeltaTri = 3, kDeltaQuad = 4, kDeltaDense = 5;
 constexpr int delta_shape_warps(int shape) {
-	return shape == kDeltaLean   ? DeltaLean::kWarps
-	       : shape == kDeltaMid  ? DeltaMid::kWarps
-	       : shape == kDeltaTri  ? DeltaTri::kWarps
-	       : shape == kDeltaQuad ? DeltaQuad::kWarps
-	                             : DeltaWide::kWarps;
+	return shape == kDeltaLean    ? DeltaLean::kWarps
+	       : shape == kDeltaMid   ? DeltaMid::kWarps
+	       : shape == kDeltaTri   ? DeltaTri::kWarps
+	       : shape == kDeltaQuad  ? DeltaQuad::kWarps
+	       : shape == kDeltaDense ? DeltaDense::kWarps
+	                              : DeltaWide::kWarps;
 }
 constexpr int kDensWarps = 8;
 constexpr int kViscRefWarps = 4;  // reference-order viscosity sweep: one task per warp
@@ -77,6 +86,16 @@ struct DensWarp;
 // The two ordered sweeps in a chosen shape (lean or wide), and their set-up.
 cudaError_t sweep_attributes();
 cudaError_t sweep_occupancy(bool viscLean, int deltaShape, int *occV, int *occD);
+// Staged entries of a delta-sweep task region in the given shape; larger
+// regions are swept unstaged (from global memory).
+inline int delta_stage_capacity(int shape) {
+	return shape == kDeltaLean    ? DeltaLean::kStage
+	       : shape == kDeltaMid   ? DeltaMid::kStage
+	       : shape == kDeltaTri   ? DeltaTri::kStage
+	       : shape == kDeltaQuad  ? DeltaQuad::kStage
+	       : shape == kDeltaDense ? DeltaDense::kStage
+	                              : DeltaWide::kStage;
+}
 void launch_viscosity(bool lean, int blocks, cudaStream_t st, Totals tt, Particles P, SimTables T);
 void launch_delta(int shape, int blocks, cudaStream_t st, Totals tt, Particles Q, SimTables T);
 size_t dens_smem_bytes();

@@ -126,10 +126,10 @@ class SpringParams(ctypes.Structure):
 
 SPRING_SLOTS = 16
 #: Warps per task of the ordered sweeps' launch shapes, (wide, lean) and for
-#: the delta sweep (wide, lean, mid, tri, quad): the values
+#: the delta sweep (wide, lean, mid, tri, quad, dense): the values
 #: ``sph_set_sweep_shape`` accepts (csrc/sph_kernels.cuh).
 VISC_WARPS = (4, 5)
-DELTA_WARPS = (12, 2, 8, 3, 4)
+DELTA_WARPS = (12, 2, 8, 3, 4, 16)
 
 
 class BodyDesc(ctypes.Structure):
@@ -236,6 +236,8 @@ def load_library(build_if_missing: bool = True):
         "sph_autotune": [vp, _c.c_float, vp],
         "sph_get_sweep_shape": [vp, vp],
         "sph_set_sweep_shape": [vp, vp],
+        "sph_set_adaptive_shapes": [vp, _c.c_int],
+        "sph_last_sweep_shape": [vp, vp],
         "sph_set_springs": [vp, P(SpringParams)],
         "sph_get_spring_count": [vp, P(_c.c_uint64)],
         "sph_dump_springs": [vp, _c.c_size_t, vp, vp, vp],
@@ -289,7 +291,8 @@ C_SYMBOLS = (
     "sph_scenario_describe", "sph_load_scenario", "sph_synchronize",
     "sph_kernel_launches",
     "sph_use_graphs", "sph_autotune", "sph_set_reference_order", "sph_get_reference_order",
-    "sph_set_wait_limit", "sph_test_hold_task", "sph_get_sweep_shape", "sph_set_sweep_shape", "sph_set_springs", "sph_get_spring_count", "sph_dump_springs", "sph_load_springs",
+    "sph_set_wait_limit", "sph_test_hold_task", "sph_get_sweep_shape", "sph_set_sweep_shape",
+    "sph_set_adaptive_shapes", "sph_last_sweep_shape", "sph_set_springs", "sph_get_spring_count", "sph_dump_springs", "sph_load_springs",
     "sph_mpnn_create", "sph_mpnn_destroy", "sph_mpnn_param_count", "sph_mpnn_get_params", "sph_mpnn_set_params",
     "sph_mpnn_set_edge_path", "sph_mpnn_get_edge_path", "sph_mpnn_capture", "sph_mpnn_sample_count", "sph_mpnn_clear_samples", "sph_mpnn_sample_info",
     "sph_mpnn_read_sample", "sph_mpnn_eval", "sph_mpnn_gradient", "sph_mpnn_train_step", "sph_learned_frame",
@@ -610,6 +613,16 @@ class Simulation:
     def set_sweep_shape(self, shape) -> None:
         a = np.ascontiguousarray(shape, np.int32)
         self._call("sph_set_sweep_shape", a.ctypes.data)
+
+    def set_adaptive_shapes(self, enable: bool = True) -> None:
+        """Dense states run the staging-safe sweep shapes (on by default)."""
+        self._call("sph_set_adaptive_shapes", 1 if enable else 0)
+
+    def last_sweep_shape(self) -> Tuple[int, int, int, int]:
+        """The sweep shapes the last update ran with."""
+        shape = np.zeros(4, np.int32)
+        self._call("sph_last_sweep_shape", shape.ctypes.data)
+        return tuple(int(v) for v in shape)
 
     # --- viscoelastic springs (no reference counterpart) ----------------------
     def set_springs(self, enabled: bool = True, yield_ratio: float = 0.1, plasticity: float = 0.3,

@@ -153,6 +153,7 @@ def _run_with_shape(scene, shape, steps):
     scene.apply(sim)
     sim.update(float(scenes.DT))
     if shape is not None:
+        sim.set_adaptive_shapes(False)  # run the shape given, dense or not
         base = sim.sweep_shape()
         sim.set_sweep_shape((shape[0], base[1] if shape[1] is None else shape[1],
                              shape[2], base[3] if shape[3] is None else shape[3]))
@@ -168,10 +169,11 @@ def _run_with_shape(scene, shape, steps):
                                    (VISC_WARPS[0], 152 * 3, DELTA_WARPS[1], 152 * 5),
                                    (VISC_WARPS[0], 152, DELTA_WARPS[2], 304),
                                    (VISC_WARPS[1], 152 * 3, DELTA_WARPS[3], 152 * 5),
-                                   (VISC_WARPS[0], 152, DELTA_WARPS[4], 152 * 4)])
+                                   (VISC_WARPS[0], 152, DELTA_WARPS[4], 152 * 4),
+                                   (VISC_WARPS[0], 152, DELTA_WARPS[5], 152)])
 def test_sweep_shapes_give_identical_results(shape):
-    """Lean, mid and wide sweeps, with any resident block count, compute the
-    same update."""
+    """Lean, mid, tri, quad, wide and dense sweeps, with any resident block
+    count, compute the same update."""
     scene = scenes.scaled_block(64, seed=13)
     want = _run_with_shape(scene, None, 12)
     got = _run_with_shape(scene, shape, 12)
@@ -189,3 +191,5 @@ def test_lean_viscosity_with_long_pair_lists():
     want = _run_with_shape(scene, None, 6)
     got = _run_with_shape(scene, (VISC_WARPS[1], None, DELTA_WARPS[1], None), 6)
     _assert_same_state(got, want, "dense")
+    got = _run_with_shape(scene, (VISC_WARPS[0], None, DELTA_WARPS[5], None), 6)
+    _assert_same_state(got, want, "dense, 16-warp delta")

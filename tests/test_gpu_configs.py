@@ -7,6 +7,8 @@
   (teacher forcing) and compared particle by particle and spring by spring.
 * The 262,144-particle dam break with obstacles (the learned frame's scene),
   plain update, the same way.
+* The 1,048,576-particle block's dense states: adaptive sweep shapes switch
+  to the staging-safe shapes without changing any result.
 
 Gates as in the smaller parity tests: cell arrays identical as ordered id
 sequences, positions and velocities bit-identical (the 1e-5 relative gate is
@@ -105,3 +107,43 @@ def test_dam_break_262144_plain_teacher_forced():
         _check(ostate.compare_step(before, sim.dump_state(), orc.get_state(lists=False)))
     orc.close()
     sim.close()
+
+
+def test_block_1m_dense_states_switch_shapes_and_keep_results():
+    """As the 1,048,576-particle column collapses, its cells crowd (the
+    fullest holds ~150 particles by update 40) and neighbour lists grow past
+    500.  With adaptive shapes on, the updates then run the wide viscosity
+    shape and the 8-warp delta shape with the 4,096-entry stage instead of
+    the tuned lean shapes; the results stay identical, bit for bit, to a
+    twin that keeps the lean shapes throughout."""
+    torch = pytest.importorskip("torch")
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    scene = scenes.block_1m()
+    lean = (5, 3 * sms, 3, 5 * sms)
+    sims = []
+    for adaptive in (True, False):
+        sim = pkg.Simulation(scene.domain())
+        scene.apply(sim)
+        sim.set_springs(True, **SPRINGS)
+        sim.set_sweep_shape(lean)
+        sim.set_adaptive_shapes(adaptive)
+        sims.append(sim)
+    seen = set()
+    for step in range(45):
+        for sim in sims:
+            sim.update(DT)
+        seen.add(sims[0].last_sweep_shape())
+        assert sims[1].last_sweep_shape() == lean
+    st = sims[0].get_stats()
+    assert st.max_cell_particle_count * 9 * 4 > 1536 * 3 and st.max_particle_neighbor_count > 440, (
+        st.max_cell_particle_count, st.max_particle_neighbor_count)
+    last = sims[0].last_sweep_shape()
+    assert lean in seen and last[0] == 4 and last[2] == 8, seen  # wide viscosity, 8-warp delta
+    a, b = sims[0].dump_state(), sims[1].dump_state()
+    for k in ("pos", "prev", "vel", "dens", "press", "id", "cell_start", "cell_count"):
+        assert np.array_equal(a[k], b[k]), k
+    ca, cb = sims[0].dump_springs(), sims[1].dump_springs()
+    for x, y in zip(ca, cb):
+        assert np.array_equal(x, y)
+    for sim in sims:
+        sim.close()
