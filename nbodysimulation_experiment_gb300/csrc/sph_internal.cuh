@@ -34,6 +34,8 @@ constexpr int kMaxPoly = 8;      // kMaxScenarioPolygonCount, sph.h:161
 // Appendix particles (added since the last update) are swept serially in runs
 // of this many consecutive numbers.
 constexpr int kAppendixRun = 32;
+// Pending dependencies a delta-sweep task lists before one warp polls them.
+constexpr int kPendCap = 128;
 // Spring slots per particle (viscoelastic springs, not in the reference).
 constexpr int kSprings = 16;
 

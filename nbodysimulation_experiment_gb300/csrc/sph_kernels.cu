@@ -1615,6 +1615,8 @@ struct DeltaSmemT {
 	int wcnt[C::kWarps];
 	int4 oneSlot, oneLen;  // slots of a particle staged on its own
 	int task;
+	int pend[kPendCap];  // dependencies still pending (wait_canonical)
+	int npend;
 };
 
 namespace {
@@ -1970,9 +1972,12 @@ __device__ __forceinline__ void summer(DeltaSmemT<C> &S, int b, int4 sl, int4 ln
 // inputs (new cell, new number, pressure, list slots) are prefetched in
 // chunks, off the serial path.
 template <class C>
-__device__ __forceinline__ void relax_group(DeltaSmemT<C> &S, int p0, int p1, const int *ord, int bx0, int by0,
-                                            int bx1, int by1, const Particles &Q, const SimTables &T,
-                                            const StepParams &s, int cellBase, int tid) {
+__device__ __forceinline__ unsigned long long relax_group(DeltaSmemT<C> &S, int p0, int p1, const int *ord, int bx0,
+                                                          int by0, int bx1, int by1, const Particles &Q,
+                                                          const SimTables &T, const StepParams &s, int cellBase,
+                                                          int tid) {
+	// Returns when the region was staged (global ns), for the task
+	// timestamps (sph_profile_tasks).
 	constexpr int kDT = C::kWarps * kWarp;
 	constexpr int kP = DeltaSmemT<C>::kProd;
 	const int warp = tid / kWarp, lane = tid & (kWarp - 1);
@@ -1993,6 +1998,7 @@ __device__ __forceinline__ void relax_group(DeltaSmemT<C> &S, int p0, int p1, co
 		pk0 = Q.press[jk0];
 	}
 	const bool staged = stage_region<C>(S, R, Q, T, s, cellBase, tid);
+	const unsigned long long tStaged = global_ns();
 	bool pending = false;  // the previous particle still needs its sum (buffer ph ^ 1)
 	int ph = 0;
 	float2 hres = make_float2(0.0f, 0.0f);  // summer: D/2 of the pending particle's reserved pair
@@ -2058,33 +2064,70 @@ __device__ __forceinline__ void relax_group(DeltaSmemT<C> &S, int p0, int p1, co
 	if (C::kPipelined && pending && warp == kP && lane == 0) finish_particle<C>(S, (ph & 1) ^ 1, hres);
 	__syncthreads();
 	if (staged) write_back_owned<C>(S, R, Q, tid);
+	return tStaged;
 }
 
 // Wait for canonical tasks of the scene (old cells) near [bx0,bx1]x[by0,by1]
 // whose new-cell bounding boxes come within two cells of it and whose task
-// index is below `limit`.  Collective over the block; waits are converged
-// per warp.
+// index is below `limit`.  Collective over the block.  The block first
+// collects the dependencies not yet done (one acquire load each) into
+// `pend`; then warp 0 alone polls them while the other warps wait at the
+// barrier, so a waiting block adds one warp's polling to the memory system
+// rather than every warp's (in crowded states many blocks wait at once, and
+// their polling starved the running tasks' loads).  If more than kPendCap
+// are pending, every warp polls its share of the window as well.
 template <int kDT>
 __device__ __forceinline__ void wait_canonical(int bx0, int by0, int bx1, int by1, int moveMax, int limit,
                                                int selfCell, const SimTables &T, const StepParams &s,
-                                               int cellBase, int tid) {
+                                               int cellBase, int *pend, int *npend, int tid) {
 	const int rad = 2 + moveMax;
 	const int x0 = max(bx0 - rad, 0), x1 = min(bx1 + rad, s.gx - 1);
 	const int y0 = max(by0 - rad, 0), y1 = min(by1 + rad, s.gy - 1);
 	const int w = x1 - x0 + 1;
 	const int total = w * (y1 - y0 + 1);
+	const int lane = tid & (kWarp - 1);
+	if (tid == 0) *npend = 0;
+	__syncthreads();
 	for (int q0 = 0; q0 < total; q0 += kDT) {
 		const int q = q0 + tid;
-		const uint32_t *flag = nullptr;
+		int r = -1;
 		if (q < total) {
 			const int c2 = cellBase + (y0 + q / w) * s.gx + (x0 + q % w);
 			const int r2 = T.taskOfCell[c2];
 			if (c2 != selfCell && r2 < limit && T.cellCount[c2] > 0) {
 				const int4 b = *reinterpret_cast<const int4 *>(&T.bbox[4 * c2]);
-				if (rect_dist(b.x, b.y, b.z, b.w, bx0, by0, bx1, by1) <= 2) flag = &T.done[r2];
+				if (rect_dist(b.x, b.y, b.z, b.w, bx0, by0, bx1, by1) <= 2 && ld_acquire(&T.done[r2]) == 0u) r = r2;
 			}
 		}
-		warp_wait(flag, T.abort, T.error, T.waitLimitNs);
+		const unsigned m = __ballot_sync(kFull, r >= 0);
+		int base = 0;
+		if (lane == 0 && m != 0u) base = atomicAdd(npend, __popc(m));
+		base = __shfl_sync(kFull, base, 0);
+		if (r >= 0) {
+			const int k = base + __popc(m & lanemask_lt());
+			if (k < kPendCap) pend[k] = r;
+		}
+	}
+	__syncthreads();
+	const int np = *npend;
+	if (np > kPendCap) {
+		// Too many to list: every warp polls its share of the window.
+		for (int q0 = 0; q0 < total; q0 += kDT) {
+			const int q = q0 + tid;
+			const uint32_t *flag = nullptr;
+			if (q < total) {
+				const int c2 = cellBase + (y0 + q / w) * s.gx + (x0 + q % w);
+				const int r2 = T.taskOfCell[c2];
+				if (c2 != selfCell && r2 < limit && T.cellCount[c2] > 0) {
+					const int4 b = *reinterpret_cast<const int4 *>(&T.bbox[4 * c2]);
+					if (rect_dist(b.x, b.y, b.z, b.w, bx0, by0, bx1, by1) <= 2) flag = &T.done[r2];
+				}
+			}
+			warp_wait(flag, T.abort, T.error, T.waitLimitNs);
+		}
+	} else if (tid < kWarp) {
+		for (int k0 = 0; k0 < np; k0 += kWarp)
+			warp_wait(k0 + lane < np ? &T.done[pend[k0 + lane]] : nullptr, T.abort, T.error, T.waitLimitNs);
 	}
 	__syncthreads();
 }
@@ -2117,9 +2160,12 @@ __global__ void __launch_bounds__(C::kWarps * kWarp, C::kMinBlocks) k_delta(Tota
 				const SceneDev &sc = T.scenes[T.sceneOfCell[c]];
 				const StepParams s = sc.p;
 				const int4 b = *reinterpret_cast<const int4 *>(&T.bbox[4 * c]);
-				wait_canonical<kDT>(b.x, b.y, b.z, b.w, moveMax, t, c, T, s, sc.cellBase, tid);
+				wait_canonical<kDT>(b.x, b.y, b.z, b.w, moveMax, t, c, T, s, sc.cellBase, S.pend, &S.npend, tid);
 				stamp(T, 1, t, 1, tid);
-				relax_group<C>(S, p0, p0 + cnt, nullptr, b.x, b.y, b.z, b.w, Q, T, s, sc.cellBase, tid);
+				const unsigned long long staged =
+				    relax_group<C>(S, p0, p0 + cnt, nullptr, b.x, b.y, b.z, b.w, Q, T, s, sc.cellBase, tid);
+				if (T.prof != nullptr && tid == 0 && t < T.profStride)
+					T.prof[((size_t)1 * T.profStride + t) * 4 + 2] = staged;
 				__syncthreads();
 				__threadfence();
 			}
@@ -2138,7 +2184,8 @@ __global__ void __launch_bounds__(C::kWarps * kWarp, C::kMinBlocks) k_delta(Tota
 			const int p1 = min(sc.pBase + sc.n, p0 + kAppendixRun);
 			const int4 box = *reinterpret_cast<const int4 *>(&T.appBox[4 * a]);
 			const int bx0 = box.x, by0 = box.y, bx1 = box.z, by1 = box.w;
-			if (!tt.refOrder) wait_canonical<kDT>(bx0, by0, bx1, by1, moveMax, tt.ncell, -1, T, s, base, tid);
+			if (!tt.refOrder)
+				wait_canonical<kDT>(bx0, by0, bx1, by1, moveMax, tt.ncell, -1, T, s, base, S.pend, &S.npend, tid);
 			for (int q0 = 0; q0 < a; q0 += kDT) {
 				const int q = q0 + tid;
 				const uint32_t *flag = nullptr;
