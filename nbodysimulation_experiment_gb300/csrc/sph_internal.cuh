@@ -27,7 +27,8 @@ constexpr int kPrefetch = 128;
 // is 500, sph.h:68).
 constexpr int kCellCap = 512;
 // Cells of a delta-sweep staging region (bounding box of a task's new cells,
-// grown by one).  Larger regions fall back to per-particle staging.
+// grown by one) in the smaller shapes (the 8- and 16-warp shapes take 256
+// and 400).  Larger regions fall back to per-particle staging.
 constexpr int kRegionCells = 100;
 constexpr int kMaxBodies = 100;  // kSPHMaxBodyCount, sph.h:71
 constexpr int kMaxPoly = 8;      // kMaxScenarioPolygonCount, sph.h:161

@@ -1609,9 +1609,9 @@ struct DeltaSmemT {
 	int pnc[C::kPrefetch];     // new cell and new number (per-particle staging only)
 	int pjk[C::kPrefetch];
 	float2 ppk[C::kPrefetch];  // pressure and near pressure
-	int segOff[kRegionCells + 1];
-	int segStart[kRegionCells];
-	int owned[kRegionCells];
+	int segOff[C::kRegion + 1];
+	int segStart[C::kRegion];
+	int owned[C::kRegion];
 	int wcnt[C::kWarps];
 	int4 oneSlot, oneLen;  // slots of a particle staged on its own
 	int task;
@@ -1634,7 +1634,7 @@ __device__ __forceinline__ bool stage_region(DeltaSmemT<C> &S, Region &R, const 
 	constexpr int kDT = C::kWarps * kWarp;
 	R.w = R.x1 - R.x0 + 1;
 	R.ncells = R.w * (R.y1 - R.y0 + 1);
-	if (R.ncells > kRegionCells) return false;
+	if (R.ncells > C::kRegion) return false;
 	if (tid < kWarp) {
 		const int lane = tid;
 		int carry = 0;

@@ -30,16 +30,19 @@ struct ViscLean {
 // than the fewest instructions.
 struct DeltaWide {
 	static constexpr int kWarps = 12, kStage = kDeltaStageCap, kChainW = 96, kPrefetch = 128, kMinBlocks = 1;
+	static constexpr int kRegion = kRegionCells;
 	static constexpr bool kPipelined = true, kShortEntry = true;
 };
 struct DeltaLean {
 	static constexpr int kWarps = 2, kStage = 1536, kChainW = 192, kPrefetch = 64, kMinBlocks = 8;
+	static constexpr int kRegion = kRegionCells;
 	static constexpr bool kPipelined = false, kShortEntry = false;
 };
 // Mid: pipelined, eight warps, two blocks per SM (mid-size scenes, where
 // more tasks run at once than one block per SM holds).
 struct DeltaMid {
 	static constexpr int kWarps = 8, kStage = kDeltaStageCap, kChainW = 128, kPrefetch = 128, kMinBlocks = 2;
+	static constexpr int kRegion = 256;
 	static constexpr bool kPipelined = true, kShortEntry = true;
 };
 // Small pipelined shapes for large scenes, where the sweep is bound by how
@@ -47,10 +50,12 @@ struct DeltaMid {
 // three (quad) producer warps and the summer warp, several blocks per SM.
 struct DeltaTri {
 	static constexpr int kWarps = 3, kStage = 1536, kChainW = 256, kPrefetch = 64, kMinBlocks = 5;
+	static constexpr int kRegion = kRegionCells;
 	static constexpr bool kPipelined = true, kShortEntry = true;
 };
 struct DeltaQuad {
 	static constexpr int kWarps = 4, kStage = 1536, kChainW = 192, kPrefetch = 128, kMinBlocks = 4;
+	static constexpr int kRegion = kRegionCells;
 	static constexpr bool kPipelined = true, kShortEntry = true;
 };
 // Dense: pipelined, sixteen warps, one block per SM, a 12,288-entry stage,
@@ -59,6 +64,7 @@ struct DeltaQuad {
 // their tasks would read unstaged from global memory.
 struct DeltaDense {
 	static constexpr int kWarps = 16, kStage = kDeltaDenseStageCap, kChainW = 96, kPrefetch = 128, kMinBlocks = 1;
+	static constexpr int kRegion = 400;
 	static constexpr bool kPipelined = true, kShortEntry = true;
 };
 // Delta shapes by index (sph_set_sweep_shape names them by warp count).
