@@ -9,6 +9,7 @@ inputs larger than L2 but a few hundred MB on the device at most).
     python profile_cases.py learned_frame
     python profile_cases.py learned_dam    # 262,144-particle dam break, learned frames
     python profile_cases.py block [side]   # side x side block, springs on, lean sweep shapes
+    python profile_cases.py dense_shapes   # the shapes taken in dense states
     python profile_cases.py all            # every kernel of the library, small sizes
 """
 from __future__ import annotations
@@ -132,12 +133,31 @@ def block(side: int = 512, updates: int = 3) -> None:
     sim.close()
 
 
+def dense_shapes(side: int = 256, updates: int = 2) -> None:
+    """A side x side block with springs on in the shapes the library takes
+    for dense states (wide viscosity, 16-warp delta), after 3 updates."""
+    scene = scenes.scaled_block(side, seed=5, obstacles=False)
+    sim = Simulation(scene.domain())
+    scene.apply(sim)
+    sim.set_springs(True, yield_ratio=0.1, plasticity=0.3, stiffness=0.3, max_per_particle=16)
+    for _ in range(3):
+        sim.update(float(scenes.DT))
+    sms = sim.sweep_shape()[3]  # the default delta shape runs one block per SM
+    sim.set_adaptive_shapes(False)
+    sim.set_sweep_shape((VISC_WARPS[0], 4 * sms, DELTA_WARPS[5], sms))
+    for _ in range(updates):
+        sim.update(float(scenes.DT))
+    sim.synchronize()
+    sim.close()
+
+
 def everything() -> None:
     """Every kernel the library launches, on small cases: the plain step
     (wide shapes), the springs block (lean shapes), training steps, learned
     frames, a small batch and the host-facing reads."""
     plain(updates=2, warm=4)
     block(side=512, updates=2)
+    dense_shapes(side=256, updates=2)
     mpnn(steps=2)
     learned_frame(frames=2)
     batched(updates=2)
@@ -173,7 +193,8 @@ def everything() -> None:
 
 
 CASES = {"plain": plain, "springs": springs, "mpnn": mpnn, "batched": batched, "learned_frame": learned_frame,
-         "learned_dam": learned_dam, "block": block, "all": everything}
+         "learned_dam": learned_dam, "block": block,
+         "dense_shapes": dense_shapes, "all": everything}
 
 if __name__ == "__main__":
     CASES[sys.argv[1]](*[int(a) for a in sys.argv[2:]])
