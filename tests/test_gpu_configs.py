@@ -135,10 +135,10 @@ def test_block_1m_dense_states_switch_shapes_and_keep_results():
         seen.add(sims[0].last_sweep_shape())
         assert sims[1].last_sweep_shape() == lean
     st = sims[0].get_stats()
-    assert st.max_cell_particle_count * 9 * 4 > 1536 * 3 and st.max_particle_neighbor_count > 440, (
+    assert st.max_cell_particle_count * 9 * 2 > 1536 and st.max_particle_neighbor_count > 440, (
         st.max_cell_particle_count, st.max_particle_neighbor_count)
     last = sims[0].last_sweep_shape()
-    assert lean in seen and last[0] == 4 and last[2] == 8, seen  # wide viscosity, 8-warp delta
+    assert lean in seen and last[0] == 4 and last[2] in (8, 16), seen  # wide viscosity, 8- or 16-warp delta
     a, b = sims[0].dump_state(), sims[1].dump_state()
     for k in ("pos", "prev", "vel", "dens", "press", "id", "cell_start", "cell_count"):
         assert np.array_equal(a[k], b[k]), k
