@@ -264,21 +264,46 @@ def run_reference_arm(args):
                           "memory; %.0f GB available" % (scene.n, need, host_memory_gb())}), flush=True)
         return 0
     workers = OracleSim.hardware_threads()
-    orc = OracleSim(scene.oracle_domain(OracleSim), fp64=False, workers=workers)
-    scene.apply(orc)
-    if springs:
-        orc.set_springs(True, **SPRINGS)
     dt = float(scenes.DT)
-    orc.update(dt)  # first update (AddParticle order)
-    per = max(1, args.cpu_steps // max(1, args.steps)) if args.workload != HEADLINE else 1
-    for _ in range(args.warmup):
+    restart_after = RESTART_AFTER.get(args.workload)
+
+    def fresh():
+        # The scene from its start: the first update in AddParticle order,
+        # then two more (the GPU arm's snapshot point).
+        o = OracleSim(scene.oracle_domain(OracleSim), fp64=False, workers=workers)
+        scene.apply(o)
+        if springs:
+            o.set_springs(True, **SPRINGS)
+        for _ in range(3):
+            o.update(dt)
+        return o
+
+    orc = fresh()
+    done, restarts = 3, 0
+    per = max(1, args.cpu_steps // max(1, args.steps)) if args.workload not in RESTART_AFTER else 1
+
+    def restart_if_due():
+        # The same window as the GPU arm: the scene restarts (outside the
+        # timed region) before it outgrows the reference's capacities.
+        nonlocal orc, done, restarts
+        if restart_after is not None and done >= restart_after:
+            orc.close()
+            orc = fresh()
+            done = 3
+            restarts += 1
+
+    for _ in range(max(0, args.warmup - 3)):
+        restart_if_due()
         orc.update(dt)
+        done += 1
     times = []
     for _ in range(args.steps):
+        restart_if_due()
         t0 = time.perf_counter()
         for _ in range(per):
             orc.update(dt)
         times.append(time.perf_counter() - t0)
+        done += per
     orc.close()
     total = sum(times)
     value = scene.n * per * args.steps / total
@@ -289,7 +314,10 @@ def run_reference_arm(args):
         "data": "synthetic (seeded)", "config": {"workload": desc, "particles": scene.n, "springs": springs},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": workers, "kind": "port",
                          "sample": "%d update(s) of the %d-particle scene per step, %d steps, after %d warm-up "
-                                   "updates from the scene's start" % (per, scene.n, args.steps, args.warmup + 1)},
+                                   "updates from the scene's start%s" % (
+                                       per, scene.n, args.steps, max(3, args.warmup),
+                                       "; restarted from update 3 before update %d (%d restarts), as the GPU arm"
+                                       % (restart_after, restarts) if restart_after is not None else "")},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
