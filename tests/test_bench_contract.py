@@ -22,3 +22,19 @@ def test_reference_arm_prints_one_contract_line():
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
     assert "obstacles_65536" in d["config"]["workload"]
+
+
+def test_reference_arm_restarts_like_the_gpu_arm(monkeypatch, capsys):
+    """A workload with a restart period (the collapsing 1M column's lines
+    restart before it outgrows the reference's capacities) restarts the CPU
+    scene the same way, outside the timed updates; exercised here on the
+    65,536-particle scene with a short period."""
+    sys.path.insert(0, ROOT)
+    import bench
+    monkeypatch.setattr(bench, "RESTART_AFTER", {"obstacles_65536": 4})
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--workload", "obstacles_65536",
+                                      "--steps", "3", "--warmup", "3"])
+    assert bench.main() == 0
+    line = json.loads([ln for ln in capsys.readouterr().out.splitlines() if ln.startswith("{")][-1])
+    assert line["steps"] == 3 and line["value"] > 0
+    assert "restarted from update 3 before update 4 (2 restarts)" in line["cpu_baseline"]["sample"]
