@@ -426,6 +426,7 @@ def measure_scene(torch, pkg, workload: str, device: int, steps: int, warmup: in
     spring_count = sim.spring_count() if springs else None
 
     # --- end to end through the C ABI with host buffers ---------------------
+    e2e_from = done
     st = sim.dump_state()
     pinned = pinned_like(torch, {k: st[k] for k in STATE_KEYS})
     pinned["canonical_count"] = st["canonical_count"]
@@ -480,7 +481,9 @@ def measure_scene(torch, pkg, workload: str, device: int, steps: int, warmup: in
                             "(sph.h:69) after ~110 updates; the scene is reloaded from its update-3 state, "
                             "outside the timed region"} if restart_after is not None else None,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(h2d),
-                "steps": e2e_steps},
+                "steps": e2e_steps,
+                "state": "the state after update %d (the last timed one), loaded from pinned host memory every "
+                         "step" % e2e_from},
         "roofline": {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": profile_traffic(kern, scene.n),
                      "algorithmic_bytes": alg, "kernel_ms": kms,
