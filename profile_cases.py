@@ -10,6 +10,7 @@ inputs larger than L2 but a few hundred MB on the device at most).
     python profile_cases.py learned_dam    # 262,144-particle dam break, learned frames
     python profile_cases.py block [side]   # side x side block, springs on, lean sweep shapes
     python profile_cases.py dense_shapes   # the shapes taken in dense states
+    python profile_cases.py dense_tasks    # delta-sweep task timestamps at update 91 of the 1M collapse
     python profile_cases.py all            # every kernel of the library, small sizes
 """
 from __future__ import annotations
@@ -151,6 +152,57 @@ def dense_shapes(side: int = 256, updates: int = 2) -> None:
     sim.close()
 
 
+def dense_tasks(update: int = 91) -> None:
+    """Task timestamps (sph_profile_tasks) of the delta sweep on the
+    1,048,576-particle block with springs at the given update of its collapse,
+    in the shapes the library picks there, under the full grid and with a
+    single block (the same tasks one after another): sweep time, total task
+    time, time spent staging, and the slowest tasks."""
+    import ctypes
+    import json
+    import numpy as np
+    from nbodysimulation_experiment_gb300 import simulation as sm
+    lib = sm.load_library()
+    lib.sph_profile_tasks.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.sph_profile_read.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                     ctypes.POINTER(ctypes.c_size_t)]
+    scene = scenes.block_1m()
+    sim = Simulation(scene.domain())
+    scene.apply(sim)
+    sim.set_springs(True, yield_ratio=0.1, plasticity=0.3, stiffness=0.3, max_per_particle=16)
+    for k in range(update):
+        if k == 5:
+            sim.autotune(float(scenes.DT))
+        sim.update(float(scenes.DT))
+    shape = sim.last_sweep_shape()
+    st0, sp0 = sim.dump_state(), sim.dump_springs()
+    sim.set_adaptive_shapes(False)
+    out = {"update": update, "shape": list(shape)}
+    for label, blocks in (("full_grid", shape[3]), ("one_block", 1)):
+        sim.load_state(st0)
+        sim.load_springs(*sp0)
+        sim.set_sweep_shape((shape[0], shape[1], shape[2], blocks))
+        lib.sph_profile_tasks(sim._h, 1)
+        sim.update(float(scenes.DT))
+        sim.synchronize()
+        stride = ctypes.c_size_t()
+        lib.sph_profile_read(sim._h, None, 0, ctypes.byref(stride))
+        buf = np.zeros(8 * stride.value, np.uint64)
+        lib.sph_profile_read(sim._h, buf.ctypes.data, buf.size, ctypes.byref(stride))
+        lib.sph_profile_tasks(sim._h, 0)
+        a = buf[4 * stride.value:8 * stride.value].reshape(-1, 4).astype(np.float64)  # the delta sweep
+        a = a[a[:, 3] > 0]
+        ready = np.where(a[:, 1] > 0, a[:, 1], a[:, 0])
+        run, stage = (a[:, 3] - ready) / 1e3, (a[:, 2] - ready) / 1e3
+        span = (a[:, 3].max() - a[:, 0].min()) / 1e3
+        out[label] = {"delta_ms": sim.get_stats().time_delta_positions, "tasks": int(len(a)),
+                      "task_time_s": float(run.sum() / 1e6), "staging_s": float(stage.sum() / 1e6),
+                      "tasks_in_flight": float(run.sum() / span),
+                      "slowest_tasks_us": [round(float(x), 1) for x in np.sort(run)[-5:][::-1]]}
+    print(json.dumps(out))
+    sim.close()
+
+
 def everything() -> None:
     """Every kernel the library launches, on small cases: the plain step
     (wide shapes), the springs block (lean shapes), training steps, learned
@@ -194,7 +246,7 @@ def everything() -> None:
 
 CASES = {"plain": plain, "springs": springs, "mpnn": mpnn, "batched": batched, "learned_frame": learned_frame,
          "learned_dam": learned_dam, "block": block,
-         "dense_shapes": dense_shapes, "all": everything}
+         "dense_shapes": dense_shapes, "dense_tasks": dense_tasks, "all": everything}
 
 if __name__ == "__main__":
     CASES[sys.argv[1]](*[int(a) for a in sys.argv[2:]])
