@@ -334,7 +334,7 @@ int sph_set_sweep_shape(sph_sim *sim, const int *shape);
 /* Dense states.  With adaptive shapes on (the default), an update whose
  * previous updates saw neighbour lists longer than 440 runs the wide
  * viscosity shape, and one where a 3x3 block of the fullest cell's count
- * passes half the tuned delta shape's stage runs the 8-warp delta shape
+ * passes 0.65 of the tuned delta shape's stage runs the 8-warp delta shape
  * (4,096 staged entries), or the 16-warp shape (12,288) once a 5x5 region
  * of it nears 4,096, instead of the tuned shapes (results are identical in
  * every shape; only the launch differs).  Single-scene simulations only: a

@@ -596,7 +596,7 @@ constexpr uint32_t kDenseNeighbors = 440;
 // The sweep shapes of the next update: the tuned ones, or in dense states
 // (see sph_sim::adaptive) the wide viscosity shape and a delta shape whose
 // stage holds the task regions: the 8-warp shape (4,096 entries) once a 3x3
-// block of the fullest cell passes half the tuned shape's stage, the
+// block of the fullest cell passes 0.65 of the tuned shape's stage, the
 // 16-warp shape (12,288 entries) once a 5x5 region of it nears 4,096.  The statistics are those of the update
 // before last at the latest: the host waits for its copy, so it never runs
 // more than two updates ahead.  Changing shapes drops the update graphs.
@@ -620,10 +620,10 @@ void choose_shapes(sph_sim *s) {
 		const uint32_t block = 9 * maxCell;   // a 3x3 block at the fullest cell's count
 		const uint32_t spread = 25 * maxCell;  // a 5x5 region: a cell's particles spread over 3x3 new cells
 		// Thresholds from measured crossovers on the collapsing 1M column:
-		// the 8-warp shape wins from ~90 particles in the fullest cell (a
-		// 3x3 block at half the 1,536-entry stage), the 16-warp one from
+		// the 8-warp shape wins from ~110 particles in the fullest cell (a
+		// 3x3 block at 0.65 of the 1,536-entry stage), the 16-warp one from
 		// ~160 (a 5x5 region near 4,096).
-		s->denseDelta = s->denseDelta ? block * 5 > cap * 2 : block * 2 > cap;
+		s->denseDelta = s->denseDelta ? block * 2 > cap : block * 20 > cap * 13;
 		s->crowdedDelta =
 		    s->crowdedDelta ? spread * 5 > (uint32_t)kDeltaStageCap * 4 : spread * 20 > (uint32_t)kDeltaStageCap * 19;
 		if (vl && s->denseVisc) {
