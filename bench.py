@@ -703,7 +703,7 @@ def bench_learned(torch, pkg, scenes, device: int, args):
             "quality": quality, "particles": n,
             "workload": "dam_break_262144: 512x512 jittered block, 102.4 x 57.6 box, 4 walls + 8 circles + "
                         "4 segments; 2-round MPNN (edge 6-128-128, node 130-128-2; edge layer on tcgen05 "
-                        "kind::tf32 + kind::f16 MMAs, dense layers BF16 tcgen05 GEMMs)",
+                        "kind::tf32 MMAs, dense layers persistent BF16 tcgen05 GEMMs)",
             "train": {"samples": ntrain, "scenes": args.learned_scenes, "frames_per_scene": args.learned_frames,
                       "scene": "obstacles_65536 seeds 1000..", "steps": args.learned_steps,
                       "collect_s": t_collect, "train_s": t_train, "final_loss": float(np.mean(losses[-50:])),

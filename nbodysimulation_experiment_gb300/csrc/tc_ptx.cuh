@@ -67,52 +67,12 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, uint32_t pari
 	return false;
 }
 
-__device__ __forceinline__ void mbar_arrive(unsigned long long *bar) {
-	asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-
-// Named barrier `id` over `count` threads (a multiple of 32); returns
-// whether any of them passed `pred` true.
-__device__ __forceinline__ bool bar_or(int id, int count, bool pred) {
-	uint32_t r;
-	asm volatile(
-	    "{\n\t.reg .pred p, q;\n\t"
-	    "setp.ne.u32 p, %1, 0;\n\t"
-	    "barrier.red.or.pred q, %2, %3, p;\n\t"
-	    "selp.u32 %0, 1, 0, q;\n\t}"
-	    : "=r"(r)
-	    : "r"((uint32_t)pred), "r"(id), "r"(count)
-	    : "memory");
-	return r != 0;
-}
-
-__device__ __forceinline__ void bar_sync(int id, int count) {
-	asm volatile("barrier.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
-}
-
 __device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc, bool acc) {
 	asm volatile(
 	    "{\n\t.reg .pred p;\n\t"
 	    "setp.ne.u32 p, %4, 0;\n\t"
 	    "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
 	    "l"(a), "l"(b), "r"(idesc), "r"((uint32_t)acc)
-	    : "memory");
-}
-
-// Instruction descriptor of kind::f16 with BF16 A and B (bits 7-9 and
-// 10-12 = 1), FP32 accumulator, both K-major.
-__device__ __forceinline__ uint32_t idesc_bf16(int m, int n) {
-	return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
-}
-
-// D (+)= A B^T with A (M x 16, BF16, two per 32-bit column, lower K in the
-// lower half) in tensor memory and B from a shared-memory descriptor.
-__device__ __forceinline__ void mma_bf16_tmem_a(uint32_t tmem, uint32_t a, uint64_t b, uint32_t idesc, bool acc) {
-	asm volatile(
-	    "{\n\t.reg .pred p;\n\t"
-	    "setp.ne.u32 p, %4, 0;\n\t"
-	    "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(tmem),
-	    "r"(a), "l"(b), "r"(idesc), "r"((uint32_t)acc)
 	    : "memory");
 }
 
@@ -137,17 +97,8 @@ __device__ __forceinline__ void tmem_free(uint32_t tmem, uint32_t cols) {
 	asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(cols) : "memory");
 }
 
-// 32 lanes x 16 consecutive 32-bit columns: thread t of the warp receives
-// lane (base lane + t), columns [col, col + 16).
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
-	asm volatile(
-	    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-	    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
-	      "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-	    : "r"(taddr)
-	    : "memory");
-}
-
+// 32 lanes x 32 consecutive 32-bit columns: thread t of the warp receives
+// lane (base lane + t), columns [col, col + 32).
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
 	asm volatile(
 	    "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
@@ -158,31 +109,6 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
 	      "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
 	    : "r"(taddr)
 	    : "memory");
-}
-
-// 32 lanes x 16 (x8) consecutive 32-bit columns from registers.
-__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&v)[16]) {
-	asm volatile(
-	    "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
-	        taddr),
-	    "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]), "r"(v[9]),
-	    "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15])
-	    : "memory");
-}
-
-__device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t (&v)[8]) {
-	asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr), "r"(v[0]),
-	             "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7])
-	             : "memory");
-}
-
-__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
-
-// relu, rounded to BF16 (nearest even), packed: lo in the lower half.
-__device__ __forceinline__ uint32_t relu_bf16x2(uint32_t lo, uint32_t hi) {
-	uint32_t d;
-	asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(__uint_as_float(hi)), "f"(__uint_as_float(lo)));
-	return d;
 }
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
