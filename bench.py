@@ -364,16 +364,16 @@ def measure_scene(torch, pkg, workload: str, device: int, steps: int, warmup: in
     for _ in range(3):
         sim.update(dt)
         done += 1
-    snap = sim.dump_state()
-    snap_springs = sim.dump_springs() if springs else None
+    restart_state = sim.dump_state()
+    restart_springs = sim.dump_springs() if springs else None
     restarts = 0
 
     def restart_if_due():
         nonlocal done, restarts
         if restart_after is not None and done >= restart_after:
-            sim.load_state(snap)
+            sim.load_state(restart_state)
             if springs:
-                sim.load_springs(*snap_springs)
+                sim.load_springs(*restart_springs)
             done = 3
             restarts += 1
 
@@ -394,7 +394,12 @@ def measure_scene(torch, pkg, workload: str, device: int, steps: int, warmup: in
     torch.cuda.synchronize()
     step_ms = []
     stage_sum = dict.fromkeys(STAGES, 0.0)
-    for _ in range(steps):
+    # States for the end-to-end part, spread over the timed window (taken
+    # after the step's events, outside the timed region).
+    n_e2e_states = min(4, steps)
+    e2e_at = {(steps * (q + 1)) // n_e2e_states - 1 for q in range(n_e2e_states)}
+    e2e_states = []
+    for k in range(steps):
         restart_if_due()
         with torch.cuda.stream(stream):
             flush.zero_()
@@ -408,8 +413,17 @@ def measure_scene(torch, pkg, workload: str, device: int, steps: int, warmup: in
         done += 1
         step_ms.append(e0.elapsed_time(e1))
         stats = sim.get_stats()
-        for k in STAGES:
-            stage_sum[k] += getattr(stats, k)
+        for key in STAGES:
+            stage_sum[key] += getattr(stats, key)
+        if k in e2e_at:
+            st = sim.dump_state()
+            host = pinned_like(torch, {key: st[key] for key in STATE_KEYS})
+            host["canonical_count"] = st["canonical_count"]
+            host["grid"] = st["grid"]
+            if springs:
+                cnt, part, rest = sim.dump_springs()
+                host["springs"] = pinned_like(torch, {"count": cnt, "partner": part, "rest": rest})
+            e2e_states.append((done, host))
     torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
@@ -426,32 +440,42 @@ def measure_scene(torch, pkg, workload: str, device: int, steps: int, warmup: in
     spring_count = sim.spring_count() if springs else None
 
     # --- end to end through the C ABI with host buffers ---------------------
-    e2e_from = done
-    st = sim.dump_state()
-    pinned = pinned_like(torch, {k: st[k] for k in STATE_KEYS})
-    pinned["canonical_count"] = st["canonical_count"]
-    pinned["grid"] = st["grid"]
-    pinned_out = pinned_like(torch, {k: st[k] for k in STATE_KEYS})
-    h2d = sum(pinned[k].nbytes for k in STATE_KEYS)
-    spr_in = spr_out = None
+    # Every step loads one of the window's states from pinned host memory,
+    # updates it and reads it back; each state takes an equal share of the
+    # steps, after two untimed steps that let the sweep shapes settle on it.
+    e2e_from = [u for u, _ in e2e_states]
+    first = e2e_states[0][1]
+    host_out = pinned_like(torch, {key: first[key] for key in STATE_KEYS})
+    h2d = sum(first[key].nbytes for key in STATE_KEYS)
+    springs_out = None
     if springs:
-        cnt, part, rest = sim.dump_springs()
-        spr_in = pinned_like(torch, {"count": cnt, "partner": part, "rest": rest})
-        spr_out = pinned_like(torch, {"count": cnt, "partner": part, "rest": rest})
-        h2d += sum(a.nbytes for a in spr_in.values())
-    torch.cuda.synchronize()
+        springs_out = pinned_like(torch, dict(first["springs"]))
+        h2d += sum(a.nbytes for a in first["springs"].values())
+
+    def e2e_step(host):
+        sim.load_state(host)
+        if springs:
+            sp = host["springs"]
+            sim.load_springs(sp["count"], sp["partner"], sp["rest"])
+        sim.update(dt)
+        sim.dump_state(out=host_out)
+        if springs:
+            sim.dump_springs(out=springs_out)
+
+    per_state = max(1, -(-e2e_steps // len(e2e_states)))
+    e2e_local = 0.0
+    for _, host in e2e_states:
+        for _ in range(2):
+            e2e_step(host)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(per_state):
+            e2e_step(host)
+        e2e_local += time.perf_counter() - t0
+    e2e_steps = per_state * len(e2e_states)
     if world > 1:
         dist.barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        sim.load_state(pinned)
-        if springs:
-            sim.load_springs(spr_in["count"], spr_in["partner"], spr_in["rest"])
-        sim.update(dt)
-        sim.dump_state(out=pinned_out)
-        if springs:
-            sim.dump_springs(out=spr_out)
-    e2e_s = job_seconds(time.perf_counter() - t0, world, "cuda")
+    e2e_s = job_seconds(e2e_local, world, "cuda")
     e2e_value = job_rate(scene.n, e2e_steps, world, e2e_s)
     sim.close()
 
@@ -482,8 +506,9 @@ def measure_scene(torch, pkg, workload: str, device: int, steps: int, warmup: in
                             "outside the timed region"} if restart_after is not None else None,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(h2d),
                 "steps": e2e_steps,
-                "state": "the state after update %d (the last timed one), loaded from pinned host memory every "
-                         "step" % e2e_from},
+                "states": "the states after updates %s of the timed window, an equal share of the steps each "
+                          "(after two untimed steps per state), loaded from pinned host memory every step"
+                          % ", ".join(str(u) for u in e2e_from)},
         "roofline": {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": profile_traffic(kern, scene.n),
                      "algorithmic_bytes": alg, "kernel_ms": kms,

@@ -60,9 +60,9 @@ int sph_mpnn_set_params(sph_mpnn *model, const float *in);
  * edges) runs in the forward pass: path 0 (default) on the tensor cores
  * (per tile of 128 edges one kind::tf32 MMA computes W1 e + b1 for every
  * edge into tensor memory; the ReLU and the per-particle sums are read out
- * of it with packed FP32 adds, in a pipeline of producer warps building the
- * tiles, an MMA thread and epilogue warps), path 1 on the CUDA cores (FP32
- * FMAs).  Both round the edge features, W1 and b1 to TF32, so they compute
+ * of it with packed FP32 adds; four CTAs per SM share its tensor memory and
+ * overlap one another's building, MMA and read-out phases), path 1 on the
+ * CUDA cores (FP32 FMAs).  Both round the edge features, W1 and b1 to TF32, so they compute
  * the same function up to summation order. */
 int sph_mpnn_set_edge_path(sph_mpnn *model, int path);
 int sph_mpnn_get_edge_path(sph_mpnn *model, int *path);
