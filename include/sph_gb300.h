@@ -283,12 +283,14 @@ int sph_use_graphs(sph_sim *sim, int enable);
 /* No counterpart in the reference.  Launch shapes of the two ordered sweeps
  * (viscosity, delta): shape[4] = {viscosity warps per block (4 = wide,
  * 5 = lean), viscosity blocks, delta warps per block (12 = wide, 8 = mid,
- * 4 = quad, 3 = tri, 2 = lean), delta blocks}.  The wide shapes shorten one
- * scene's critical path: one task per block; the wide viscosity sweep runs
- * each particle's head beside the previous particle's tail on two lanes; the
- * wide, mid, quad and tri delta sweeps overlap each particle's ordered sum
- * with the next particle's pairs (11, 7, 3 and 2 producer warps beside one
- * summer warp; mid, quad and tri run several blocks per SM).  The lean ones
+ * 4 = quad, 3 = tri, 2 = lean, 16 = dense), delta blocks}.  The wide shapes
+ * shorten one scene's critical path: one task per block; the wide viscosity
+ * sweep runs each particle's head beside the previous particle's tail on two
+ * lanes; the wide, mid, quad, tri and dense delta sweeps overlap each
+ * particle's ordered sum with the next particle's pairs (11, 7, 3, 2 and 15
+ * producer warps beside one summer warp; mid, quad and tri run several
+ * blocks per SM; dense stages 12,288 entries per task, for crowded
+ * states).  The lean ones
  * fit more tasks on an SM (the lean viscosity sweep runs five tasks per
  * block) for large scenes and many scenes.  Results do not depend on the
  * shape.  sph_autotune times the
