@@ -3,6 +3,7 @@ restates them, against the reference's own table and loader steps
 (app.cpp:477-534) compiled into the oracle harness: every call's arguments
 must be identical, bit for bit.  No GPU needed."""
 import ctypes
+import numpy as np
 
 import pytest
 
@@ -53,3 +54,37 @@ def test_describe_rejects_bad_indices():
     for k in (-1, 8):
         with pytest.raises(simulation.SphError):
             simulation.scenario_describe(k)
+
+
+@pytest.mark.parametrize("index", range(8))
+def test_restatement_runs_every_scenario_like_the_reference(reference, index):
+    """Free runs of each built-in scenario, loaded by the same calls into the
+    reference's own solver and into the restatement (FP32, one worker), with
+    the C library's rand() seeded alike before loading and before every
+    update (emitters, volume jitter): identical particles, cell arrays and
+    statistics after every update, neighbour lists at the first and last."""
+    from oracle.oracle import OracleSim, ReferenceSim
+    from oracle.scenario_calls import load_description
+    from nbodysimulation_experiment_gb300 import scenes
+    d = simulation.scenario_describe(index)
+    ref = ReferenceSim(multithreading=False)
+    orc = OracleSim()
+    for sim in (ref, orc):
+        sim.srand(4242 + index)
+        load_description(sim, d)
+    assert ref.particle_count() == orc.particle_count()
+    steps = 20
+    for step in range(steps):
+        for sim in (ref, orc):
+            sim.srand(77 + step)
+            sim.update(float(scenes.DT))
+        lists = step in (0, steps - 1)
+        a, b = ref.get_state(lists=lists), orc.get_state(lists=lists)
+        assert len(a["pos"]) == len(b["pos"]), (d.name, step)
+        for k in ("pos", "prev", "vel", "dens", "press"):
+            assert np.array_equal(a[k], b[k]), (d.name, step, k)
+        assert np.array_equal(a["cell_flat"], b["cell_flat"]), (d.name, step)
+        if lists:
+            assert np.array_equal(a["nb_flat"], b["nb_flat"]), (d.name, step)
+        assert np.array_equal(ref.get_stats()[0], orc.get_stats()[0]), (d.name, step)
+    assert ref.particle_count() > 0 or d.emitter_count == 0, d.name
